@@ -1,0 +1,260 @@
+"""Benchmark: H.v throughput (GB/s of algorithmic bytes) on the N=32 Kitaev-Heisenberg honeycomb.
+
+Workload (the configuration the headline metric is quoted on): 4x4 unit cells (Lx=4, Ly=8),
+N=32 sites, 2^32 states, K=-1, J=0.05, h=0.02 along [111], complex64 vectors (mixed precision:
+FP32 arithmetic on complex64 storage, FP64 reductions).  One step = one H.v over the full 2^32
+basis (34.4 GB in, 34.4 GB out) with the inputs resident in HBM.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--sites 32]
+
+Prints ONE JSON line (rank 0).  Fields beyond the contract: roofline (dominant kernel vs the
+measured HBM copy peak), cpu_baseline (the CPU oracle's matrix-free H.v on a bounded row-slab of
+the same operator, all host threads), e2e (the same step through esc_hv with host buffers:
+host->device copy, H.v, device->host copy inside the timed region), clocks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+S3 = 3 ** 0.5
+METRIC = "H·v GB/s and time-to-S(ω) at N=32: batched mixed vs FP64 GPU at ≤1e-6 error"
+
+
+def workload(sites):
+    shapes = {32: (4, 8), 30: (5, 6), 28: (7, 4), 24: (3, 8), 20: (5, 4), 18: (3, 6), 16: (4, 4), 12: (3, 4)}
+    Lx, Ly = shapes[sites]
+    hf, J = 0.02, 0.05
+    b = -hf / S3
+    return dict(Lx=Lx, Ly=Ly, Kxx=-1.0, Kyy=-1.0, Kzz=-1.0, Bxx=b, Byy=b, Bzz=b, jheis=J, seed=1)
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """DRAM bytes per H.v launch from the committed ncu summary, or None."""
+    p = os.path.join(REPO, "profiles", "hv_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+class Clocks:
+    """Samples nvidia-smi during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if len(s) > 2 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 2 and s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples if len(s) >= 9 for i in range(4) if s[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_baseline(params, sites, target_s=12.0, kind="port"):
+    """The oracle's matrix-free H.v (OpenMP, all host threads) on rows [0, R) of the same operator.
+
+    The input vector is a lazily-zeroed 2^N complex64 array in which only the index ranges that
+    rows [0, R) read (k ^ mask for every term mask) are filled with data."""
+    import numpy as np
+    import oracle as O
+    m = O.Model("Kitaev", params["Lx"], params["Ly"], 1, 1, params["Kxx"], params["Kyy"], params["Kzz"],
+                params["Bxx"], params["Byy"], params["Bzz"], params["jheis"], os.cpu_count(), False)
+    D = m.D
+    rbits = min(sites, 24)
+    R = 1 << rbits
+    v = np.zeros(D, dtype=np.complex64)
+    masks = {0}
+    nb = O.lattice("Kitaev", params["Lx"], params["Ly"])
+    for i in range(m.N):
+        masks.add(1 << i)
+        for j in nb[i]:
+            masks.add((1 << i) | (1 << int(j)))
+    rng = np.random.default_rng(0)
+    fill = (rng.standard_normal(R) + 1j * rng.standard_normal(R)).astype(np.complex64)
+    for hi in sorted({mk & ~(R - 1) for mk in masks}):
+        v[hi:hi + R] = fill
+    threads = os.cpu_count()
+    m.hv_rows(v, 0, R, threads, c64=True)         # warm-up
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        m.hv_rows(v, 0, R, threads, c64=True)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > target_s or reps >= 200:
+            break
+    gbs = reps * R * 16 / el / 1e9
+    return {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": kind,
+            "sample": f"rows [0, 2^{rbits}) of the N={sites} H.v, {reps} passes in {el:.1f} s, complex64, "
+                      f"oracle matrix-free gather (oracle/esc_oracle.cpp hv_matfree)"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    params = workload(args.sites)
+    cb = cpu_baseline(params, args.sites, target_s=max(3.0, 2.0 * args.steps))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "GB/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": {"workload": f"Kitaev-Heisenberg honeycomb N={args.sites} H.v (CPU oracle port, bounded sample)"},
+            "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "GB/s", "h2d_bytes_per_step": 0,
+                                          "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--sites", type=int, default=32)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import numpy as np
+    import torch
+    import energyspincurrents_gb300 as esc
+    from energyspincurrents_gb300 import build
+    build.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    params = workload(args.sites)
+    h = esc.Handle(params)
+    D = h.D
+    stream = torch.cuda.ExternalStream(h.stream())
+    v = torch.empty(D, dtype=torch.complex64, device="cuda")
+    out = torch.empty_like(v)
+    h_st = esc.lib().esc_start_vector(h.h, 1, 1, esc.ctypes.c_void_p(v.data_ptr()), esc.C64, esc.DEVICE_PTR)
+    assert h_st == 0, esc.lib().esc_last_error(h.h)
+    torch.cuda.synchronize()
+
+    def step():
+        h.hv_device(v.data_ptr(), out.data_ptr(), esc.C64, esc.DEVICE_PTR | esc.ASYNC)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    algo_bytes = D * 16                              # read v + write out, complex64
+    gbs_total = world * algo_bytes / (ms * 1e-3) / 1e9
+    kernel_gbs = algo_bytes / (ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    prof = traffic_from_profile()
+    roof = {"bound": "hbm", "achieved": round(kernel_gbs, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(kernel_gbs / peak, 4), "peak_source": peak_kind,
+            "traffic": (prof or {}).get("bytes_per_launch"),
+            "kernel": "k_hv<float>", "algorithmic_bytes_per_launch": algo_bytes}
+
+    # end to end through the C ABI with host buffers (pinned), copies inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        try:
+            hin = torch.empty(D, dtype=torch.complex64, pin_memory=True)
+            hout = torch.empty(D, dtype=torch.complex64, pin_memory=True)
+            del out
+            torch.cuda.empty_cache()
+            h.hv(hin.numpy(), out=hout.numpy())   # warm-up (allocates the staging buffers)
+            reps = max(1, min(args.steps, 3))
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                h.hv(hin.numpy(), out=hout.numpy())
+            el = (time.perf_counter() - t0) / reps
+            e2e = {"value": round(world * algo_bytes / el / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": D * 8,
+                   "d2h_bytes_per_step": D * 8, "ms_per_step": round(el * 1e3, 3)}
+        except Exception as ex:
+            e2e = {"value": None, "unit": "GB/s", "error": str(ex)[:200]}
+    cb = None
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_baseline(params, args.sites)
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(gbs_total, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+                "config": {"workload": f"Kitaev-Heisenberg honeycomb N={args.sites} ({params['Lx']}x{params['Ly']//2} "
+                                       f"unit cells, PBC), K=-1 J=0.05 h=0.02[111], one H.v per step",
+                           "states": D, "l2": "inputs larger than L2 (no flush needed)" if D * 8 > 129e6 else
+                           "inputs smaller than L2", "parallelism": "replicas" if world > 1 else "single GPU"},
+                "roofline": roof, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(),
+                "gpu_launches": args.steps}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

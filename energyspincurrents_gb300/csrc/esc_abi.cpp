@@ -1,0 +1,797 @@
+// esc_abi.cpp -- the C ABI (include/esc.h): handle, operators, GPU Lanczos, spectra.
+//
+// Host C++ drives hand-written sm_103a kernels (kernels.cu).  No CPU fallback exists: every
+// vector operation runs on the device; the host only does O(M^2)-O(M^3) work on the tridiagonal
+// matrix and the O(Omega x M) Lehmann / continued-fraction sums.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "esc_internal.h"
+
+using esc::cplx;
+
+struct esc_handle {
+    esc_params p{};
+    esc::Lattice L;
+    std::vector<esc::Bond> bonds;
+    esc::DevModel dm{};
+    int N = 0;
+    int64_t D = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    // device memory owned by the handle
+    double* d_part = nullptr; size_t part_bytes = 0;   // reduction partials
+    double* d_sc = nullptr; size_t sc_bytes = 0;       // scalars (alpha, |w|^2, projections, ...)
+    void* d_L = nullptr; size_t L_bytes = 0;           // Krylov basis
+    void* d_work = nullptr; size_t work_bytes = 0;     // work vectors
+    void* d_gs = nullptr; size_t gs_bytes = 0;         // ground state
+    void* d_io = nullptr; size_t io_bytes = 0;         // staging for host-pointer calls
+    // ground-state Lanczos results
+    int nsteps = 0;
+    bool have_gs = false, have_basis = false;
+    esc_dtype basis_dt = ESC_C128;
+    int64_t L_ld = 0;
+    std::vector<double> alpha, beta, ritz, Z;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+struct Fail : std::runtime_error {
+    esc_status st;
+    Fail(esc_status s, const std::string& m) : std::runtime_error(m), st(s) {}
+};
+
+esc_status finish(esc_handle* h, esc_status st, const std::string& msg) {
+    g_err = msg;
+    if (h) h->err = msg;
+    return st;
+}
+
+template <typename F>
+esc_status guarded(esc_handle* h, F&& f) {
+    try {
+        f();
+        if (h) h->err.clear();
+        return ESC_OK;
+    } catch (Fail& e) {
+        return finish(h, e.st, e.what());
+    } catch (esc::CudaError& e) {
+        return finish(h, ESC_ERR_CUDA, e.what());
+    } catch (std::invalid_argument& e) {
+        return finish(h, ESC_ERR_PARAM, e.what());
+    } catch (std::bad_alloc&) {
+        return finish(h, ESC_ERR_MEMORY, "host allocation failed");
+    } catch (std::exception& e) {
+        return finish(h, ESC_ERR_NUMERIC, e.what());
+    }
+}
+
+size_t esize(esc_dtype dt) { return dt == ESC_C64 ? 8 : 16; }
+
+void ensure(void*& p, size_t& cap, size_t need) {
+    if (need <= cap && p) return;
+    if (p) { cudaFree(p); p = nullptr; cap = 0; }
+    if (need == 0) return;
+    cudaError_t e = cudaMalloc(&p, need);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        p = nullptr;
+        throw Fail(ESC_ERR_MEMORY, "device allocation of " + std::to_string(need >> 20) + " MiB failed (" +
+                                       cudaGetErrorString(e) + ")");
+    }
+    cap = need;
+}
+template <typename T>
+void ensure_t(T*& p, size_t& cap, size_t need) {
+    void* q = p;
+    ensure(q, cap, need);
+    p = (T*)q;
+}
+
+void sync(esc_handle* h) { ESC_CUDA(cudaStreamSynchronize(h->stream)); }
+
+void ensure_partials(esc_handle* h, int rows) {
+    const size_t need = (size_t)std::max(rows, 4) * esc::RED_MAX_BLOCKS * 2 * sizeof(double);
+    ensure_t(h->d_part, h->part_bytes, need);
+}
+int64_t part_cap_doubles(esc_handle* h) { return (int64_t)(h->part_bytes / sizeof(double)); }
+
+// Staged input/output: device pointer as-is, host pointer copied through d_io.
+struct Staged {
+    const void* in;
+    void* out;
+};
+Staged stage(esc_handle* h, const void* in, void* out, size_t in_bytes, size_t out_bytes, int flags) {
+    if (flags & ESC_DEVICE_PTR) return {in, out};
+    ensure(h->d_io, h->io_bytes, in_bytes + out_bytes);
+    char* base = (char*)h->d_io;
+    if (in) ESC_CUDA(cudaMemcpyAsync(base, in, in_bytes, cudaMemcpyHostToDevice, h->stream));
+    return {in ? base : nullptr, base + in_bytes};
+}
+void unstage(esc_handle* h, const Staged& s, void* out, size_t out_bytes, int flags) {
+    if (!(flags & ESC_DEVICE_PTR) && out) ESC_CUDA(cudaMemcpyAsync(out, s.out, out_bytes, cudaMemcpyDeviceToHost, h->stream));
+    if (!(flags & ESC_ASYNC) || !(flags & ESC_DEVICE_PTR)) sync(h);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Templated device pipelines
+// ---------------------------------------------------------------------------------------------
+template <typename R>
+struct Pipe {
+    esc_handle* h;
+    static constexpr size_t ES = 2 * sizeof(R);
+    int64_t D;
+    explicit Pipe(esc_handle* hh) : h(hh), D(hh->D) {}
+    void hv(const void* in, void* out) { esc::launch_hv<R>(h->dm, in, out, D, h->stream); }
+    void apply(const esc::DevOp& op, const void* in, void* out) { esc::launch_apply<R>(op, in, out, D, h->stream); }
+    void dot(const void* a, const void* b, double* dst) { esc::launch_dot<R>(a, b, D, h->d_part, dst, h->stream); }
+    void nrm2(const void* a, double* dst) { esc::launch_nrm2<R>(a, D, h->d_part, dst, h->stream); }
+    void scale(const void* in, void* out, const double* d_nrm2) { esc::launch_scale_rsqrt<R>(in, out, d_nrm2, D, h->stream); }
+};
+
+// Ground-state Lanczos, DynLanczosSolver::Lanczos_Nirav (src/DynLanczosSolver.h:38-239).
+template <typename R>
+void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) {
+    Pipe<R> P(h);
+    const int64_t D = h->D;
+    const size_t ES = Pipe<R>::ES;
+    const int M = cfg.steps;
+    const bool store = cfg.lanctype != 0;                // OnlyEgs keeps no basis (returns a zero vector)
+    const bool reo = store && cfg.reortho;
+    const int nvec = store ? M + 1 : 3;
+    h->have_gs = h->have_basis = false;
+    ensure(h->d_L, h->L_bytes, (size_t)nvec * D * ES);
+    ensure(h->d_work, h->work_bytes, (size_t)D * ES);
+    // scalars: alpha[2M] | b2[M+2] | tmp[8] | r[2(M+2)] | z[M+2]
+    const size_t n_sc = 2 * (size_t)M + (M + 2) + 8 + 2 * (size_t)(M + 2) + (M + 2);
+    ensure_t(h->d_sc, h->sc_bytes, n_sc * sizeof(double));
+    double* d_alpha = h->d_sc;
+    double* d_b2 = d_alpha + 2 * M;
+    double* d_tmp = d_b2 + (M + 2);
+    double* d_r = d_tmp + 8;
+    double* d_z = d_r + 2 * (M + 2);
+    ensure_partials(h, reo ? M + 2 : 4);
+    ESC_CUDA(cudaMemsetAsync(h->d_sc, 0, n_sc * sizeof(double), h->stream));
+    auto Lv = [&](int i) -> char* { return (char*)h->d_L + (size_t)(store ? i : i % 3) * D * ES; };
+    void* w = h->d_work;
+
+    // Vorig.normalize(); V0 = Vorig (:58-66)
+    P.nrm2(d_start, d_tmp);
+    P.scale(d_start, Lv(0), d_tmp);
+    // iteration 0 (:75-83): V1 = H V0; alpha0 = <V0|V1>; V1 -= alpha0 V0; beta1 = |V1|; normalise
+    P.hv(Lv(0), w);
+    P.dot(Lv(0), w, d_alpha);
+    esc::launch_lanczos_update<R>(w, Lv(0), nullptr, d_alpha, nullptr, D, h->d_part, d_b2 + 1, h->stream);
+    P.scale(w, Lv(1), d_b2 + 1);
+    int exit_iter = M - 1;
+    double E0 = 1.0;
+    for (int iter = 1; iter <= M - 1; iter++) {             // :91-163
+        P.hv(Lv(iter), w);
+        P.dot(Lv(iter), w, d_alpha + 2 * iter);
+        esc::launch_lanczos_update<R>(w, Lv(iter), Lv(iter - 1), d_alpha + 2 * iter, d_b2 + iter, D, h->d_part,
+                                      d_b2 + iter + 1, h->stream);
+        P.scale(w, Lv(iter + 1), d_b2 + iter + 1);
+        if (reo) {
+            // Full reorthogonalisation against L_0..L_iter (:105-119).  The reference does one
+            // modified Gram-Schmidt sweep; here two classical sweeps (CGS2) as two GEMV pairs,
+            // which orthogonalise to the same working precision.
+            for (int pass = 0; pass < 2; pass++) {
+                esc::launch_gemv_h<R>(h->d_L, D, iter + 1, Lv(iter + 1), D, h->d_part, part_cap_doubles(h), d_r,
+                                      h->stream);
+                esc::launch_gemv_sub<R>(h->d_L, D, iter + 1, d_r, Lv(iter + 1), D, h->stream);
+            }
+            P.nrm2(Lv(iter + 1), d_tmp + 1);
+            P.scale(Lv(iter + 1), Lv(iter + 1), d_tmp + 1);
+        }
+        if (cfg.eps > 0.0) {                                 // :125-151 (convergence test)
+            std::vector<double> a(2 * (iter + 1)), b2(iter + 2);
+            ESC_CUDA(cudaMemcpyAsync(a.data(), d_alpha, a.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            ESC_CUDA(cudaMemcpyAsync(b2.data(), d_b2, b2.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            sync(h);
+            std::vector<double> d(iter + 1), e(iter + 1, 0.0);
+            for (int i = 0; i <= iter; i++) d[i] = a[2 * i];
+            for (int i = 0; i < iter; i++) e[i] = std::sqrt(b2[i + 1]);
+            if (!esc::tridiag_eig(iter + 1, d, e, nullptr)) throw Fail(ESC_ERR_NUMERIC, "diag: tridiagonal eigensolver failed");
+            const double diff = std::fabs(E0 - d[0]);
+            E0 = d[0];
+            if (diff < cfg.eps) { exit_iter = iter; break; }
+        }
+    }
+    const int n = exit_iter + 1;                             // EXITiter (:164)
+    std::vector<double> a(2 * (size_t)M), b2(M + 2);
+    ESC_CUDA(cudaMemcpyAsync(a.data(), d_alpha, a.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    ESC_CUDA(cudaMemcpyAsync(b2.data(), d_b2, b2.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    sync(h);
+    h->alpha.assign(n, 0.0);
+    h->beta.assign(n + 1, 0.0);
+    for (int i = 0; i < n; i++) h->alpha[i] = a[2 * i];
+    for (int i = 1; i <= n; i++) h->beta[i] = std::sqrt(b2[i]);
+    for (int i = 0; i < n; i++)
+        if (!std::isfinite(h->alpha[i]) || !std::isfinite(h->beta[i + 1]))
+            throw Fail(ESC_ERR_NUMERIC, "NaN/Inf in Lanczos coefficients at step " + std::to_string(i));
+    for (int i = 1; i < n; i++)
+        if (h->beta[i] == 0.0)
+            throw Fail(ESC_ERR_NUMERIC, "Lanczos breakdown: beta=0 at step " + std::to_string(i) +
+                                            " (Krylov space exhausted; use fewer LanczosSteps)");
+    std::vector<double> d(h->alpha), e(n, 0.0);
+    for (int i = 0; i < n - 1; i++) e[i] = h->beta[i + 1];
+    h->Z.clear();
+    if (!esc::tridiag_eig(n, d, e, store ? &h->Z : nullptr)) throw Fail(ESC_ERR_NUMERIC, "diag: tridiagonal eigensolver failed");
+    h->ritz = d;
+    h->nsteps = n;
+    ensure(h->d_gs, h->gs_bytes, (size_t)D * 16);
+    if (store) {
+        // PsiAll[0] = sum_m L_m Z(m,0) (:208-234), without forming the other Ritz vectors
+        ESC_CUDA(cudaMemcpyAsync(d_z, h->Z.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        esc::launch_lincomb<R>(h->d_L, D, n, d_z, h->d_gs, D, h->stream);
+        h->have_basis = cfg.lanctype == 2;
+    } else {
+        ESC_CUDA(cudaMemsetAsync(h->d_gs, 0, (size_t)D * ES, h->stream));   // OnlyEgs returns zeros (:178-180)
+    }
+    h->basis_dt = sizeof(R) == 8 ? ESC_C128 : ESC_C64;
+    h->L_ld = D;
+    h->have_gs = true;
+    sync(h);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Spectra
+// ---------------------------------------------------------------------------------------------
+struct Grid {
+    int nw;
+    double dw, eta;
+};
+
+// One operator "channel": a combination of operator strings applied to |gs>.
+std::vector<esc::OpTerm> combine(const std::vector<esc::OpTerm>& a, const std::vector<esc::OpTerm>& b, cplx cb) {
+    std::vector<esc::OpTerm> t(a);
+    for (auto x : b) { x.coef *= cb; t.push_back(x); }
+    return t;
+}
+
+template <typename R>
+struct Spectra {
+    esc_handle* h;
+    Pipe<R> P;
+    const int64_t D;
+    char* buf(int i) { return (char*)h->d_work + (size_t)i * D * Pipe<R>::ES; }
+    explicit Spectra(esc_handle* hh) : h(hh), P(hh), D(hh->D) {}
+
+    // <gs| A |gs> with A given as terms; uses work vector `slot`.
+    cplx expect(const std::vector<esc::OpTerm>& t, int slot, double* d_tmp) {
+        P.apply(esc::make_dev_op(t), h->d_gs, buf(slot));
+        P.dot(h->d_gs, buf(slot), d_tmp);
+        double r[2];
+        ESC_CUDA(cudaMemcpyAsync(r, d_tmp, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        sync(h);
+        return cplx(r[0], r[1]);
+    }
+
+    // Ritz-mode overlaps O[n] = <psi_n | A gs> = sum_m Z(m,n) <L_m | A gs>  (dynamics.h:256-263)
+    std::vector<cplx> ritz_overlaps(const std::vector<esc::OpTerm>& t, int slot, double* d_r, double* d_tmp,
+                                    cplx* elastic) {
+        const int M = h->nsteps;
+        P.apply(esc::make_dev_op(t), h->d_gs, buf(slot));
+        P.dot(h->d_gs, buf(slot), d_tmp);
+        esc::launch_gemv_h<R>(h->d_L, h->L_ld, M, buf(slot), D, h->d_part, part_cap_doubles(h), d_r, h->stream);
+        std::vector<double> r(2 * (size_t)M), el(2);
+        ESC_CUDA(cudaMemcpyAsync(r.data(), d_r, r.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        ESC_CUDA(cudaMemcpyAsync(el.data(), d_tmp, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        sync(h);
+        *elastic = cplx(el[0], el[1]);
+        std::vector<cplx> O(M);
+        for (int n = 0; n < M; n++) {
+            cplx s(0, 0);
+            for (int m = 0; m < M; m++) s += h->Z[(size_t)n * M + m] * cplx(r[2 * m], r[2 * m + 1]);
+            O[n] = s;
+        }
+        return O;
+    }
+
+    // CF-mode: Lanczos from phi = A|gs> (plain three-term recurrence, K steps) -> a, b; b[0]=|phi|.
+    void cf_coeffs(const std::vector<esc::OpTerm>& t, int K, double* d_sc, std::vector<double>& a,
+                   std::vector<double>& b) {
+        double* d_a = d_sc;             // 2K
+        double* d_b2 = d_a + 2 * K;     // K+1
+        ESC_CUDA(cudaMemsetAsync(d_sc, 0, (3 * (size_t)K + 1) * sizeof(double), h->stream));
+        int prev = 0, cur = 1, wb = 2;
+        P.apply(esc::make_dev_op(t), h->d_gs, buf(cur));
+        P.nrm2(buf(cur), d_b2);
+        P.scale(buf(cur), buf(cur), d_b2);
+        for (int k = 0; k < K; k++) {
+            P.hv(buf(cur), buf(wb));
+            P.dot(buf(cur), buf(wb), d_a + 2 * k);
+            esc::launch_lanczos_update<R>(buf(wb), buf(cur), k ? buf(prev) : nullptr, d_a + 2 * k, k ? d_b2 + k : nullptr,
+                                          D, h->d_part, d_b2 + k + 1, h->stream);
+            P.scale(buf(wb), buf(wb), d_b2 + k + 1);
+            const int np = cur, nc = wb, nw = prev;
+            prev = np; cur = nc; wb = nw;
+        }
+        std::vector<double> ha(2 * (size_t)K), hb2(K + 1);
+        ESC_CUDA(cudaMemcpyAsync(ha.data(), d_a, ha.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        ESC_CUDA(cudaMemcpyAsync(hb2.data(), d_b2, hb2.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        sync(h);
+        a.clear(); b.clear();
+        const double b0 = std::sqrt(hb2[0]);
+        b.push_back(b0);
+        if (b0 == 0.0) return;
+        for (int k = 0; k < K; k++) {
+            a.push_back(ha[2 * k]);
+            const double bn = std::sqrt(hb2[k + 1]);
+            if (k + 1 == K || !(bn > 1e-10 * b0)) break;       // stop at beta < 1e-10 |phi|
+            b.push_back(bn);
+        }
+    }
+};
+
+// S_ab(omega) pieces for CF mode via polarisation: S_ab = (X - iY)/2, S_ba = (X + iY)/2 with
+// X = S(a+b) - S_aa - S_bb, Y = S(a+ib) - S_aa - S_bb.
+struct CFSet {
+    std::vector<std::vector<cplx>> S;   // per run, per omega
+};
+
+}  // namespace
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+extern "C" {
+
+const char* esc_last_error(const esc_handle* h) { return h ? h->err.c_str() : g_err.c_str(); }
+
+esc_status esc_create(const esc_params* p, esc_handle** out) {
+    if (!p || !out) return finish(nullptr, ESC_ERR_PARAM, "null argument");
+    *out = nullptr;
+    std::unique_ptr<esc_handle> h(new esc_handle());
+    esc_status st = guarded(h.get(), [&]() {
+        h->p = *p;
+        const std::string solver(p->solver);
+        if (solver == "ED") throw Fail(ESC_ERR_PARAM, "Solver=ED (dense diagonalisation) is not provided on the GPU; use Solver=none");
+        esc::build_lattice(*p, h->L);
+        esc::build_bonds(*p, h->L, h->bonds);
+        h->N = h->L.N;
+        h->D = int64_t(1) << h->N;
+        h->dm = esc::make_dev_model(*p, h->L, h->bonds, p->Bxx, p->Byy, p->Bzz);
+        int ndev = 0;
+        cudaError_t e = cudaGetDeviceCount(&ndev);
+        if (e != cudaSuccess || ndev == 0) {
+            (void)cudaGetLastError();
+            throw Fail(ESC_ERR_CUDA, "no CUDA device available: this library has no CPU path");
+        }
+        ESC_CUDA(cudaGetDevice(&h->device));
+        ESC_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        ensure_partials(h.get(), 4);
+    });
+    if (st != ESC_OK) {
+        g_err = h->err;
+        esc_destroy(h.release());
+        return st;
+    }
+    *out = h.release();
+    return ESC_OK;
+}
+
+esc_status esc_destroy(esc_handle* h) {
+    if (!h) return ESC_OK;
+    for (void* p : {(void*)h->d_part, (void*)h->d_sc, h->d_L, h->d_work, h->d_gs, h->d_io})
+        if (p) cudaFree(p);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return ESC_OK;
+}
+
+int esc_num_sites(const esc_handle* h) { return h ? h->N : 0; }
+int64_t esc_dim(const esc_handle* h) { return h ? h->D : 0; }
+void* esc_stream(esc_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+esc_status esc_lattice(const esc_params* p, int* neigh, int* nsites) {
+    if (!p) return finish(nullptr, ESC_ERR_PARAM, "null argument");
+    return guarded(nullptr, [&]() {
+        esc::Lattice L;
+        esc::build_lattice(*p, L);
+        if (nsites) *nsites = L.N;
+        if (neigh) std::memcpy(neigh, L.neigh.data(), L.neigh.size() * sizeof(int));
+    });
+}
+
+esc_status esc_neighbors(const esc_handle* h, int* neigh) {
+    if (!h || !neigh) return finish(nullptr, ESC_ERR_PARAM, "null argument");
+    std::memcpy(neigh, h->L.neigh.data(), h->L.neigh.size() * sizeof(int));
+    return ESC_OK;
+}
+
+esc_status esc_hv(esc_handle* h, const void* in, void* out, esc_dtype dt, int flags) {
+    if (!h || !in || !out) return finish(h, ESC_ERR_PARAM, "null argument");
+    if (in == out) return finish(h, ESC_ERR_PARAM, "esc_hv: in and out must differ");
+    return guarded(h, [&]() {
+        const size_t bytes = (size_t)h->D * esize(dt);
+        Staged s = stage(h, in, out, bytes, bytes, flags);
+        if (dt == ESC_C64) esc::launch_hv<float>(h->dm, s.in, s.out, h->D, h->stream);
+        else esc::launch_hv<double>(h->dm, s.in, s.out, h->D, h->stream);
+        unstage(h, s, out, bytes, flags);
+    });
+}
+
+esc_status esc_hv_batched(esc_handle* h, const void* in, void* out, int ncols, int64_t ld, const double* fields,
+                          esc_dtype dt, int flags) {
+    if (!h || !in || !out) return finish(h, ESC_ERR_PARAM, "null argument");
+    if (ncols < 1 || ncols > esc::MAX_COLS) return finish(h, ESC_ERR_PARAM, "ncols must be 1..16");
+    if (ld < h->D) return finish(h, ESC_ERR_PARAM, "ld must be >= 2^N");
+    return guarded(h, [&]() {
+        esc::DevFields f;
+        for (int c = 0; c < esc::MAX_COLS; c++) {
+            const double* b = (fields && c < ncols) ? fields + 3 * c : nullptr;
+            f.fx[c] = 0.5 * (b ? b[0] : h->p.Bxx);
+            f.fy[c] = 0.5 * (b ? b[1] : h->p.Byy);
+            f.fz[c] = 0.5 * (b ? b[2] : h->p.Bzz);
+        }
+        const size_t bytes = (size_t)((ncols - 1) * ld + h->D) * esize(dt);
+        Staged s = stage(h, in, out, bytes, bytes, flags);
+        if (dt == ESC_C64) esc::launch_hv_batched<float>(h->dm, f, s.in, s.out, ncols, ld, h->D, h->stream);
+        else esc::launch_hv_batched<double>(h->dm, f, s.in, s.out, ncols, ld, h->D, h->stream);
+        unstage(h, s, out, bytes, flags);
+    });
+}
+
+esc_status esc_apply_op(esc_handle* h, int op, int site, const void* in, void* out, esc_dtype dt, int flags) {
+    if (!h || !in || !out) return finish(h, ESC_ERR_PARAM, "null argument");
+    if (in == out) return finish(h, ESC_ERR_PARAM, "esc_apply_op: in and out must differ");
+    return guarded(h, [&]() {
+        const esc::DevOp d = esc::make_dev_op(esc::operator_terms(op, site, h->p, h->L));
+        const size_t bytes = (size_t)h->D * esize(dt);
+        Staged s = stage(h, in, out, bytes, bytes, flags);
+        if (dt == ESC_C64) esc::launch_apply<float>(d, s.in, s.out, h->D, h->stream);
+        else esc::launch_apply<double>(d, s.in, s.out, h->D, h->stream);
+        unstage(h, s, out, bytes, flags);
+    });
+}
+
+esc_status esc_start_vector(esc_handle* h, int kind, int seed, void* out, esc_dtype dt, int flags) {
+    if (!h || !out) return finish(h, ESC_ERR_PARAM, "null argument");
+    return guarded(h, [&]() {
+        const int64_t D = h->D;
+        const size_t bytes = (size_t)D * esize(dt);
+        Staged s = stage(h, nullptr, out, 0, bytes, flags);
+        ensure_t(h->d_sc, h->sc_bytes, std::max<size_t>(h->sc_bytes, 64));
+        if (kind == ESC_START_REFUNIFORM) {
+            std::vector<cplx> v((size_t)D);
+            esc::ref_uniform_start(seed, D, v.data());
+            if (dt == ESC_C128) {
+                ESC_CUDA(cudaMemcpyAsync(s.out, v.data(), bytes, cudaMemcpyHostToDevice, h->stream));
+            } else {
+                ensure(h->d_work, h->work_bytes, (size_t)D * 16);
+                ESC_CUDA(cudaMemcpyAsync(h->d_work, v.data(), (size_t)D * 16, cudaMemcpyHostToDevice, h->stream));
+                esc::launch_convert_c128_to_c64(h->d_work, s.out, D, h->stream);
+            }
+            sync(h);
+        } else if (kind == ESC_START_NORMAL) {
+            if (dt == ESC_C128) esc::launch_start_normal<double>((uint64_t)(int64_t)seed, s.out, D, h->stream);
+            else esc::launch_start_normal<float>((uint64_t)(int64_t)seed, s.out, D, h->stream);
+        } else {
+            throw Fail(ESC_ERR_PARAM, "unknown start-vector kind");
+        }
+        // normalised
+        if (dt == ESC_C128) { esc::launch_nrm2<double>(s.out, D, h->d_part, h->d_sc, h->stream); esc::launch_scale_rsqrt<double>(s.out, s.out, h->d_sc, D, h->stream); }
+        else { esc::launch_nrm2<float>(s.out, D, h->d_part, h->d_sc, h->stream); esc::launch_scale_rsqrt<float>(s.out, s.out, h->d_sc, D, h->stream); }
+        unstage(h, s, out, bytes, flags);
+    });
+}
+
+esc_status esc_lanczos_gs(esc_handle* h, const esc_lanczos_cfg* cfg, const void* start, int flags, double* E0,
+                          double* alpha, double* beta, double* ritz, int* steps, void* gs_out) {
+    if (!h || !cfg) return finish(h, ESC_ERR_PARAM, "null argument");
+    if (cfg->steps < 2) return finish(h, ESC_ERR_PARAM, "LanczosSteps must be >= 2");
+    if (cfg->lanctype < 0 || cfg->lanctype > 2) return finish(h, ESC_ERR_PARAM, "DynLanczosSolver: Use PsiOrAll==GS or All");
+    return guarded(h, [&]() {
+        const int64_t D = h->D;
+        const esc_dtype dt = cfg->dtype;
+        const size_t es = esize(dt), bytes = (size_t)D * es;
+        // start vector into the staging area (device)
+        ensure(h->d_io, h->io_bytes, bytes);
+        void* d_start = h->d_io;
+        if (start) {
+            ESC_CUDA(cudaMemcpyAsync(d_start, start, bytes, (flags & ESC_DEVICE_PTR) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+        } else {
+            const esc_status st = esc_start_vector(h, h->p.start_vector, h->p.seed, d_start, dt, ESC_DEVICE_PTR);
+            if (st != ESC_OK) throw Fail(st, h->err);
+        }
+        if (dt == ESC_C64) lanczos_gs<float>(h, *cfg, d_start);
+        else lanczos_gs<double>(h, *cfg, d_start);
+        const int n = h->nsteps;
+        if (steps) *steps = n;
+        if (E0) *E0 = h->ritz[0];
+        if (alpha) std::copy(h->alpha.begin(), h->alpha.end(), alpha);
+        if (beta) std::copy(h->beta.begin(), h->beta.end(), beta);
+        if (ritz) std::copy(h->ritz.begin(), h->ritz.end(), ritz);
+        if (gs_out) ESC_CUDA(cudaMemcpyAsync(gs_out, h->d_gs, bytes, (flags & ESC_DEVICE_PTR) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+        sync(h);
+    });
+}
+
+}  // extern "C"
+
+namespace {
+
+// Lehmann sum helpers (src/dynamics.h:277-316, :396-425, :133-187)
+inline cplx lehmann_term(cplx a, cplx b, double w, double dE, double eta) { return std::conj(a) * b / cplx(w - dE, -eta); }
+
+template <typename R>
+void spectrum_impl(esc_handle* h, const esc_dyn_cfg& cfg, std::vector<double>& out, int& ncols) {
+    Spectra<R> S(h);
+    const int64_t D = h->D;
+    const int N = h->N;
+    const int nw = cfg.omega_steps + 1;
+    const double eta = cfg.eta;
+    const bool ritz = cfg.mode == ESC_DYNMODE_RITZ;
+    const double Eg = h->ritz[0];
+    const int M = h->nsteps;
+    const int K = cfg.cf_steps > 0 ? cfg.cf_steps : M;
+    const int nwork = ritz ? 1 : 3;
+    ensure(h->d_work, h->work_bytes, (size_t)nwork * D * Pipe<R>::ES);
+    const size_t nsc = 2 * (size_t)std::max(M, 1) + 8 + 3 * (size_t)K + 8;
+    ensure_t(h->d_sc, h->sc_bytes, std::max(h->sc_bytes, nsc * sizeof(double)));
+    ensure_partials(h, std::max(M, 4));
+    double* d_r = h->d_sc;
+    double* d_tmp = d_r + 2 * std::max(M, 1);
+    double* d_cf = d_tmp + 8;
+    auto T = [&](int op, int site) { return esc::operator_terms(op, site, h->p, h->L); };
+    auto omega = [&](int k) { return cfg.domega * k; };
+
+    // CF resolvent G_A(omega) = <A gs|(z-H)^-1|A gs>, z = omega + E0 - i eta
+    auto cf_run = [&](const std::vector<esc::OpTerm>& t) {
+        std::vector<double> a, b;
+        S.cf_coeffs(t, K, d_cf, a, b);
+        std::vector<cplx> g(nw);
+        for (int k = 0; k < nw; k++) g[k] = esc::cf_eval(a.data(), b.data(), (int)a.size(), cplx(omega(k) + Eg, -eta));
+        return g;
+    };
+
+    if (cfg.kind == ESC_DYN_JEJE || cfg.kind == ESC_DYN_JSJS) {
+        const bool je = cfg.kind == ESC_DYN_JEJE;
+        // channels: Je -> x, y, t = x+y ; Js -> x, y, z, t = x+y+z   (dynamics.h:365-367, :244-247)
+        std::vector<std::vector<esc::OpTerm>> ch;
+        if (je) {
+            ch.push_back(T(ESC_OP_JEX_TOTAL, 0));
+            ch.push_back(T(ESC_OP_JEY_TOTAL, 0));
+            ch.push_back(combine(ch[0], ch[1], 1.0));
+        } else {
+            ch.push_back(T(ESC_OP_JSX_TOTAL, 0));
+            ch.push_back(T(ESC_OP_JSY_TOTAL, 0));
+            ch.push_back(T(ESC_OP_JSZ_TOTAL, 0));
+            ch.push_back(combine(combine(ch[0], ch[1], 1.0), ch[2], 1.0));
+        }
+        const int nc = (int)ch.size();
+        std::vector<cplx> el(nc);
+        // pairs whose off-diagonal correlation the file needs
+        std::vector<std::pair<int, int>> pairs = je ? std::vector<std::pair<int, int>>{{0, 1}}
+                                                    : std::vector<std::pair<int, int>>{{0, 1}, {0, 2}, {1, 2}};
+        // S[a][b][omega]
+        std::vector<std::vector<std::vector<cplx>>> Sab(nc, std::vector<std::vector<cplx>>(nc, std::vector<cplx>(nw)));
+        if (ritz) {
+            std::vector<std::vector<cplx>> O(nc);
+            for (int c = 0; c < nc; c++) O[c] = S.ritz_overlaps(ch[c], 0, d_r, d_tmp, &el[c]);
+            for (int k = 0; k < nw; k++) {
+                const double w = omega(k);
+                for (int a = 0; a < nc; a++)
+                    for (int b = 0; b < nc; b++) {
+                        if (!(a == b || (a < 3 && b < 3))) continue;
+                        cplx s(0, 0);
+                        for (int n = 0; n < M; n++) s = s + lehmann_term(O[a][n], O[b][n], w, h->ritz[n] - Eg, eta);
+                        Sab[a][b][k] = s;
+                    }
+            }
+        } else {
+            for (int c = 0; c < nc; c++) {
+                el[c] = S.expect(ch[c], 0, d_tmp);
+                Sab[c][c] = cf_run(ch[c]);
+            }
+            for (auto pr : pairs) {
+                const int a = pr.first, b = pr.second;
+                auto Sp = cf_run(combine(ch[a], ch[b], 1.0));
+                auto Sq = cf_run(combine(ch[a], ch[b], cplx(0, 1)));
+                for (int k = 0; k < nw; k++) {
+                    const cplx X = Sp[k] - Sab[a][a][k] - Sab[b][b][k];
+                    const cplx Y = Sq[k] - Sab[a][a][k] - Sab[b][b][k];
+                    Sab[a][b][k] = 0.5 * (X - cplx(0, 1) * Y);
+                    Sab[b][a][k] = 0.5 * (X + cplx(0, 1) * Y);
+                }
+            }
+        }
+        const int t = nc - 1;
+        if (je) {
+            ncols = 6;
+            out.assign((size_t)nw * ncols, 0.0);
+            for (int k = 0; k < nw; k++) {
+                const cplx dn(omega(k), -eta);
+                const cplx xx = Sab[0][0][k] - std::conj(el[0]) * el[0] / dn;
+                const cplx xy = Sab[0][1][k] - std::conj(el[0]) * el[1] / dn;
+                const cplx yy = Sab[1][1][k] - std::conj(el[1]) * el[1] / dn;
+                const cplx yx = Sab[1][0][k];   // reference subtracts conj(Jey)*Jez[0] with Jez[0] never set (:368-369,424)
+                const cplx tt = Sab[t][t][k] - std::conj(el[t]) * el[t] / dn;
+                double* r = &out[(size_t)k * ncols];
+                r[0] = omega(k); r[1] = xx.imag(); r[2] = yy.imag(); r[3] = xy.imag(); r[4] = yx.imag(); r[5] = tt.imag();
+            }
+        } else {
+            ncols = 15;
+            out.assign((size_t)nw * ncols, 0.0);
+            const int ord[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};   // dynamics.h:318-323
+            for (int k = 0; k < nw; k++) {
+                const cplx dn(omega(k), -eta);
+                double* r = &out[(size_t)k * ncols];
+                r[0] = omega(k);
+                for (int q = 0; q < 6; q++) {
+                    const int a = ord[q][0], b = ord[q][1];
+                    const cplx v = Sab[a][b][k] - std::conj(el[a]) * el[b] / dn;
+                    r[1 + 2 * q] = v.real(); r[2 + 2 * q] = v.imag();
+                }
+                const cplx tt = Sab[t][t][k] - std::conj(el[t]) * el[t] / dn;
+                r[13] = tt.real(); r[14] = tt.imag();
+            }
+        }
+        return;
+    }
+    if (cfg.kind != ESC_DYN_LOCALSZSZ) throw std::invalid_argument("Unknown dynstr parameter");
+    // LocalDynSzSz (dynamics.h:64-217): per site Sx, Sy, Sz, Sx+Sy+Sz, Spe3, Sme3
+    ncols = 9;
+    std::vector<cplx> acc((size_t)nw * 8, cplx(0, 0));
+    const int ops[6] = {ESC_OP_SX, ESC_OP_SY, ESC_OP_SZ, ESC_OP_SXSYSZ, ESC_OP_SPE3, ESC_OP_SME3};
+    for (int si = 0; si < N; si++) {
+        std::vector<std::vector<esc::OpTerm>> ch(6);
+        for (int c = 0; c < 6; c++) ch[c] = T(ops[c], si);
+        std::vector<cplx> el(6);
+        // Sab for (xx, yy, zz, xy, xz, yz, tt, pp, mm)
+        std::vector<std::vector<cplx>> R9(9, std::vector<cplx>(nw));
+        const int pa[9] = {0, 1, 2, 0, 0, 1, 3, 4, 5}, pb[9] = {0, 1, 2, 1, 2, 2, 3, 4, 5};
+        if (ritz) {
+            std::vector<std::vector<cplx>> O(6);
+            for (int c = 0; c < 6; c++) O[c] = S.ritz_overlaps(ch[c], 0, d_r, d_tmp, &el[c]);
+            for (int k = 0; k < nw; k++)
+                for (int q = 0; q < 9; q++) {
+                    cplx s(0, 0);
+                    for (int n = 0; n < M; n++) s = s + lehmann_term(O[pa[q]][n], O[pb[q]][n], omega(k), h->ritz[n] - Eg, eta);
+                    R9[q][k] = s;
+                }
+        } else {
+            std::vector<std::vector<cplx>> G(6);
+            for (int c = 0; c < 6; c++) {
+                el[c] = S.expect(ch[c], 0, d_tmp);
+                if (c == 0 || c == 1 || c == 2 || c == 3 || c == 4 || c == 5) G[c] = cf_run(ch[c]);
+            }
+            R9[0] = G[0]; R9[1] = G[1]; R9[2] = G[2]; R9[6] = G[3]; R9[7] = G[4]; R9[8] = G[5];
+            const int pp[3][3] = {{0, 1, 3}, {0, 2, 4}, {1, 2, 5}};
+            for (auto& q : pp) {
+                auto Sp = cf_run(combine(ch[q[0]], ch[q[1]], 1.0));
+                auto Sq = cf_run(combine(ch[q[0]], ch[q[1]], cplx(0, 1)));
+                for (int k = 0; k < nw; k++) {
+                    const cplx X = Sp[k] - G[q[0]][k] - G[q[1]][k];
+                    const cplx Y = Sq[k] - G[q[0]][k] - G[q[1]][k];
+                    R9[q[2]][k] = 0.5 * (X - cplx(0, 1) * Y);
+                }
+            }
+        }
+        for (int k = 0; k < nw; k++) {
+            const cplx dn(omega(k), -eta);
+            cplx* A = &acc[(size_t)k * 8];
+            for (int q = 0; q < 6; q++) A[q] += R9[q][k];
+            A[6] += R9[7][k];
+            A[7] += R9[8][k];
+            A[0] -= std::conj(el[0]) * el[0] / dn; A[3] -= std::conj(el[0]) * el[1] / dn; A[4] -= std::conj(el[0]) * el[2] / dn;
+            A[1] -= std::conj(el[1]) * el[1] / dn; A[5] -= std::conj(el[1]) * el[2] / dn; A[2] -= std::conj(el[2]) * el[2] / dn;
+            A[6] -= el[5] * el[4] / dn;   // Sm*Sp without conjugate, as written (dynamics.h:185-186)
+            A[7] -= el[4] * el[5] / dn;
+        }
+    }
+    out.assign((size_t)nw * ncols, 0.0);
+    for (int k = 0; k < nw; k++) {
+        double* r = &out[(size_t)k * ncols];
+        r[0] = omega(k);
+        // data order: xx, yy, zz, xy, xz, yz, SmSp, SpSm (dynamics.h:189-196)
+        for (int q = 0; q < 8; q++) r[1 + q] = acc[(size_t)k * 8 + q].imag();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+esc_status esc_spectrum(esc_handle* h, const esc_dyn_cfg* cfg, double* out, int* nrows, int* ncols) {
+    if (!h || !cfg) return finish(h, ESC_ERR_PARAM, "null argument");
+    if (!h->have_gs) return finish(h, ESC_ERR_STATE, "no ground state: call esc_lanczos_gs first");
+    if (cfg->mode == ESC_DYNMODE_RITZ && !h->have_basis)
+        return finish(h, ESC_ERR_STATE, "You need to set LancType=All for Dynamical calculations --- you dummy!");
+    if (cfg->omega_steps < 0) return finish(h, ESC_ERR_PARAM, "omega_steps must be >= 0");
+    return guarded(h, [&]() {
+        std::vector<double> s;
+        int nc = 0;
+        // The ground state and the Krylov basis share one precision; CF runs use cfg->dtype only
+        // when there is no basis to match (the GS vector is converted as needed).
+        const esc_dtype dt = h->basis_dt;
+        if (dt == ESC_C64) spectrum_impl<float>(h, *cfg, s, nc);
+        else spectrum_impl<double>(h, *cfg, s, nc);
+        if (nrows) *nrows = cfg->omega_steps + 1;
+        if (ncols) *ncols = nc;
+        if (out) std::copy(s.begin(), s.end(), out);
+    });
+}
+
+esc_status esc_measure_local(esc_handle* h, double* s_out, double* je_out) {
+    if (!h) return finish(h, ESC_ERR_PARAM, "null argument");
+    if (!h->have_gs) return finish(h, ESC_ERR_STATE, "no ground state: call esc_lanczos_gs first");
+    return guarded(h, [&]() {
+        auto run = [&](auto tag) {
+            typedef decltype(tag) R;
+            Spectra<R> S(h);
+            ensure(h->d_work, h->work_bytes, std::max(h->work_bytes, (size_t)h->D * Pipe<R>::ES));
+            ensure_t(h->d_sc, h->sc_bytes, std::max(h->sc_bytes, (size_t)16 * sizeof(double)));
+            double* d_tmp = h->d_sc;
+            for (int s = 0; s < h->N; s++) {
+                if (s_out) {
+                    const int ops[3] = {ESC_OP_SX, ESC_OP_SY, ESC_OP_SZ};
+                    for (int c = 0; c < 3; c++) {
+                        const cplx v = S.expect(esc::operator_terms(ops[c], s, h->p, h->L), 0, d_tmp);
+                        s_out[(s * 3 + c) * 2] = v.real(); s_out[(s * 3 + c) * 2 + 1] = v.imag();
+                    }
+                }
+                if (je_out) {
+                    const int ops[2] = {ESC_OP_JEX, ESC_OP_JEY};
+                    for (int c = 0; c < 2; c++) {
+                        const cplx v = S.expect(esc::operator_terms(ops[c], s, h->p, h->L), 0, d_tmp);
+                        je_out[(s * 2 + c) * 2] = v.real(); je_out[(s * 2 + c) * 2 + 1] = v.imag();
+                    }
+                }
+            }
+        };
+        if (h->basis_dt == ESC_C64) run(float()); else run(double());
+    });
+}
+
+esc_status esc_grad(esc_handle* h, const esc_dyn_cfg* cfg, double* dE0, double* dS) {
+    (void)cfg; (void)dS;
+    if (!h || !dE0) return finish(h, ESC_ERR_PARAM, "null argument");
+    if (!h->have_gs) return finish(h, ESC_ERR_STATE, "no ground state: call esc_lanczos_gs first");
+    return guarded(h, [&]() {
+        // Hellmann-Feynman: dE0/dtheta = <gs| dH/dtheta |gs> / <gs|gs>, with dH/dK the Kitaev
+        // bonds at unit coupling, dH/dJ the Heisenberg bonds at unit coupling and dH/dh the
+        // field -(Sx+Sy+Sz)/sqrt3 summed over sites.
+        esc_params pk = h->p, pj = h->p, ph = h->p;
+        pk.Kxx = pk.Kyy = pk.Kzz = 1.0; pk.jheis = 0.0;
+        pj.Kxx = pj.Kyy = pj.Kzz = 0.0; pj.jheis = 1.0;
+        ph.Kxx = ph.Kyy = ph.Kzz = 0.0; ph.jheis = 0.0;
+        const double s3 = -1.0 / std::sqrt(3.0);
+        std::vector<esc::Bond> bk, bj, bh;
+        esc::build_bonds(pk, h->L, bk);
+        esc::build_bonds(pj, h->L, bj);
+        const esc::DevModel mk = esc::make_dev_model(pk, h->L, bk, 0, 0, 0);
+        const esc::DevModel mj = esc::make_dev_model(pj, h->L, bj, 0, 0, 0);
+        const esc::DevModel mh = esc::make_dev_model(ph, h->L, bh, s3, s3, s3);
+        auto run = [&](auto tag) {
+            typedef decltype(tag) R;
+            const int64_t D = h->D;
+            ensure(h->d_work, h->work_bytes, std::max(h->work_bytes, (size_t)D * Pipe<R>::ES));
+            ensure_t(h->d_sc, h->sc_bytes, std::max(h->sc_bytes, (size_t)16 * sizeof(double)));
+            const esc::DevModel* ms[3] = {&mk, &mj, &mh};
+            double nn[2];
+            esc::launch_dot<R>(h->d_gs, h->d_gs, D, h->d_part, h->d_sc + 8, h->stream);
+            for (int q = 0; q < 3; q++) {
+                esc::launch_hv<R>(*ms[q], h->d_gs, h->d_work, D, h->stream);
+                esc::launch_dot<R>(h->d_gs, h->d_work, D, h->d_part, h->d_sc + 2 * q, h->stream);
+            }
+            double r[6];
+            ESC_CUDA(cudaMemcpyAsync(r, h->d_sc, 6 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            ESC_CUDA(cudaMemcpyAsync(nn, h->d_sc + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            sync(h);
+            for (int q = 0; q < 3; q++) dE0[q] = r[2 * q] / nn[0];
+        };
+        if (h->basis_dt == ESC_C64) run(float()); else run(double());
+        if (dS) throw Fail(ESC_ERR_STATE, "dS(omega) requires DynMode=CF gradients (not built yet)");
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,158 @@
+// esc_internal.h -- shared declarations of the GB300 Lanczos ED library (host C++ + CUDA).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/esc.h"
+
+namespace esc {
+
+constexpr int MAX_SITES = 40;     // 2^40 complex64 = 8.8 TB: far beyond one GPU, so never binding
+constexpr int MAX_BONDS = 96;     // honeycomb: 3N/2 = 48 at N = 32
+constexpr int MAX_TERMS = 256;    // operator strings (spin-current total: 6N terms)
+constexpr int MAX_COLS = 16;      // columns of one batched H.V launch
+
+typedef std::complex<double> cplx;
+
+// ---------------------------------------------------------------------------------------------
+// Device-side model, passed by value as a __grid_constant__ kernel parameter (so that several
+// handles with different models can coexist; no __constant__ globals).
+//
+// Off-diagonal bond term (i,j): out[k] += c(k) * in[k ^ mask], c = bits i,j equal ? ceq : cdiff.
+//   Built from per-bond couplings (kx, ky, kz) as ceq = (kx - ky)/4, cdiff = (kx + ky)/4, which
+//   reproduces the reference's S^x S^x (1/4) and S^y S^y (-1/4 equal, +1/4 differ) matrix
+//   elements (src/Hamiltonian.h:113-158) and adds J S.S where enabled.
+// Diagonal bond term: dz * (equal ? +1/4 : -1/4) (src/Hamiltonian.h:344-360).
+// Field: out[k] += (Bx/2 + i By/2 * (bit_s(k) ? +1 : -1)) in[k ^ 2^s]  (:167-198)
+//        diag   += Bz/2 * (N - 2 popcount(k))                         (:364-375)
+// ---------------------------------------------------------------------------------------------
+struct DevBond {
+    unsigned long long mask;
+    double ceq, cdiff;
+};
+struct DevDiagBond {
+    unsigned long long mask;
+    double dz;
+};
+struct DevModel {
+    int N;
+    int nb;          // off-diagonal bonds
+    int nd;          // diagonal bonds
+    int pad;
+    double fx, fy, fz;   // Bx/2, By/2, Bz/2
+    DevBond b[MAX_BONDS];
+    DevDiagBond d[MAX_BONDS];
+};
+// Per-column field (batched H.V with one field per column).
+struct DevFields {
+    double fx[MAX_COLS], fy[MAX_COLS], fz[MAX_COLS];
+};
+
+// Operator = sum of terms; term t = coef * f_{n-1} ... f_0 (f_0 applied first), each factor a
+// single-site S^x/S^y/S^z.  Gather form: out[k] += coef * phi_t(k0) * in[k0], k0 = k ^ flip.
+struct DevOp {
+    int nt;
+    int pad;
+    unsigned long long flip[MAX_TERMS];
+    unsigned int fac[MAX_TERMS];   // bits 0-1 nf; factor f at bits 2+8f: 6 bits site, 2 bits op (1 x, 2 y, 3 z)
+    double cre[MAX_TERMS], cim[MAX_TERMS];
+};
+
+// ---------------------------------------------------------------------------------------------
+// Host-side model
+// ---------------------------------------------------------------------------------------------
+struct Bond {
+    int i, j;
+    char type;                // 'x' 'y' 'z' (honeycomb column) or 'c' (chain)
+    double kx, ky, kz;        // coupling of S^aS^a on this bond (incl. J)
+};
+
+struct Lattice {
+    int N = 0, ncol = 0;
+    std::vector<int> neigh;   // N x 3, -1 = none
+    std::vector<int> indx, indy;
+};
+
+struct Params;  // = esc_params
+
+void build_lattice(const esc_params& p, Lattice& L);
+void build_bonds(const esc_params& p, const Lattice& L, std::vector<Bond>& bonds);
+DevModel make_dev_model(const esc_params& p, const Lattice& L, const std::vector<Bond>& bonds,
+                        double Bx, double By, double Bz);
+
+struct OpTerm {
+    cplx coef;
+    int nf;
+    int site[3];
+    char op[3];   // 'x' 'y' 'z'
+};
+// Throws std::invalid_argument for unknown operators / missing neighbours.
+std::vector<OpTerm> operator_terms(int op, int site, const esc_params& p, const Lattice& L);
+DevOp make_dev_op(const std::vector<OpTerm>& terms);
+
+// ---------------------------------------------------------------------------------------------
+// Kernel launchers (kernels.cu).  R = double (complex128 vectors) or float (complex64 vectors).
+// Reductions always accumulate in double and are deterministic: fixed grids, fixed trees.
+// ---------------------------------------------------------------------------------------------
+int red_blocks(int64_t n);
+constexpr int RED_MAX_BLOCKS = 1216;   // 8 x 152 SMs
+
+template <typename R> void launch_hv(const DevModel& m, const void* in, void* out, int64_t D, cudaStream_t s);
+template <typename R> void launch_hv_batched(const DevModel& m, const DevFields& f, const void* in, void* out,
+                                             int ncols, int64_t ld, int64_t D, cudaStream_t s);
+template <typename R> void launch_apply(const DevOp& op, const void* in, void* out, int64_t D, cudaStream_t s);
+
+// dst (double2) = sum conj(a) b
+template <typename R> void launch_dot(const void* a, const void* b, int64_t n, double* partials, double* dst,
+                                      cudaStream_t s);
+// dst (double) = |a|^2
+template <typename R> void launch_nrm2(const void* a, int64_t n, double* partials, double* dst, cudaStream_t s);
+// w = w - alpha*v - beta*u (alpha: double2 at d_alpha, beta = sqrt(*d_beta2), u may be NULL);
+// then dst = |w|^2
+template <typename R> void launch_lanczos_update(void* w, const void* v, const void* u, const double* d_alpha,
+                                                 const double* d_beta2, int64_t n, double* partials, double* dst,
+                                                 cudaStream_t s);
+// out = in / sqrt(*d_nrm2)  (out may equal in)
+template <typename R> void launch_scale_rsqrt(const void* in, void* out, const double* d_nrm2, int64_t n,
+                                              cudaStream_t s);
+// out = a*x + b*y  (complex scalars on host)
+template <typename R> void launch_axpby(const void* x, const void* y, void* out, cplx a, cplx b, int64_t n,
+                                        cudaStream_t s);
+// r[j] = sum_k conj(L_j[k]) w[k], j < m; L_j at L + j*ld (elements).  r: m double2.
+template <typename R> void launch_gemv_h(const void* L, int64_t ld, int m, const void* w, int64_t n,
+                                         double* partials, int64_t partials_cap, double* r, cudaStream_t s);
+// w[k] -= sum_j L_j[k] r[j]   (r: m double2 on device)
+template <typename R> void launch_gemv_sub(const void* L, int64_t ld, int m, const double* r, void* w, int64_t n,
+                                           cudaStream_t s);
+// out[k] = sum_j L_j[k] z[j]  (z: m doubles on device, real)
+template <typename R> void launch_lincomb(const void* L, int64_t ld, int m, const double* z, void* out, int64_t n,
+                                          cudaStream_t s);
+void launch_convert_c128_to_c64(const void* in, void* out, int64_t n, cudaStream_t s);
+void launch_convert_c64_to_c128(const void* in, void* out, int64_t n, cudaStream_t s);
+template <typename R> void launch_start_normal(uint64_t seed, void* out, int64_t n, cudaStream_t s);
+
+// ---------------------------------------------------------------------------------------------
+// Host numerics
+// ---------------------------------------------------------------------------------------------
+// Symmetric tridiagonal eigenproblem (implicit QL); d: diagonal, e: off-diagonal (e[i] couples
+// i,i+1).  Eigenvalues ascending in d; z (optional) n x n column-major.  Returns false on failure.
+bool tridiag_eig(int n, std::vector<double>& d, std::vector<double> e, std::vector<double>* z);
+
+// Continued fraction b0^2/(z - a0 - b1^2/(z - a1 - ...)).
+cplx cf_eval(const double* a, const double* b, int n, cplx z);
+
+// Reference start vector: mt19937_64(seed), generate_canonical<double,53> draws, re then im.
+void ref_uniform_start(int seed, int64_t D, cplx* out);
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+void check_cuda(cudaError_t e, const char* what);
+#define ESC_CUDA(x) ::esc::check_cuda((x), #x)
+
+}  // namespace esc

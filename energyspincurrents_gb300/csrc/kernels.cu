@@ -1,0 +1,551 @@
+// kernels.cu -- sm_103a kernels of the Lanczos ED library: H.v gathers, operator apply,
+// deterministic reductions, Krylov-basis GEMVs.  R = double (complex128 storage and arithmetic)
+// or float (complex64 storage and arithmetic, double accumulation in every reduction).
+//
+// All kernels are pull-style gathers: each output element is written by exactly one thread, so
+// there are no atomics and results are bit-reproducible for a given launch geometry.
+#include <cuda_runtime.h>
+
+#include "esc_internal.h"
+
+namespace esc {
+
+template <typename R> struct V2;
+template <> struct V2<double> { typedef double2 T; };
+template <> struct V2<float> { typedef float2 T; };
+
+static inline int grid_for(int64_t n, int tpb, int max_blocks) {
+    int64_t g = (n + tpb - 1) / tpb;
+    if (g > max_blocks) g = max_blocks;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+static constexpr int SMS = 152;
+
+int red_blocks(int64_t n) {
+    // Fixed function of n: identical launch geometry (and so identical rounding) on every call.
+    return grid_for(n, 2048, RED_MAX_BLOCKS);
+}
+
+// =============================================================================================
+// H.v  (src/Hamiltonian.h:480-557 restated as a gather, coefficients computed from the bits)
+// =============================================================================================
+template <typename R>
+__global__ void __launch_bounds__(256) k_hv(const __grid_constant__ DevModel m,
+                                            const typename V2<R>::T* __restrict__ in,
+                                            typename V2<R>::T* __restrict__ out, long long D) {
+    typedef typename V2<R>::T C;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < D; k += stride) {
+        const unsigned long long uk = (unsigned long long)k;
+        double dg = 0.0;
+        for (int b = 0; b < m.nd; b++) {
+            const double q = 0.25 * m.d[b].dz;
+            dg += (__popcll(uk & m.d[b].mask) == 1) ? -q : q;
+        }
+        dg += m.fz * (double)(m.N - 2 * __popcll(uk));
+        const C v = in[k];
+        R ar = (R)dg * v.x, ai = (R)dg * v.y;
+        for (int b = 0; b < m.nb; b++) {
+            const unsigned long long mk = m.b[b].mask;
+            const R c = (R)((__popcll(uk & mk) == 1) ? m.b[b].cdiff : m.b[b].ceq);
+            const C w = in[uk ^ mk];
+            ar = fma(c, w.x, ar);
+            ai = fma(c, w.y, ai);
+        }
+        // field partners: F = sum v[k^2^s], G = sum (bit_s(k) ? +1 : -1) v[k^2^s]
+        R Fr = 0, Fi = 0, Gr = 0, Gi = 0;
+        for (int s = 0; s < m.N; s++) {
+            const C w = in[uk ^ (1ull << s)];
+            Fr += w.x; Fi += w.y;
+            if ((uk >> s) & 1ull) { Gr += w.x; Gi += w.y; } else { Gr -= w.x; Gi -= w.y; }
+        }
+        const R fx = (R)m.fx, fy = (R)m.fy;
+        ar = fma(fx, Fr, ar); ar = fma(-fy, Gi, ar);
+        ai = fma(fx, Fi, ai); ai = fma(fy, Gr, ai);
+        C o; o.x = ar; o.y = ai;
+        out[k] = o;
+    }
+}
+
+// Batched H.V: NC columns (leading dimension ld), one field per column, index decoded once.
+template <typename R, int NC>
+__global__ void __launch_bounds__(256) k_hv_batched(const __grid_constant__ DevModel m,
+                                                    const __grid_constant__ DevFields f,
+                                                    const typename V2<R>::T* __restrict__ in,
+                                                    typename V2<R>::T* __restrict__ out, long long D,
+                                                    long long ld, int ncols) {
+    typedef typename V2<R>::T C;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < D; k += stride) {
+        const unsigned long long uk = (unsigned long long)k;
+        double dgb = 0.0;
+        for (int b = 0; b < m.nd; b++) {
+            const double q = 0.25 * m.d[b].dz;
+            dgb += (__popcll(uk & m.d[b].mask) == 1) ? -q : q;
+        }
+        const double nz = (double)(m.N - 2 * __popcll(uk));
+        R ar[NC], ai[NC], Fr[NC], Fi[NC], Gr[NC], Gi[NC];
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            ar[c] = ai[c] = Fr[c] = Fi[c] = Gr[c] = Gi[c] = (R)0;
+            if (c < ncols) {
+                const R dg = (R)(dgb + f.fz[c] * nz);
+                const C v = in[c * ld + k];
+                ar[c] = dg * v.x; ai[c] = dg * v.y;
+            }
+        }
+        for (int b = 0; b < m.nb; b++) {
+            const unsigned long long mk = m.b[b].mask;
+            const R cc = (R)((__popcll(uk & mk) == 1) ? m.b[b].cdiff : m.b[b].ceq);
+            const unsigned long long kp = uk ^ mk;
+#pragma unroll
+            for (int c = 0; c < NC; c++)
+                if (c < ncols) {
+                    const C w = in[c * ld + kp];
+                    ar[c] = fma(cc, w.x, ar[c]);
+                    ai[c] = fma(cc, w.y, ai[c]);
+                }
+        }
+        for (int s = 0; s < m.N; s++) {
+            const unsigned long long kp = uk ^ (1ull << s);
+            const R sg = ((uk >> s) & 1ull) ? (R)1 : (R)-1;
+#pragma unroll
+            for (int c = 0; c < NC; c++)
+                if (c < ncols) {
+                    const C w = in[c * ld + kp];
+                    Fr[c] += w.x; Fi[c] += w.y;
+                    Gr[c] = fma(sg, w.x, Gr[c]); Gi[c] = fma(sg, w.y, Gi[c]);
+                }
+        }
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+            if (c < ncols) {
+                const R fx = (R)f.fx[c], fy = (R)f.fy[c];
+                C o;
+                o.x = fma(-fy, Gi[c], fma(fx, Fr[c], ar[c]));
+                o.y = fma(fy, Gr[c], fma(fx, Fi[c], ai[c]));
+                out[c * ld + k] = o;
+            }
+    }
+}
+
+template <typename R>
+void launch_hv(const DevModel& m, const void* in, void* out, int64_t D, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    k_hv<R><<<grid_for(D, 256, SMS * 16), 256, 0, s>>>(m, (const C*)in, (C*)out, (long long)D);
+    ESC_CUDA(cudaGetLastError());
+}
+
+template <typename R>
+void launch_hv_batched(const DevModel& m, const DevFields& f, const void* in, void* out, int ncols, int64_t ld,
+                       int64_t D, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    const int g = grid_for(D, 256, SMS * 16);
+    const C* pi = (const C*)in;
+    C* po = (C*)out;
+    if (ncols <= 1) k_hv_batched<R, 1><<<g, 256, 0, s>>>(m, f, pi, po, D, ld, ncols);
+    else if (ncols <= 2) k_hv_batched<R, 2><<<g, 256, 0, s>>>(m, f, pi, po, D, ld, ncols);
+    else if (ncols <= 4) k_hv_batched<R, 4><<<g, 256, 0, s>>>(m, f, pi, po, D, ld, ncols);
+    else if (ncols <= 8) k_hv_batched<R, 8><<<g, 256, 0, s>>>(m, f, pi, po, D, ld, ncols);
+    else k_hv_batched<R, 16><<<g, 256, 0, s>>>(m, f, pi, po, D, ld, ncols);
+    ESC_CUDA(cudaGetLastError());
+}
+
+// =============================================================================================
+// Operator strings (src/Observables.h: single-site ops :429-521, currents :161-470, totals)
+// =============================================================================================
+template <typename R>
+__global__ void __launch_bounds__(256) k_apply(const __grid_constant__ DevOp op,
+                                               const typename V2<R>::T* __restrict__ in,
+                                               typename V2<R>::T* __restrict__ out, long long D) {
+    typedef typename V2<R>::T C;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < D; k += stride) {
+        R ar = 0, ai = 0;
+        for (int t = 0; t < op.nt; t++) {
+            const unsigned long long k0 = (unsigned long long)k ^ op.flip[t];
+            const unsigned int fac = op.fac[t];
+            const int nf = fac & 3;
+            double cr = op.cre[t], ci = op.cim[t];
+            unsigned long long ket = k0;
+            for (int q = 0; q < nf; q++) {
+                const int s = (fac >> (2 + 8 * q)) & 63;
+                const int o = (fac >> (8 + 8 * q)) & 3;
+                const double h = ((ket >> s) & 1ull) ? -0.5 : 0.5;
+                if (o == 1) { cr *= 0.5; ci *= 0.5; ket ^= 1ull << s; }               // S^x: 1/2, flip
+                else if (o == 2) { const double nr = -ci * h, ni = cr * h; cr = nr; ci = ni; ket ^= 1ull << s; }  // S^y: +-i/2
+                else { cr *= h; ci *= h; }                                            // S^z: +-1/2
+            }
+            const C w = in[k0];
+            const R r = (R)cr, i = (R)ci;
+            ar = fma(r, w.x, ar); ar = fma(-i, w.y, ar);
+            ai = fma(r, w.y, ai); ai = fma(i, w.x, ai);
+        }
+        C o; o.x = ar; o.y = ai;
+        out[k] = o;
+    }
+}
+
+template <typename R>
+void launch_apply(const DevOp& op, const void* in, void* out, int64_t D, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    k_apply<R><<<grid_for(D, 256, SMS * 16), 256, 0, s>>>(op, (const C*)in, (C*)out, (long long)D);
+    ESC_CUDA(cudaGetLastError());
+}
+
+// =============================================================================================
+// Deterministic reductions (double accumulation, fixed grid, fixed butterfly tree)
+// =============================================================================================
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NV], double* dst) {
+    // 256 threads: warp butterflies, then 8 warp results summed in warp order by warp 0.
+    __shared__ double sm[8][NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0)
+#pragma unroll
+        for (int q = 0; q < NV; q++) sm[w][q] = v[q];
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double s = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += sm[i][threadIdx.x];
+        dst[threadIdx.x] = s;
+    }
+    __syncthreads();
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_dot_partial(const typename V2<R>::T* __restrict__ a,
+                                                     const typename V2<R>::T* __restrict__ b, long long n,
+                                                     double* __restrict__ partials) {
+    double v[2] = {0.0, 0.0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double xr = a[i].x, xi = a[i].y, yr = b[i].x, yi = b[i].y;
+        v[0] += xr * yr + xi * yi;
+        v[1] += xr * yi - xi * yr;
+    }
+    block_reduce_store<2>(v, partials + 2 * blockIdx.x);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_nrm2_partial(const typename V2<R>::T* __restrict__ a, long long n,
+                                                      double* __restrict__ partials) {
+    double v[1] = {0.0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double xr = a[i].x, xi = a[i].y;
+        v[0] += xr * xr + xi * xi;
+    }
+    block_reduce_store<1>(v, partials + blockIdx.x);
+}
+
+// Sum NV-vectors of nparts partials (stride NV) in a fixed order into dst[NV].
+template <int NV>
+__global__ void __launch_bounds__(256) k_finalize(const double* __restrict__ partials, int nparts,
+                                                  double* __restrict__ dst) {
+    double v[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) v[q] = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x)
+#pragma unroll
+        for (int q = 0; q < NV; q++) v[q] += partials[(size_t)i * NV + q];
+    block_reduce_store<NV>(v, dst);
+}
+
+template <typename R>
+void launch_dot(const void* a, const void* b, int64_t n, double* partials, double* dst, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    const int g = red_blocks(n);
+    k_dot_partial<R><<<g, 256, 0, s>>>((const C*)a, (const C*)b, n, partials);
+    k_finalize<2><<<1, 256, 0, s>>>(partials, g, dst);
+    ESC_CUDA(cudaGetLastError());
+}
+
+template <typename R>
+void launch_nrm2(const void* a, int64_t n, double* partials, double* dst, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    const int g = red_blocks(n);
+    k_nrm2_partial<R><<<g, 256, 0, s>>>((const C*)a, n, partials);
+    k_finalize<1><<<1, 256, 0, s>>>(partials, g, dst);
+    ESC_CUDA(cudaGetLastError());
+}
+
+// w = (w - alpha v) - beta u ; |w|^2 partials.  Mirrors V2 - alpha*V1 - beta*V0
+// (src/DynLanczosSolver.h:96) with complex alpha and real beta.
+template <typename R>
+__global__ void __launch_bounds__(256) k_lanczos_update(typename V2<R>::T* __restrict__ w,
+                                                        const typename V2<R>::T* __restrict__ v,
+                                                        const typename V2<R>::T* __restrict__ u,
+                                                        const double* __restrict__ d_alpha,
+                                                        const double* __restrict__ d_beta2, long long n,
+                                                        double* __restrict__ partials) {
+    typedef typename V2<R>::T C;
+    const R are = (R)d_alpha[0], aim = (R)d_alpha[1];
+    const R be = d_beta2 ? (R)sqrt(d_beta2[0]) : (R)0;   // beta = |w_prev| = sqrt(|w_prev|^2)
+    double acc[1] = {0.0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        C x = w[i];
+        const C y = v[i];
+        x.x = x.x - (are * y.x - aim * y.y);
+        x.y = x.y - (are * y.y + aim * y.x);
+        if (u) {
+            const C z = u[i];
+            x.x = x.x - be * z.x;
+            x.y = x.y - be * z.y;
+        }
+        w[i] = x;
+        acc[0] += (double)x.x * (double)x.x + (double)x.y * (double)x.y;
+    }
+    block_reduce_store<1>(acc, partials + blockIdx.x);
+}
+
+template <typename R>
+void launch_lanczos_update(void* w, const void* v, const void* u, const double* d_alpha, const double* d_beta2,
+                           int64_t n, double* partials, double* dst, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    const int g = red_blocks(n);
+    k_lanczos_update<R><<<g, 256, 0, s>>>((C*)w, (const C*)v, (const C*)u, d_alpha, d_beta2, n, partials);
+    k_finalize<1><<<1, 256, 0, s>>>(partials, g, dst);
+    ESC_CUDA(cudaGetLastError());
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_scale_rsqrt(const typename V2<R>::T* in, typename V2<R>::T* out,
+                                                     const double* __restrict__ d_nrm2, long long n) {
+    typedef typename V2<R>::T C;
+    // |w| = 0 (Krylov space exhausted) leaves a zero vector instead of NaNs; the host reports it.
+    const double nrm = sqrt(d_nrm2[0]);
+    const double inv_ok = nrm > 0.0 ? 1.0 : 0.0;
+    const double den = nrm > 0.0 ? nrm : 1.0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const C x = in[i];
+        C y;
+        y.x = (R)(inv_ok * ((double)x.x / den));
+        y.y = (R)(inv_ok * ((double)x.y / den));
+        out[i] = y;
+    }
+}
+
+template <typename R>
+void launch_scale_rsqrt(const void* in, void* out, const double* d_nrm2, int64_t n, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    k_scale_rsqrt<R><<<grid_for(n, 256, SMS * 16), 256, 0, s>>>((const C*)in, (C*)out, d_nrm2, n);
+    ESC_CUDA(cudaGetLastError());
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_axpby(const typename V2<R>::T* x, const typename V2<R>::T* y,
+                                               typename V2<R>::T* out, double ar, double ai, double br, double bi,
+                                               long long n) {
+    typedef typename V2<R>::T C;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const C p = x[i], q = y[i];
+        C o;
+        o.x = (R)(ar * p.x - ai * p.y + br * q.x - bi * q.y);
+        o.y = (R)(ar * p.y + ai * p.x + br * q.y + bi * q.x);
+        out[i] = o;
+    }
+}
+
+template <typename R>
+void launch_axpby(const void* x, const void* y, void* out, cplx a, cplx b, int64_t n, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    k_axpby<R><<<grid_for(n, 256, SMS * 16), 256, 0, s>>>((const C*)x, (const C*)y, (C*)out, a.real(), a.imag(),
+                                                         b.real(), b.imag(), n);
+    ESC_CUDA(cudaGetLastError());
+}
+
+// r[j] = sum_k conj(L_j[k]) w[k] for j < m, in groups of JB columns; partials [m][G][2].
+template <typename R, int JB>
+__global__ void __launch_bounds__(256) k_gemv_h(const typename V2<R>::T* __restrict__ L, long long ld, int m,
+                                                const typename V2<R>::T* __restrict__ w, long long n,
+                                                double* __restrict__ partials) {
+    const int G = gridDim.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (int j0 = 0; j0 < m; j0 += JB) {
+        double v[2 * JB];
+#pragma unroll
+        for (int q = 0; q < 2 * JB; q++) v[q] = 0.0;
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            const double yr = w[i].x, yi = w[i].y;
+#pragma unroll
+            for (int q = 0; q < JB; q++)
+                if (j0 + q < m) {
+                    const typename V2<R>::T x = L[(long long)(j0 + q) * ld + i];
+                    v[2 * q] += (double)x.x * yr + (double)x.y * yi;
+                    v[2 * q + 1] += (double)x.x * yi - (double)x.y * yr;
+                }
+        }
+        __shared__ double out[2 * JB];
+        block_reduce_store<2 * JB>(v, out);
+        if (threadIdx.x < 2 * JB && j0 + (int)threadIdx.x / 2 < m)
+            partials[((size_t)(j0 + threadIdx.x / 2) * G + blockIdx.x) * 2 + (threadIdx.x & 1)] = out[threadIdx.x];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_finalize_rows(const double* __restrict__ partials, int G, int m,
+                                                       double* __restrict__ r) {
+    // one block per row j
+    const int j = blockIdx.x;
+    double v[2] = {0.0, 0.0};
+    for (int i = threadIdx.x; i < G; i += blockDim.x) {
+        v[0] += partials[((size_t)j * G + i) * 2];
+        v[1] += partials[((size_t)j * G + i) * 2 + 1];
+    }
+    block_reduce_store<2>(v, r + 2 * j);
+}
+
+template <typename R>
+void launch_gemv_h(const void* L, int64_t ld, int m, const void* w, int64_t n, double* partials,
+                   int64_t partials_cap, double* r, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    if (m <= 0) return;
+    int g = red_blocks(n);
+    while ((int64_t)m * g * 2 > partials_cap && g > 1) g = (g + 1) / 2;
+    k_gemv_h<R, 4><<<g, 256, 0, s>>>((const C*)L, ld, m, (const C*)w, n, partials);
+    k_finalize_rows<<<m, 256, 0, s>>>(partials, g, m, r);
+    ESC_CUDA(cudaGetLastError());
+}
+
+// w[k] -= sum_j L_j[k] r_j (complex r, double accumulation)
+template <typename R>
+__global__ void __launch_bounds__(256) k_gemv_sub(const typename V2<R>::T* __restrict__ L, long long ld, int m,
+                                                  const double* __restrict__ r, typename V2<R>::T* __restrict__ w,
+                                                  long long n) {
+    extern __shared__ double rs[];
+    for (int q = threadIdx.x; q < 2 * m; q += blockDim.x) rs[q] = r[q];
+    __syncthreads();
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        double sr = 0.0, si = 0.0;
+        for (int j = 0; j < m; j++) {
+            const typename V2<R>::T x = L[(long long)j * ld + i];
+            const double cr = rs[2 * j], ci = rs[2 * j + 1];
+            sr += (double)x.x * cr - (double)x.y * ci;
+            si += (double)x.x * ci + (double)x.y * cr;
+        }
+        typename V2<R>::T y = w[i];
+        y.x = (R)((double)y.x - sr);
+        y.y = (R)((double)y.y - si);
+        w[i] = y;
+    }
+}
+
+template <typename R>
+void launch_gemv_sub(const void* L, int64_t ld, int m, const double* r, void* w, int64_t n, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    if (m <= 0) return;
+    k_gemv_sub<R><<<grid_for(n, 256, SMS * 16), 256, 2 * m * sizeof(double), s>>>((const C*)L, ld, m, r, (C*)w, n);
+    ESC_CUDA(cudaGetLastError());
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_lincomb(const typename V2<R>::T* __restrict__ L, long long ld, int m,
+                                                 const double* __restrict__ z, typename V2<R>::T* __restrict__ out,
+                                                 long long n) {
+    extern __shared__ double zs[];
+    for (int q = threadIdx.x; q < m; q += blockDim.x) zs[q] = z[q];
+    __syncthreads();
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        double sr = 0.0, si = 0.0;
+        for (int j = 0; j < m; j++) {
+            const typename V2<R>::T x = L[(long long)j * ld + i];
+            sr += (double)x.x * zs[j];
+            si += (double)x.y * zs[j];
+        }
+        typename V2<R>::T y;
+        y.x = (R)sr;
+        y.y = (R)si;
+        out[i] = y;
+    }
+}
+
+template <typename R>
+void launch_lincomb(const void* L, int64_t ld, int m, const double* z, void* out, int64_t n, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    k_lincomb<R><<<grid_for(n, 256, SMS * 16), 256, m * sizeof(double), s>>>((const C*)L, ld, m, z, (C*)out, n);
+    ESC_CUDA(cudaGetLastError());
+}
+
+__global__ void k_c128_to_c64(const double2* in, float2* out, long long n) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        out[i] = make_float2((float)in[i].x, (float)in[i].y);
+}
+__global__ void k_c64_to_c128(const float2* in, double2* out, long long n) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        out[i] = make_double2((double)in[i].x, (double)in[i].y);
+}
+void launch_convert_c128_to_c64(const void* in, void* out, int64_t n, cudaStream_t s) {
+    k_c128_to_c64<<<grid_for(n, 256, SMS * 16), 256, 0, s>>>((const double2*)in, (float2*)out, n);
+    ESC_CUDA(cudaGetLastError());
+}
+void launch_convert_c64_to_c128(const void* in, void* out, int64_t n, cudaStream_t s) {
+    k_c64_to_c128<<<grid_for(n, 256, SMS * 16), 256, 0, s>>>((const float2*)in, (double2*)out, n);
+    ESC_CUDA(cudaGetLastError());
+}
+
+// Counter-based complex normal start vector: SplitMix64 (Steele, Lea & Flood 2014) hashes of
+// (seed, 2k) and (seed, 2k+1) -> two uniforms -> Box-Muller.  Not normalised here.
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+template <typename R>
+__global__ void k_start_normal(unsigned long long seed, typename V2<R>::T* out, long long n) {
+    const unsigned long long base = splitmix64(seed);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const unsigned long long h1 = splitmix64(base ^ (2ull * (unsigned long long)i));
+        const unsigned long long h2 = splitmix64(base ^ (2ull * (unsigned long long)i + 1ull));
+        const double u1 = (double)((h1 >> 11) + 1ull) * 0x1.0p-53;   // (0, 1]
+        const double u2 = (double)(h2 >> 11) * 0x1.0p-53;            // [0, 1)
+        const double r = sqrt(-2.0 * log(u1));
+        double sn, cs;
+        sincospi(2.0 * u2, &sn, &cs);
+        typename V2<R>::T o;
+        o.x = (R)(r * cs);
+        o.y = (R)(r * sn);
+        out[i] = o;
+    }
+}
+template <typename R>
+void launch_start_normal(uint64_t seed, void* out, int64_t n, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    k_start_normal<R><<<grid_for(n, 256, SMS * 16), 256, 0, s>>>(seed, (C*)out, n);
+    ESC_CUDA(cudaGetLastError());
+}
+
+// explicit instantiations
+#define ESC_INST(R)                                                                                        \
+    template void launch_hv<R>(const DevModel&, const void*, void*, int64_t, cudaStream_t);                \
+    template void launch_hv_batched<R>(const DevModel&, const DevFields&, const void*, void*, int, int64_t, \
+                                       int64_t, cudaStream_t);                                             \
+    template void launch_apply<R>(const DevOp&, const void*, void*, int64_t, cudaStream_t);                \
+    template void launch_dot<R>(const void*, const void*, int64_t, double*, double*, cudaStream_t);        \
+    template void launch_nrm2<R>(const void*, int64_t, double*, double*, cudaStream_t);                    \
+    template void launch_lanczos_update<R>(void*, const void*, const void*, const double*, const double*,  \
+                                           int64_t, double*, double*, cudaStream_t);                       \
+    template void launch_scale_rsqrt<R>(const void*, void*, const double*, int64_t, cudaStream_t);         \
+    template void launch_axpby<R>(const void*, const void*, void*, cplx, cplx, int64_t, cudaStream_t);      \
+    template void launch_gemv_h<R>(const void*, int64_t, int, const void*, int64_t, double*, int64_t,      \
+                                   double*, cudaStream_t);                                                 \
+    template void launch_gemv_sub<R>(const void*, int64_t, int, const double*, void*, int64_t, cudaStream_t); \
+    template void launch_lincomb<R>(const void*, int64_t, int, const double*, void*, int64_t, cudaStream_t); \
+    template void launch_start_normal<R>(uint64_t, void*, int64_t, cudaStream_t);
+ESC_INST(double)
+ESC_INST(float)
+
+}  // namespace esc

@@ -1,0 +1,205 @@
+/*
+ * esc.h -- C ABI of the GB300 (sm_103a) Lanczos exact-diagonalisation library.
+ *
+ * Drop-in for the Lanczos path of fengshi96/EnergySpinCurrents ("LanczosCond"): the spin-1/2
+ * Kitaev(-Heisenberg) honeycomb model (and the Heisenberg chain) on the full 2^N basis, its
+ * ground state, the spin-current / energy-current / single-site operators applied to it, and the
+ * dynamical correlation spectra S(omega).
+ *
+ * The reference has no library API: its seams are C++ member functions taking Eigen vectors.
+ * Each entry point below names the reference function it replaces (file:line in the reference).
+ *
+ * Conventions
+ *   - Basis order is the reference's: index k in [0, 2^N), bit s of k = site s, bit 0 = spin up
+ *     (S^z = +1/2)  (src/QuantumBasis.h:36-60).
+ *   - Vectors are interleaved complex: ESC_C128 = pairs of double, ESC_C64 = pairs of float.
+ *   - Pointers are host memory unless ESC_DEVICE_PTR is set in `flags`, in which case they are
+ *     device pointers on the handle's device.  Host pointers are copied in and out inside the
+ *     call.  Calls on one handle are serial; each handle owns one CUDA stream and every call
+ *     returns with that stream synchronised unless ESC_ASYNC is set (device pointers only).
+ *   - Scalars (alpha, beta, E0, spectra) are always double.
+ *   - No call throws; every call returns an esc_status and esc_last_error() explains failures.
+ */
+#ifndef ESC_H
+#define ESC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    ESC_OK = 0,
+    ESC_ERR_PARAM = 1,     /* bad or missing parameter (reference: std::invalid_argument) */
+    ESC_ERR_MEMORY = 2,    /* device or host allocation failed / problem too large         */
+    ESC_ERR_CUDA = 3,      /* CUDA runtime error                                           */
+    ESC_ERR_NUMERIC = 4,   /* eigensolver failure, NaN in alpha/beta (reference: runtime_error) */
+    ESC_ERR_STATE = 5,     /* call order (e.g. spectrum before a ground state)             */
+    ESC_ERR_TIMEOUT = 6    /* a bounded device wait gave up                                */
+} esc_status;
+
+typedef enum { ESC_C128 = 0, ESC_C64 = 1 } esc_dtype;
+
+enum { ESC_DEVICE_PTR = 1, ESC_ASYNC = 2 };
+
+/* Operator identifiers for esc_apply_op (reference: Observables::ApplyOp, src/Observables.h:24-67,
+ * plus the totals of :448-470, :664-699). */
+typedef enum {
+    ESC_OP_I = 0, ESC_OP_SX, ESC_OP_SY, ESC_OP_SZ, ESC_OP_SP, ESC_OP_SM, ESC_OP_SPE3, ESC_OP_SME3,
+    ESC_OP_SXSYSZ, ESC_OP_JSX, ESC_OP_JSY, ESC_OP_JSZ, ESC_OP_JEX, ESC_OP_JEY, ESC_OP_JEXJEYJEZ,
+    ESC_OP_JSXJSYJSZ, ESC_OP_JSX_TOTAL, ESC_OP_JSY_TOTAL, ESC_OP_JSZ_TOTAL, ESC_OP_JEX_TOTAL,
+    ESC_OP_JEY_TOTAL, ESC_OP_JS_TOTAL, ESC_OP_JE_TOTAL, ESC_OP_COUNT
+} esc_op;
+
+/* Dynamics kinds (reference: StartDynamics dispatch, src/dynamics.h:43-60). */
+typedef enum { ESC_DYN_JEJE = 0, ESC_DYN_JSJS = 1, ESC_DYN_LOCALSZSZ = 2 } esc_dyn_kind;
+
+/* Spectrum method: Ritz = Lehmann sum over the ground-state Ritz pairs (the reference,
+ * src/dynamics.h:277-307); CF = continued fraction from A|gs> (extension). */
+typedef enum { ESC_DYNMODE_RITZ = 0, ESC_DYNMODE_CF = 1 } esc_dyn_mode;
+
+typedef enum { ESC_START_REFUNIFORM = 0, ESC_START_NORMAL = 1 } esc_start_kind;
+
+/* Parameter set.  Keys and defaults follow ConstVariables (src/ParametersEngine.h:21-149);
+ * fields marked EXT are optional keys this library adds, with defaults equal to the reference's
+ * hard-wired constants so that an unmodified reference input file gives the reference result. */
+typedef struct {
+    int Lx, Ly;                 /* NumberofSitesLx / NumberofSitesLy                          */
+    int pbcx, pbcy;             /* IsPeriodicX / IsPeriodicY                                   */
+    int seed;                   /* RandomSeed                                                  */
+    char model[32];             /* Model: Kitaev | HeisenbergChain                             */
+    char solver[16];            /* Solver: none (Lanczos) | ED                                 */
+    char lanctype[16];          /* LancType: OnlyEgs | GS | All                                */
+    double Kxx, Kyy, Kzz;
+    double Bxx, Byy, Bzz;
+    double temperature;         /* read, unused (as in the reference)                          */
+    double lanczos_eps;         /* LanczosEps                                                  */
+    int lanczos_steps;          /* LanczosSteps (default 200)                                  */
+    int threads;                /* Threads (host threads for CPU-side work)                    */
+    int local_skw;              /* LocalSkw -> spin-current dynamics (main.cpp:98-104)         */
+    int spin_curr_dyn;          /* SpinCurrDynamics (read, unused by the reference main)       */
+    int energy_curr_dyn;        /* EnergyCurrDynamics                                          */
+    /* EXT */
+    double jheis;               /* Jheis: Heisenberg J on every nearest-neighbour bond (0)     */
+    int omega_steps;            /* OmegaSteps: omega = k*DOmega, k=0..OmegaSteps (1000)        */
+    double domega;              /* DOmega (0.002)                                              */
+    double eta;                 /* Eta (0.005)                                                 */
+    int dyn_mode;               /* DynMode: Ritz | CF (Ritz)                                   */
+    int dyn_lanczos_steps;      /* DynLanczosSteps for CF (LanczosSteps)                       */
+    int precision;              /* Precision: fp64 | mixed (fp64)                              */
+    int start_vector;           /* StartVector: RefUniform | Normal (RefUniform)               */
+    int local_szsz_dyn;         /* LocalSzSzDynamics: run LocalDynSzSz from main (0)           */
+    int reortho;                /* Reortho: 1 = full reorthogonalisation (reference), 0 = off  */
+} esc_params;
+
+/* Ground-state Lanczos configuration. */
+typedef struct {
+    int steps;                  /* MAXiter (LanczosSteps)                                      */
+    double eps;                 /* LanczosEps                                                  */
+    int lanctype;               /* 0 OnlyEgs, 1 GS, 2 All                                      */
+    int reortho;                /* 1 = full Gram-Schmidt against every stored vector           */
+    esc_dtype dtype;            /* storage/arithmetic of the Krylov vectors                    */
+} esc_lanczos_cfg;
+
+/* Dynamics configuration. */
+typedef struct {
+    int kind;                   /* esc_dyn_kind                                                */
+    int mode;                   /* esc_dyn_mode                                                */
+    int omega_steps;            /* rows = omega_steps + 1                                      */
+    double domega, eta;
+    int cf_steps;               /* continued-fraction Lanczos steps (CF mode)                  */
+    esc_dtype dtype;            /* CF mode: precision of the CF Lanczos vectors                */
+} esc_dyn_cfg;
+
+typedef struct esc_handle esc_handle;
+
+/* ---- parameters -------------------------------------------------------------------------- */
+
+/* Fill `p` with the reference defaults (LanczosSteps=200, Threads=1, omega grid 1001 x 0.002,
+ * eta 0.005, Ritz mode, fp64, reference start vector). */
+esc_status esc_params_default(esc_params* p);
+
+/* Parse a reference input file.  Replaces ConstVariables::Initialize and its matchers
+ * (src/ParametersEngine.h:53-149, :157-229): first line whose key matches exactly and whose
+ * value parses wins; a missing mandatory key fails with "<Key>= argument is missing in the
+ * input file!"; LocalSkw/SpinCurrDynamics/EnergyCurrDynamics require LancType=All. */
+esc_status esc_params_from_file(const char* path, esc_params* p, char* errbuf, size_t errlen);
+
+/* Neighbour table N x 3 (columns 0=z, 1=y, 2=x; -1 = none) of the cluster described by `p`,
+ * computed on the host without a device.  Replaces Lattice::Honeycomb1 / Lattice::Chain
+ * (src/Lattice.h:434-576, :60-136). */
+esc_status esc_lattice(const esc_params* p, int* neigh, int* nsites);
+
+/* ---- handle --------------------------------------------------------------------------------- */
+
+/* Build lattice, bond tables and device state.  Replaces the construction sequence
+ * Lattice -> QBasis -> Hamiltonian(TightB_Ham, Diagonal) of main.cpp:56-73
+ * (src/Lattice.h:37-58, src/QuantumBasis.h:36-46, src/Hamiltonian.h:44-54, :94-206, :331-377). */
+esc_status esc_create(const esc_params* p, esc_handle** out);
+esc_status esc_destroy(esc_handle* h);
+const char* esc_last_error(const esc_handle* h);   /* h may be NULL: last error of this thread */
+
+int esc_num_sites(const esc_handle* h);
+int64_t esc_dim(const esc_handle* h);
+/* Neighbour table N x 3 (columns 0=z, 1=y, 2=x; -1 = none), Lattice::N1neigh_
+ * (src/Lattice.h:29, :497-564). */
+esc_status esc_neighbors(const esc_handle* h, int* neigh);
+/* The handle's CUDA stream (cudaStream_t), for callers that order their own work with it. */
+void* esc_stream(esc_handle* h);
+
+/* ---- operators -------------------------------------------------------------------------------- */
+
+/* out = H in.  Replaces Hamiltonian::MatrixVectorMult (src/Hamiltonian.h:480-557); in != out. */
+esc_status esc_hv(esc_handle* h, const void* in, void* out, esc_dtype dt, int flags);
+
+/* OUT[:, c] = H(c) IN[:, c] for ncols columns stored with leading dimension ld (elements).
+ * `fields` (ncols x 3 doubles: Bxx, Byy, Bzz per column) may be NULL to use the handle's field
+ * for every column.  Batched form of MatrixVectorMult; no reference counterpart. */
+esc_status esc_hv_batched(esc_handle* h, const void* in, void* out, int ncols, int64_t ld,
+                          const double* fields, esc_dtype dt, int flags);
+
+/* out = Op(site) in.  Replaces Observables::ApplyOp and the Apply* members
+ * (src/Observables.h:24-67, :161-470, :488-607, :664-699).  `site` is ignored for totals. */
+esc_status esc_apply_op(esc_handle* h, int op, int site, const void* in, void* out, esc_dtype dt,
+                        int flags);
+
+/* Reference start vector (src/DynLanczosSolver.h:57-59, :465-474) or the counter-based normal
+ * start vector, normalised, in basis order. */
+esc_status esc_start_vector(esc_handle* h, int kind, int seed, void* out, esc_dtype dt, int flags);
+
+/* ---- solvers ----------------------------------------------------------------------------------- */
+
+/* Ground-state Lanczos.  Replaces DynLanczosSolver::Lanczos_Nirav (src/DynLanczosSolver.h:38-239)
+ * including TriDiag (:371-414).  `start` (may be NULL: the handle's configured start vector) is
+ * normalised by the call.  On return: alpha[0..steps-1], beta[0..steps] (beta[0] = 0), ritz
+ * [0..steps-1] ascending, E0 = ritz[0]; gs_out (may be NULL) receives |gs> = PsiAll[0].
+ * Arrays must hold cfg->steps (+1 for beta) entries.  The Krylov basis and the tridiagonal
+ * eigenvectors stay in the handle for esc_spectrum (Ritz mode). */
+esc_status esc_lanczos_gs(esc_handle* h, const esc_lanczos_cfg* cfg, const void* start, int flags,
+                          double* E0, double* alpha, double* beta, double* ritz, int* steps,
+                          void* gs_out);
+
+/* Dynamical correlations of the last ground state.  Replaces DynJeJe / DynJsJs / LocalDynSzSz
+ * (src/dynamics.h:345-460, :222-341, :64-217).  `out` receives (omega_steps+1) x ncols doubles in
+ * the column order of the reference's JeJe_ (6) / JsJs_ (15) / 2SSLocal_ (9) files. */
+esc_status esc_spectrum(esc_handle* h, const esc_dyn_cfg* cfg, double* out, int* nrows, int* ncols);
+
+/* Ground-state expectation values printed by Observables::measureLocalS / measureLocalJe
+ * (src/Observables.h:107-128, :88-104): s_out N x 3 complex (<Sx>,<Sy>,<Sz>), je_out N x 2
+ * complex (<Jex_i>,<Jey_i>).  Either may be NULL. */
+esc_status esc_measure_local(esc_handle* h, double* s_out, double* je_out);
+
+/* Gradients (extension, no reference counterpart).  dE0[3] = dE0/d{K, J, h} by
+ * Hellmann-Feynman on the last ground state, with K the common Kitaev coupling
+ * (Kxx=Kyy=Kzz=K) and h the [111] field (Bxx=Byy=Bzz=-h/sqrt3).  If dS is non-NULL it receives
+ * (omega_steps+1) x 3 derivatives d Im S_tt(omega) / d{K,J,h} of the CF-mode total-current
+ * spectrum of `kind`, by reverse mode through the continued fraction and the dynamical Lanczos
+ * recurrence (vectors recomputed, not stored). */
+esc_status esc_grad(esc_handle* h, const esc_dyn_cfg* cfg, double* dE0, double* dS);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ESC_H */

@@ -1,0 +1,217 @@
+"""GPU library (C ABI, sm_103a kernels) against the golden vectors of the reference's own code
+and against the CPU oracle.  Tolerances are the bar of the port: E0 to 1e-10 relative and S(omega)
+to 1e-8 absolute on the same seeded start vector; H.v and operators to ~1e-14 relative (double
+rounding of a different summation order)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import GOLDEN, golden_names, parse_param_text
+
+pytestmark = pytest.mark.gpu
+esc = pytest.importorskip("energyspincurrents_gb300")
+
+OPS = ["Sx", "Sy", "Sz", "Sp", "Sm", "Spe3", "Sme3", "Jsx", "Jsy", "Jsz", "Jex", "Jey", "JexJeyJez", "JsxJsyJsz"]
+TOTALS = ["JsxTotal", "JsyTotal", "JszTotal", "JexTotal", "JeyTotal"]
+NONDEGENERATE = {"kitaev8", "kitaev12", "aniso12", "kitaev16obc"}   # "midinput": 2-fold degenerate |gs>
+
+
+def golden_handle(name, tmp_path):
+    g = np.load(f"{GOLDEN}/{name}.npz")
+    f = tmp_path / f"{name}.inp"
+    f.write_text(str(g["params"]))
+    P = esc.ConstVariables(str(f))
+    return g, P, esc.Handle(P)
+
+
+def relerr(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_hv_and_diag(name, tmp_path):
+    g, P, h = golden_handle(name, tmp_path)
+    assert (h.neighbors() == g["neigh"]).all()
+    x = O.random_start(int(g["testvec_seed"]), h.D, normalize=False)
+    hx = h.hv(x)
+    assert relerr(hx[: g["hx"].size], g["hx"]) < 1e-14
+    # diagonal: H acting on basis vectors e_k restricted to their own component
+    e = np.zeros(h.D, dtype=np.complex128)
+    for k in (0, 1, h.D // 3, h.D - 1):
+        e[:] = 0; e[k] = 1.0
+        assert h.hv(e)[k] == g["hdiag"][k]          # bit-identical: same operations as the reference
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names() if "proj_Jex" in np.load(f"{GOLDEN}/{n}.npz").files])
+def test_operators(name, tmp_path):
+    g, P, h = golden_handle(name, tmp_path)
+    x = O.random_start(int(g["testvec_seed"]), h.D, normalize=False)
+    y1, y2 = [O.random_start(int(s), h.D, normalize=False) for s in g["probe_seeds"]]
+    proj = lambda o: np.array([np.vdot(y1, o), np.vdot(y2, o), np.vdot(o, o)])
+    for op in OPS:
+        for s in range(h.N):
+            o = h.apply(op, s, x)
+            np.testing.assert_allclose(proj(o), g["proj_" + op][s], rtol=1e-13, atol=1e-12)
+            if "full_" + op in g.files:
+                assert relerr(o, g["full_" + op][s]) < 1e-15
+    for op in TOTALS:
+        o = h.apply(op, 0, x)
+        np.testing.assert_allclose(proj(o), g["proj_" + op], rtol=1e-13, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_lanczos(name, tmp_path):
+    g, P, h = golden_handle(name, tmp_path)
+    r = h.lanczos_gs()                       # reference start vector from RandomSeed
+    n = g["alpha"].size
+    assert r["steps"] == n
+    assert abs(r["E0"] - g["ritz"][0]) <= 1e-10 * abs(g["ritz"][0])
+    # first Lanczos coefficients agree to rounding; later ones stay within 1e-8
+    np.testing.assert_allclose(r["alpha"][:20], g["alpha"][:20], atol=1e-12)
+    np.testing.assert_allclose(r["beta"][1:21], g["beta"][1:21], atol=1e-12)
+    if "psi" in g.files:
+        assert abs(abs(np.vdot(g["psi"], r["gs"])) - 1.0) < 1e-9
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names() if "JeJe" in np.load(f"{GOLDEN}/{n}.npz").files])
+def test_spectra_ritz(name, tmp_path):
+    g, P, h = golden_handle(name, tmp_path)
+    h.lanczos_gs()
+    tol = 1e-8 if name in NONDEGENERATE else 1e-5
+    for key, kind in (("JeJe", "Energy Current"), ("JsJs", "Spin Current"), ("SSLocal", "LocalSzSz")):
+        s = h.spectrum(kind, "Ritz")
+        assert s.shape == g[key].shape
+        err = np.abs(s - g[key]).max()
+        assert err <= tol, (key, err)
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names() if "localS" in np.load(f"{GOLDEN}/{n}.npz").files])
+def test_measure_local(name, tmp_path):
+    g, P, h = golden_handle(name, tmp_path)
+    h.lanczos_gs()
+    s, je = h.measure_local()
+    tol = 1e-9 if name in NONDEGENERATE else 1e-4
+    assert np.abs(s - g["localS"]).max() < tol
+
+
+S3 = 3 ** 0.5
+
+
+def kitaev(Lx=3, Ly=4, J=0.1, h=0.05, **kw):
+    b = -h / S3
+    return dict(Lx=Lx, Ly=Ly, Kxx=-1.0, Kyy=-1.0, Kzz=-1.0, Bxx=b, Byy=b, Bzz=b, jheis=J, **kw)
+
+
+@pytest.mark.parametrize("J", [0.0, 0.1])
+def test_heisenberg_extension_vs_oracle(J):
+    p = kitaev(J=J, seed=0, lanczos_steps=120)
+    h = esc.Handle(p)
+    m = O.Model("Kitaev", 3, 4, 1, 1, -1.0, -1.0, -1.0, p["Bxx"], p["Byy"], p["Bzz"], J, 8, True)
+    x = O.random_start(5, h.D, normalize=False)
+    assert relerr(h.hv(x), m.hv(x)) < 1e-14
+    v0 = O.random_start(0, h.D)
+    r = h.lanczos_gs(start=v0)
+    ro = m.lanczos(v0, 120)
+    assert abs(r["E0"] - ro["ritz"][0]) <= 1e-10 * abs(ro["ritz"][0])
+    w = np.linalg.eigvalsh(m.dense())
+    assert abs(r["E0"] - w[0]) < 1e-9
+
+
+def test_heisenberg_chain_vs_dense():
+    h = esc.Handle(dict(model="HeisenbergChain", Lx=10, Ly=1, pbcx=1, pbcy=0, Kxx=1.0, Kyy=0.9, Kzz=1.1, Bxx=0.1,
+                        Bzz=0.05, lanczos_steps=150, lanctype="GS"))
+    m = O.Model("HeisenbergChain", 10, 1, 1, 0, 1.0, 0.9, 1.1, 0.1, 0.0, 0.05, 0.0, 4, True)
+    x = O.random_start(3, h.D, normalize=False)
+    assert relerr(h.hv(x), m.hv(x)) < 1e-14
+    r = h.lanczos_gs(start=O.random_start(1, h.D))
+    assert abs(r["E0"] - np.linalg.eigvalsh(m.dense())[0]) < 1e-9
+
+
+def test_mixed_precision_hv_and_e0():
+    p = kitaev(J=0.1, seed=0, lanczos_steps=150)
+    h = esc.Handle(p)
+    x = O.random_start(5, h.D)
+    y64 = h.hv(x)
+    y32 = h.hv(x.astype(np.complex64))
+    assert relerr(y32.astype(np.complex128), y64) < 2e-6
+    r64 = h.lanczos_gs(start=x)
+    r32 = h.lanczos_gs(start=x, dtype=np.complex64)
+    assert abs(r32["E0"] - r64["E0"]) < 1e-5 * abs(r64["E0"])
+
+
+def test_cf_spectrum_vs_exact():
+    """CF mode against the exact Lehmann sum of dense ED (8 sites: Krylov space exhausted)."""
+    p = kitaev(Lx=2, Ly=4, J=0.1, seed=0, lanczos_steps=100)
+    h = esc.Handle(p)
+    m = O.Model("Kitaev", 2, 4, 1, 1, -1.0, -1.0, -1.0, p["Bxx"], p["Byy"], p["Bzz"], 0.1, 2, True)
+    H = m.dense()
+    w, V = np.linalg.eigh(H)
+    h.lanczos_gs(start=O.random_start(0, h.D))
+    nw, dw, eta = 300, 0.02, 0.05
+    s = h.spectrum("Energy Current", "CF", omega_steps=nw - 1, domega=dw, eta=eta, cf_steps=256)
+    gs = V[:, 0]
+    jx, jy = m.apply("JexTotal", 0, gs), m.apply("JeyTotal", 0, gs)
+    ox, oy, ot = V.conj().T @ jx, V.conj().T @ jy, V.conj().T @ (jx + jy)
+    om = dw * np.arange(nw)
+    den = om[:, None] - (w[None, :] - w[0]) - 1j * eta
+    S = lambda a, b: (a.conj()[None, :] * b[None, :] / den).sum(1)
+    el = lambda a: np.vdot(gs, a)
+    ex, ey, et = el(jx), el(jy), el(jx + jy)
+    dn = om - 1j * eta
+    ref = np.stack([om, (S(ox, ox) - np.conj(ex) * ex / dn).imag, (S(oy, oy) - np.conj(ey) * ey / dn).imag,
+                    (S(ox, oy) - np.conj(ex) * ey / dn).imag, S(oy, ox).imag,
+                    (S(ot, ot) - np.conj(et) * et / dn).imag], 1)
+    assert np.abs(s - ref).max() < 1e-8
+
+
+def test_batched_hv_matches_single():
+    p = kitaev(J=0.1)
+    h = esc.Handle(p)
+    rng = np.random.default_rng(0)
+    for dt in (np.complex128, np.complex64):
+        V = (rng.standard_normal((5, h.D)) + 1j * rng.standard_normal((5, h.D))).astype(dt)
+        fields = np.array([[-0.02, -0.02, -0.02], [0, 0, 0], [-0.05, -0.05, -0.05], [0.1, 0.2, 0.3], [p["Bxx"]] * 3])
+        out = h.hv_batched(V, fields)
+        for c in range(5):
+            hc = esc.Handle(dict(p, Bxx=fields[c, 0], Byy=fields[c, 1], Bzz=fields[c, 2]))
+            tol = 1e-14 if dt == np.complex128 else 2e-6
+            assert relerr(out[c], hc.hv(V[c])) < tol
+
+
+def test_grad_e0_hellmann_feynman():
+    """dE0/d{K,J,h} against central differences of the GPU ground-state energy."""
+    base = dict(Lx=2, Ly=4, seed=0, lanczos_steps=120)
+
+    def e0(K, J, hf):
+        b = -hf / S3
+        hh = esc.Handle(dict(base, Kxx=K, Kyy=K, Kzz=K, Bxx=b, Byy=b, Bzz=b, jheis=J))
+        return hh, hh.lanczos_gs(start=O.random_start(0, hh.D))["E0"]
+
+    K, J, hf, d = -1.0, 0.1, 0.05, 1e-5
+    hh, _ = e0(K, J, hf)
+    g = hh.grad_E0()
+    fd = [(e0(K + d, J, hf)[1] - e0(K - d, J, hf)[1]) / (2 * d), (e0(K, J + d, hf)[1] - e0(K, J - d, hf)[1]) / (2 * d),
+          (e0(K, J, hf + d)[1] - e0(K, J, hf - d)[1]) / (2 * d)]
+    np.testing.assert_allclose(g, fd, atol=1e-6)
+
+
+def test_deterministic():
+    p = kitaev(J=0.1, seed=0, lanczos_steps=80)
+    a = esc.Handle(p).lanczos_gs()
+    b = esc.Handle(p).lanczos_gs()
+    assert np.array_equal(a["alpha"], b["alpha"]) and np.array_equal(a["gs"], b["gs"])
+
+
+def test_errors_are_reported():
+    h = esc.Handle(kitaev(Lx=2, Ly=4))
+    with pytest.raises(esc.EscError, match="no ground state"):
+        h.spectrum("Energy Current")
+    with pytest.raises(esc.EscError, match="LanczosSteps must be"):
+        h.lanczos_gs(steps=1)
+    with pytest.raises(esc.EscError, match="site out of range"):
+        h.apply("Sx", 99, np.zeros(h.D, np.complex128))
+    with pytest.raises(esc.EscError, match="neighbour"):
+        ho = esc.Handle(dict(kitaev(Lx=4, Ly=4), pbcx=0))
+        ho.apply("JexTotal", 0, np.zeros(ho.D, np.complex128))
