@@ -43,7 +43,8 @@ __global__ void __launch_bounds__(256) k_hv(const __grid_constant__ DevModel m,
             const double q = 0.25 * m.d[b].dz;
             dg += (__popcll(uk & m.d[b].mask) == 1) ? -q : q;
         }
-        dg += m.fz * (double)(m.N - 2 * __popcll(uk));
+        // product rounded before the sum (no FMA contraction), as HDiag += Bzz*SzT does
+        dg = __dadd_rn(dg, __dmul_rn(m.fz, (double)(m.N - 2 * __popcll(uk))));
         const C v = in[k];
         R ar = (R)dg * v.x, ai = (R)dg * v.y;
         for (int b = 0; b < m.nb; b++) {
@@ -90,7 +91,7 @@ __global__ void __launch_bounds__(256) k_hv_batched(const __grid_constant__ DevM
         for (int c = 0; c < NC; c++) {
             ar[c] = ai[c] = Fr[c] = Fi[c] = Gr[c] = Gi[c] = (R)0;
             if (c < ncols) {
-                const R dg = (R)(dgb + f.fz[c] * nz);
+                const R dg = (R)__dadd_rn(dgb, __dmul_rn(f.fz[c], nz));
                 const C v = in[c * ld + k];
                 ar[c] = dg * v.x; ai[c] = dg * v.y;
             }
