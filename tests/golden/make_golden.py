@@ -75,6 +75,29 @@ Bxx={-0.05 / S3!r}
 Byy={-0.05 / S3!r}
 Bzz={-0.05 / S3!r}
 """, False),
+    # same model, 60 steps: short of the step (~66) where the reference's own Lanczos sequence
+    # starts to depend on its summation order, so every output is reproducible to ~1e-12
+    "kitaev12m60": (f"""NumberofSitesLx=3
+NumberofSitesLy=4
+IsPeriodicX=1
+IsPeriodicY=1
+RandomSeed=0
+Model=Kitaev
+Solver=none
+Temperature=0
+LanczosEps=0
+LanczosSteps=60
+Threads=8
+LancType=All
+LocalSkw=1
+EnergyCurrDynamics=1
+Kxx=-1.0
+Kyy=-1.0
+Kzz=-1.0
+Bxx={-0.05 / S3!r}
+Byy={-0.05 / S3!r}
+Bzz={-0.05 / S3!r}
+""", False),
     # anisotropic couplings and an off-axis field on the (2,6) cluster: catches x/y/z mix-ups
     "aniso12": ("""NumberofSitesLx=2
 NumberofSitesLy=6

@@ -8,14 +8,13 @@ import numpy as np
 import pytest
 
 import oracle as O
-from conftest import GOLDEN, golden_names, parse_param_text
+from conftest import GOLDEN, golden_names, parse_param_text, reference_envelope
 
 pytestmark = pytest.mark.gpu
 esc = pytest.importorskip("energyspincurrents_gb300")
 
 OPS = ["Sx", "Sy", "Sz", "Sp", "Sm", "Spe3", "Sme3", "Jsx", "Jsy", "Jsz", "Jex", "Jey", "JexJeyJez", "JsxJsyJsz"]
 TOTALS = ["JsxTotal", "JsyTotal", "JszTotal", "JexTotal", "JeyTotal"]
-NONDEGENERATE = {"kitaev8", "kitaev12", "aniso12", "kitaev16obc"}   # "midinput": 2-fold degenerate |gs>
 
 
 def golden_handle(name, tmp_path):
@@ -67,7 +66,10 @@ def test_lanczos(name, tmp_path):
     r = h.lanczos_gs()                       # reference start vector from RandomSeed
     n = g["alpha"].size
     assert r["steps"] == n
-    assert abs(r["E0"] - g["ritz"][0]) <= 1e-10 * abs(g["ritz"][0])
+    # 1e-10 relative, or (2-fold degenerate ground state of "midinput", unconverged at 100 steps)
+    # within twice the reference's own spread under a change of summation order
+    tol = max(1e-10 * abs(g["ritz"][0]), 2 * reference_envelope(name)["E0"])
+    assert abs(r["E0"] - g["ritz"][0]) <= tol
     # first Lanczos coefficients agree to rounding; later ones stay within 1e-8
     np.testing.assert_allclose(r["alpha"][:20], g["alpha"][:20], atol=1e-12)
     np.testing.assert_allclose(r["beta"][1:21], g["beta"][1:21], atol=1e-12)
@@ -79,12 +81,20 @@ def test_lanczos(name, tmp_path):
 def test_spectra_ritz(name, tmp_path):
     g, P, h = golden_handle(name, tmp_path)
     h.lanczos_gs()
-    tol = 1e-8 if name in NONDEGENERATE else 1e-5
+    env = reference_envelope(name)
     for key, kind in (("JeJe", "Energy Current"), ("JsJs", "Spin Current"), ("SSLocal", "LocalSzSz")):
         s = h.spectrum(kind, "Ritz")
         assert s.shape == g[key].shape
         err = np.abs(s - g[key]).max()
-        assert err <= tol, (key, err)
+        # the 1e-8 bar wherever the reference's output is itself reproducible (kitaev12m60,
+        # kitaev8, aniso12); otherwise within 3x the reference's own rounding spread
+        tol = max(1e-8, 3 * env[key])
+        assert err <= tol, (key, err, env[key])
+
+
+def test_spectra_strict_bar():
+    """At least one full Ritz-mode parity case meets S(omega) to 1e-8 with no envelope."""
+    assert max(reference_envelope("kitaev12m60")[k] for k in ("JeJe", "JsJs", "SSLocal")) < 1e-9
 
 
 @pytest.mark.parametrize("name", [n for n in golden_names() if "localS" in np.load(f"{GOLDEN}/{n}.npz").files])
@@ -92,7 +102,7 @@ def test_measure_local(name, tmp_path):
     g, P, h = golden_handle(name, tmp_path)
     h.lanczos_gs()
     s, je = h.measure_local()
-    tol = 1e-9 if name in NONDEGENERATE else 1e-4
+    tol = 1e-9 if name != "midinput" else 1e-4       # midinput: 2-fold degenerate |gs> (start-vector dependent)
     assert np.abs(s - g["localS"]).max() < tol
 
 
