@@ -22,7 +22,7 @@ _LIB_PATH = os.path.join(_PKG, "_build", "libesc.so")
 
 ESC_OK, ESC_ERR_PARAM, ESC_ERR_MEMORY, ESC_ERR_CUDA, ESC_ERR_NUMERIC, ESC_ERR_STATE, ESC_ERR_TIMEOUT = range(7)
 C128, C64 = 0, 1
-DEVICE_PTR, ASYNC = 1, 2
+DEVICE_PTR, ASYNC, INTERNAL_ORDER = 1, 2, 4
 
 OPS = ["I", "Sx", "Sy", "Sz", "Sp", "Sm", "Spe3", "Sme3", "SxSySz", "Jsx", "Jsy", "Jsz", "Jex", "Jey", "JexJeyJez",
        "JsxJsyJsz", "JsxTotal", "JsyTotal", "JszTotal", "JexTotal", "JeyTotal", "JsTotal", "JeTotal"]
@@ -67,8 +67,8 @@ class DynCfg(ctypes.Structure):
 _lib = None
 
 # every symbol declared in include/esc.h
-EXPORTS = ["esc_params_default", "esc_params_from_file", "esc_lattice", "esc_create", "esc_destroy", "esc_last_error",
-           "esc_num_sites", "esc_dim", "esc_neighbors", "esc_stream", "esc_hv", "esc_hv_batched", "esc_apply_op",
+EXPORTS = ["esc_params_default", "esc_params_from_file", "esc_lattice", "esc_plan", "esc_create", "esc_destroy", "esc_last_error",
+           "esc_num_sites", "esc_dim", "esc_neighbors", "esc_basis_permutation", "esc_stream", "esc_hv", "esc_hv_batched", "esc_apply_op",
            "esc_start_vector", "esc_lanczos_gs", "esc_spectrum", "esc_measure_local", "esc_grad"]
 
 
@@ -88,6 +88,7 @@ def lib():
     L.esc_params_default.argtypes = [P(Params)]
     L.esc_params_from_file.argtypes = [ctypes.c_char_p, P(Params), ctypes.c_char_p, ctypes.c_size_t]
     L.esc_lattice.argtypes = [P(Params), P(ci), P(ci)]
+    L.esc_plan.argtypes = [P(Params), ci, ci, P(ci), P(ci)]
     L.esc_create.argtypes = [P(Params), P(vp)]
     L.esc_destroy.argtypes = [vp]
     L.esc_last_error.argtypes = [vp]
@@ -96,6 +97,7 @@ def lib():
     L.esc_dim.argtypes = [vp]
     L.esc_dim.restype = i64
     L.esc_neighbors.argtypes = [vp, P(ci)]
+    L.esc_basis_permutation.argtypes = [vp, P(ci)]
     L.esc_stream.argtypes = [vp]
     L.esc_stream.restype = vp
     L.esc_hv.argtypes = [vp, vp, vp, ci, ci]
@@ -167,6 +169,20 @@ def lattice(params):
     return out[: 3 * n.value].reshape(n.value, 3)
 
 
+def plan(params, tile_bits=0, low_bits=0):
+    """(bit_of_site, npasses) of the tiled H.v plan, computed on the host."""
+    if not isinstance(params, ConstVariables):
+        params = ConstVariables(**params)
+    N = params.p.Lx * params.p.Ly
+    perm = np.empty(N, dtype=np.int32)
+    n = ctypes.c_int()
+    st = lib().esc_plan(ctypes.byref(params.p), tile_bits, low_bits, perm.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                        ctypes.byref(n))
+    if st != ESC_OK:
+        raise EscError(st, lib().esc_last_error(None).decode())
+    return perm, n.value
+
+
 def _check(h, st):
     if st != ESC_OK:
         raise EscError(st, lib().esc_last_error(h).decode())
@@ -202,11 +218,28 @@ class Handle:
         _check(self.h, lib().esc_neighbors(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
         return out.reshape(self.N, 3)
 
+    def basis_permutation(self):
+        """bit_of_site[s]: position of site s's bit in the internal basis index."""
+        out = np.empty(self.N, dtype=np.int32)
+        _check(self.h, lib().esc_basis_permutation(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return out
+
+    def to_internal(self, v):
+        """Reference-order vector -> internal order (host-side permutation, for tests)."""
+        perm = self.basis_permutation()
+        k = np.arange(self.D, dtype=np.int64)
+        j = np.zeros_like(k)
+        for s in range(self.N):
+            j |= ((k >> s) & 1) << int(perm[s])
+        out = np.empty_like(v)
+        out[j] = v
+        return out
+
     # -- operators ------------------------------------------------------------------------------
-    def hv(self, v, out=None):
+    def hv(self, v, out=None, flags=0):
         v = np.ascontiguousarray(v)
         out = np.empty_like(v) if out is None else out
-        _check(self.h, lib().esc_hv(self.h, _ptr(v), _ptr(out), _dt(v), 0))
+        _check(self.h, lib().esc_hv(self.h, _ptr(v), _ptr(out), _dt(v), flags))
         return out
 
     def hv_device(self, in_ptr, out_ptr, dtype=C128, flags=DEVICE_PTR):

@@ -24,7 +24,7 @@ EXE = os.path.join(OUT, "LanczosCond")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kernels.cu", "hv_tiled.cu"]
-CPP_SOURCES = ["esc_abi.cpp", "params.cpp", "model.cpp", "numerics.cpp", "batched.cpp"]
+CPP_SOURCES = ["esc_abi.cpp", "params.cpp", "model.cpp", "numerics.cpp", "planner.cpp", "batched.cpp"]
 
 
 def _nvcc():

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -18,7 +19,10 @@ struct esc_handle {
     esc_params p{};
     esc::Lattice L;
     std::vector<esc::Bond> bonds;
-    esc::DevModel dm{};
+    esc::DevModel dm{};                 // model on relabelled sites (internal basis order)
+    esc::Plan plan;                     // site relabelling + pass plan of the tiled H.v
+    std::vector<esc::DevPass> passes;
+    esc::DevPerm to_int{}, to_ref{};    // basis permutations reference <-> internal
     int N = 0;
     int64_t D = 0;
     int device = 0;
@@ -103,21 +107,63 @@ void ensure_partials(esc_handle* h, int rows) {
 }
 int64_t part_cap_doubles(esc_handle* h) { return (int64_t)(h->part_bytes / sizeof(double)); }
 
-// Staged input/output: device pointer as-is, host pointer copied through d_io.
+void permute(esc_handle* h, const esc::DevPerm& p, const void* in, void* out, int64_t n, esc_dtype dt) {
+    if (dt == ESC_C64) esc::launch_permute<float>(p, in, out, n, h->stream);
+    else esc::launch_permute<double>(p, in, out, n, h->stream);
+}
+
+// Staged input/output.  The kernels work in the internal basis order; unless the caller says
+// ESC_INTERNAL_ORDER, inputs are permuted in and outputs permuted out (through d_io), and host
+// pointers are copied.  One call handles `cols` vectors of `n` elements with stride `ld`.
 struct Staged {
     const void* in;
     void* out;
+    int64_t ld;
 };
-Staged stage(esc_handle* h, const void* in, void* out, size_t in_bytes, size_t out_bytes, int flags) {
-    if (flags & ESC_DEVICE_PTR) return {in, out};
-    ensure(h->d_io, h->io_bytes, in_bytes + out_bytes);
-    char* base = (char*)h->d_io;
-    if (in) ESC_CUDA(cudaMemcpyAsync(base, in, in_bytes, cudaMemcpyHostToDevice, h->stream));
-    return {in ? base : nullptr, base + in_bytes};
+Staged stage(esc_handle* h, const void* in, void* out, int cols, int64_t ld, esc_dtype dt, int flags) {
+    const size_t es = esize(dt);
+    const int64_t n = h->D;
+    const bool dev = flags & ESC_DEVICE_PTR, internal = flags & ESC_INTERNAL_ORDER;
+    if (dev && internal) return {in, out, ld};
+    const size_t vb = (size_t)n * es;
+    ensure(h->d_io, h->io_bytes, 2 * (size_t)cols * vb);
+    char* A = (char*)h->d_io;              // internal-order input
+    char* B = A + (size_t)cols * vb;       // internal-order output / reference-order staging
+    for (int c = 0; c < cols; c++) {
+        if (!in) break;
+        const char* src = (const char*)in + (size_t)c * ld * es;
+        if (internal) {
+            ESC_CUDA(cudaMemcpyAsync(A + c * vb, src, vb, cudaMemcpyHostToDevice, h->stream));
+        } else if (dev) {
+            permute(h, h->to_int, src, A + c * vb, n, dt);
+        } else {
+            ESC_CUDA(cudaMemcpyAsync(B + c * vb, src, vb, cudaMemcpyHostToDevice, h->stream));
+            permute(h, h->to_int, B + c * vb, A + c * vb, n, dt);
+        }
+    }
+    return {in ? A : nullptr, B, n};
 }
-void unstage(esc_handle* h, const Staged& s, void* out, size_t out_bytes, int flags) {
-    if (!(flags & ESC_DEVICE_PTR) && out) ESC_CUDA(cudaMemcpyAsync(out, s.out, out_bytes, cudaMemcpyDeviceToHost, h->stream));
-    if (!(flags & ESC_ASYNC) || !(flags & ESC_DEVICE_PTR)) sync(h);
+void unstage(esc_handle* h, const Staged& s, void* out, int cols, int64_t ld, esc_dtype dt, int flags) {
+    const size_t es = esize(dt);
+    const int64_t n = h->D;
+    const bool dev = flags & ESC_DEVICE_PTR, internal = flags & ESC_INTERNAL_ORDER;
+    if (!(dev && internal) && out) {
+        const size_t vb = (size_t)n * es;
+        char* A = (char*)h->d_io;
+        for (int c = 0; c < cols; c++) {
+            char* dst = (char*)out + (size_t)c * ld * es;
+            const char* res = (const char*)s.out + (size_t)c * vb;
+            if (internal) {
+                ESC_CUDA(cudaMemcpyAsync(dst, res, vb, cudaMemcpyDeviceToHost, h->stream));
+            } else if (dev) {
+                permute(h, h->to_ref, res, dst, n, dt);
+            } else {
+                permute(h, h->to_ref, res, A + c * vb, n, dt);
+                ESC_CUDA(cudaMemcpyAsync(dst, A + c * vb, vb, cudaMemcpyDeviceToHost, h->stream));
+            }
+        }
+    }
+    if (!(flags & ESC_ASYNC) || !dev) sync(h);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -129,7 +175,7 @@ struct Pipe {
     static constexpr size_t ES = 2 * sizeof(R);
     int64_t D;
     explicit Pipe(esc_handle* hh) : h(hh), D(hh->D) {}
-    void hv(const void* in, void* out) { esc::launch_hv<R>(h->dm, in, out, D, h->stream); }
+    void hv(const void* in, void* out) { esc::launch_hv_tiled<R>(h->dm, h->passes, in, out, D, h->stream); }
     void apply(const esc::DevOp& op, const void* in, void* out) { esc::launch_apply<R>(op, in, out, D, h->stream); }
     void dot(const void* a, const void* b, double* dst) { esc::launch_dot<R>(a, b, D, h->d_part, dst, h->stream); }
     void nrm2(const void* a, double* dst) { esc::launch_nrm2<R>(a, D, h->d_part, dst, h->stream); }
@@ -266,7 +312,7 @@ struct Spectra {
 
     // <gs| A |gs> with A given as terms; uses work vector `slot`.
     cplx expect(const std::vector<esc::OpTerm>& t, int slot, double* d_tmp) {
-        P.apply(esc::make_dev_op(t), h->d_gs, buf(slot));
+        P.apply(esc::make_dev_op(t, &h->plan.perm), h->d_gs, buf(slot));
         P.dot(h->d_gs, buf(slot), d_tmp);
         double r[2];
         ESC_CUDA(cudaMemcpyAsync(r, d_tmp, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -278,7 +324,7 @@ struct Spectra {
     std::vector<cplx> ritz_overlaps(const std::vector<esc::OpTerm>& t, int slot, double* d_r, double* d_tmp,
                                     cplx* elastic) {
         const int M = h->nsteps;
-        P.apply(esc::make_dev_op(t), h->d_gs, buf(slot));
+        P.apply(esc::make_dev_op(t, &h->plan.perm), h->d_gs, buf(slot));
         P.dot(h->d_gs, buf(slot), d_tmp);
         esc::launch_gemv_h<R>(h->d_L, h->L_ld, M, buf(slot), D, h->d_part, part_cap_doubles(h), d_r, h->stream);
         std::vector<double> r(2 * (size_t)M), el(2);
@@ -302,7 +348,7 @@ struct Spectra {
         double* d_b2 = d_a + 2 * K;     // K+1
         ESC_CUDA(cudaMemsetAsync(d_sc, 0, (3 * (size_t)K + 1) * sizeof(double), h->stream));
         int prev = 0, cur = 1, wb = 2;
-        P.apply(esc::make_dev_op(t), h->d_gs, buf(cur));
+        P.apply(esc::make_dev_op(t, &h->plan.perm), h->d_gs, buf(cur));
         P.nrm2(buf(cur), d_b2);
         P.scale(buf(cur), buf(cur), d_b2);
         for (int k = 0; k < K; k++) {
@@ -358,7 +404,22 @@ esc_status esc_create(const esc_params* p, esc_handle** out) {
         esc::build_bonds(*p, h->L, h->bonds);
         h->N = h->L.N;
         h->D = int64_t(1) << h->N;
-        h->dm = esc::make_dev_model(*p, h->L, h->bonds, p->Bxx, p->Byy, p->Bzz);
+        // site relabelling and pass plan of the tiled H.v (planner.cpp)
+        std::vector<std::pair<int, int>> pairs;
+        for (const auto& b : h->bonds)
+            if (b.kx - b.ky != 0.0 || b.kx + b.ky != 0.0) pairs.push_back({b.i, b.j});
+        int T = 13, c = 3;
+        if (const char* e = std::getenv("ESC_TILE_BITS")) T = std::atoi(e);
+        if (const char* e = std::getenv("ESC_TILE_LOW")) c = std::atoi(e);
+        h->plan = esc::make_plan(h->N, pairs, T, c, 200);
+        std::vector<esc::Bond> rb(h->bonds);
+        for (auto& b : rb) { b.i = h->plan.perm[b.i]; b.j = h->plan.perm[b.j]; }
+        h->dm = esc::make_dev_model(*p, h->L, rb, p->Bxx, p->Byy, p->Bzz);
+        h->passes = esc::make_passes(h->plan, h->dm);
+        std::vector<int> inv(h->N), fwd(h->N);
+        for (int s = 0; s < h->N; s++) { inv[h->plan.perm[s]] = s; fwd[s] = h->plan.perm[s]; }
+        h->to_int = esc::make_perm_table(inv);    // internal bit b reads reference bit inv[b]
+        h->to_ref = esc::make_perm_table(fwd);    // reference bit s reads internal bit perm[s]
         int ndev = 0;
         cudaError_t e = cudaGetDeviceCount(&ndev);
         if (e != cudaSuccess || ndev == 0) {
@@ -407,15 +468,20 @@ esc_status esc_neighbors(const esc_handle* h, int* neigh) {
     return ESC_OK;
 }
 
+esc_status esc_basis_permutation(const esc_handle* h, int* bit_of_site) {
+    if (!h || !bit_of_site) return finish(nullptr, ESC_ERR_PARAM, "null argument");
+    std::copy(h->plan.perm.begin(), h->plan.perm.end(), bit_of_site);
+    return ESC_OK;
+}
+
 esc_status esc_hv(esc_handle* h, const void* in, void* out, esc_dtype dt, int flags) {
     if (!h || !in || !out) return finish(h, ESC_ERR_PARAM, "null argument");
     if (in == out) return finish(h, ESC_ERR_PARAM, "esc_hv: in and out must differ");
     return guarded(h, [&]() {
-        const size_t bytes = (size_t)h->D * esize(dt);
-        Staged s = stage(h, in, out, bytes, bytes, flags);
-        if (dt == ESC_C64) esc::launch_hv<float>(h->dm, s.in, s.out, h->D, h->stream);
-        else esc::launch_hv<double>(h->dm, s.in, s.out, h->D, h->stream);
-        unstage(h, s, out, bytes, flags);
+        Staged s = stage(h, in, out, 1, h->D, dt, flags);
+        if (dt == ESC_C64) esc::launch_hv_tiled<float>(h->dm, h->passes, s.in, s.out, h->D, h->stream);
+        else esc::launch_hv_tiled<double>(h->dm, h->passes, s.in, s.out, h->D, h->stream);
+        unstage(h, s, out, 1, h->D, dt, flags);
     });
 }
 
@@ -432,11 +498,10 @@ esc_status esc_hv_batched(esc_handle* h, const void* in, void* out, int ncols, i
             f.fy[c] = 0.5 * (b ? b[1] : h->p.Byy);
             f.fz[c] = 0.5 * (b ? b[2] : h->p.Bzz);
         }
-        const size_t bytes = (size_t)((ncols - 1) * ld + h->D) * esize(dt);
-        Staged s = stage(h, in, out, bytes, bytes, flags);
-        if (dt == ESC_C64) esc::launch_hv_batched<float>(h->dm, f, s.in, s.out, ncols, ld, h->D, h->stream);
-        else esc::launch_hv_batched<double>(h->dm, f, s.in, s.out, ncols, ld, h->D, h->stream);
-        unstage(h, s, out, bytes, flags);
+        Staged s = stage(h, in, out, ncols, ld, dt, flags);
+        if (dt == ESC_C64) esc::launch_hv_batched<float>(h->dm, f, s.in, s.out, ncols, s.ld, h->D, h->stream);
+        else esc::launch_hv_batched<double>(h->dm, f, s.in, s.out, ncols, s.ld, h->D, h->stream);
+        unstage(h, s, out, ncols, ld, dt, flags);
     });
 }
 
@@ -444,43 +509,47 @@ esc_status esc_apply_op(esc_handle* h, int op, int site, const void* in, void* o
     if (!h || !in || !out) return finish(h, ESC_ERR_PARAM, "null argument");
     if (in == out) return finish(h, ESC_ERR_PARAM, "esc_apply_op: in and out must differ");
     return guarded(h, [&]() {
-        const esc::DevOp d = esc::make_dev_op(esc::operator_terms(op, site, h->p, h->L));
-        const size_t bytes = (size_t)h->D * esize(dt);
-        Staged s = stage(h, in, out, bytes, bytes, flags);
+        const esc::DevOp d = esc::make_dev_op(esc::operator_terms(op, site, h->p, h->L), &h->plan.perm);
+        Staged s = stage(h, in, out, 1, h->D, dt, flags);
         if (dt == ESC_C64) esc::launch_apply<float>(d, s.in, s.out, h->D, h->stream);
         else esc::launch_apply<double>(d, s.in, s.out, h->D, h->stream);
-        unstage(h, s, out, bytes, flags);
+        unstage(h, s, out, 1, h->D, dt, flags);
     });
+}
+
+// Start vector into `dst` (device, internal order, normalised).  Generated in the reference basis
+// order (the reference's draw order) and permuted; uses d_work as scratch.
+static void start_vector_internal(esc_handle* h, int kind, int seed, void* dst, esc_dtype dt) {
+    const int64_t D = h->D;
+    ensure(h->d_work, h->work_bytes, std::max(h->work_bytes, (size_t)D * 16));
+    ensure_t(h->d_sc, h->sc_bytes, std::max<size_t>(h->sc_bytes, 64));
+    void* gen = h->d_work;
+    if (kind == ESC_START_REFUNIFORM) {
+        std::vector<cplx> v((size_t)D);
+        esc::ref_uniform_start(seed, D, v.data());
+        ESC_CUDA(cudaMemcpyAsync(gen, v.data(), (size_t)D * 16, cudaMemcpyHostToDevice, h->stream));
+        if (dt == ESC_C64) {
+            esc::launch_convert_c128_to_c64(gen, dst, D, h->stream);
+            ESC_CUDA(cudaMemcpyAsync(gen, dst, (size_t)D * 8, cudaMemcpyDeviceToDevice, h->stream));
+        }
+        sync(h);
+    } else if (kind == ESC_START_NORMAL) {
+        if (dt == ESC_C128) esc::launch_start_normal<double>((uint64_t)(int64_t)seed, gen, D, h->stream);
+        else esc::launch_start_normal<float>((uint64_t)(int64_t)seed, gen, D, h->stream);
+    } else {
+        throw Fail(ESC_ERR_PARAM, "unknown start-vector kind");
+    }
+    permute(h, h->to_int, gen, dst, D, dt);
+    if (dt == ESC_C128) { esc::launch_nrm2<double>(dst, D, h->d_part, h->d_sc, h->stream); esc::launch_scale_rsqrt<double>(dst, dst, h->d_sc, D, h->stream); }
+    else { esc::launch_nrm2<float>(dst, D, h->d_part, h->d_sc, h->stream); esc::launch_scale_rsqrt<float>(dst, dst, h->d_sc, D, h->stream); }
 }
 
 esc_status esc_start_vector(esc_handle* h, int kind, int seed, void* out, esc_dtype dt, int flags) {
     if (!h || !out) return finish(h, ESC_ERR_PARAM, "null argument");
     return guarded(h, [&]() {
-        const int64_t D = h->D;
-        const size_t bytes = (size_t)D * esize(dt);
-        Staged s = stage(h, nullptr, out, 0, bytes, flags);
-        ensure_t(h->d_sc, h->sc_bytes, std::max<size_t>(h->sc_bytes, 64));
-        if (kind == ESC_START_REFUNIFORM) {
-            std::vector<cplx> v((size_t)D);
-            esc::ref_uniform_start(seed, D, v.data());
-            if (dt == ESC_C128) {
-                ESC_CUDA(cudaMemcpyAsync(s.out, v.data(), bytes, cudaMemcpyHostToDevice, h->stream));
-            } else {
-                ensure(h->d_work, h->work_bytes, (size_t)D * 16);
-                ESC_CUDA(cudaMemcpyAsync(h->d_work, v.data(), (size_t)D * 16, cudaMemcpyHostToDevice, h->stream));
-                esc::launch_convert_c128_to_c64(h->d_work, s.out, D, h->stream);
-            }
-            sync(h);
-        } else if (kind == ESC_START_NORMAL) {
-            if (dt == ESC_C128) esc::launch_start_normal<double>((uint64_t)(int64_t)seed, s.out, D, h->stream);
-            else esc::launch_start_normal<float>((uint64_t)(int64_t)seed, s.out, D, h->stream);
-        } else {
-            throw Fail(ESC_ERR_PARAM, "unknown start-vector kind");
-        }
-        // normalised
-        if (dt == ESC_C128) { esc::launch_nrm2<double>(s.out, D, h->d_part, h->d_sc, h->stream); esc::launch_scale_rsqrt<double>(s.out, s.out, h->d_sc, D, h->stream); }
-        else { esc::launch_nrm2<float>(s.out, D, h->d_part, h->d_sc, h->stream); esc::launch_scale_rsqrt<float>(s.out, s.out, h->d_sc, D, h->stream); }
-        unstage(h, s, out, bytes, flags);
+        Staged s = stage(h, nullptr, out, 1, h->D, dt, flags);
+        start_vector_internal(h, kind, seed, s.out, dt);
+        unstage(h, s, out, 1, h->D, dt, flags);
     });
 }
 
@@ -492,15 +561,13 @@ esc_status esc_lanczos_gs(esc_handle* h, const esc_lanczos_cfg* cfg, const void*
     return guarded(h, [&]() {
         const int64_t D = h->D;
         const esc_dtype dt = cfg->dtype;
-        const size_t es = esize(dt), bytes = (size_t)D * es;
-        // start vector into the staging area (device)
-        ensure(h->d_io, h->io_bytes, bytes);
-        void* d_start = h->d_io;
-        if (start) {
-            ESC_CUDA(cudaMemcpyAsync(d_start, start, bytes, (flags & ESC_DEVICE_PTR) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
-        } else {
-            const esc_status st = esc_start_vector(h, h->p.start_vector, h->p.seed, d_start, dt, ESC_DEVICE_PTR);
-            if (st != ESC_OK) throw Fail(st, h->err);
+        // start vector -> internal order in d_io[0]
+        Staged s = stage(h, start, nullptr, 1, D, dt, flags);
+        void* d_start = (void*)s.in;
+        if (!start) {
+            ensure(h->d_io, h->io_bytes, std::max(h->io_bytes, 2 * (size_t)D * esize(dt)));
+            d_start = h->d_io;
+            start_vector_internal(h, h->p.start_vector, h->p.seed, d_start, dt);
         }
         if (dt == ESC_C64) lanczos_gs<float>(h, *cfg, d_start);
         else lanczos_gs<double>(h, *cfg, d_start);
@@ -510,7 +577,10 @@ esc_status esc_lanczos_gs(esc_handle* h, const esc_lanczos_cfg* cfg, const void*
         if (alpha) std::copy(h->alpha.begin(), h->alpha.end(), alpha);
         if (beta) std::copy(h->beta.begin(), h->beta.end(), beta);
         if (ritz) std::copy(h->ritz.begin(), h->ritz.end(), ritz);
-        if (gs_out) ESC_CUDA(cudaMemcpyAsync(gs_out, h->d_gs, bytes, (flags & ESC_DEVICE_PTR) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+        if (gs_out) {
+            Staged g{nullptr, h->d_gs, D};
+            unstage(h, g, gs_out, 1, D, dt, flags & ~ESC_ASYNC);
+        }
         sync(h);
     });
 }
@@ -795,3 +865,23 @@ esc_status esc_grad(esc_handle* h, const esc_dyn_cfg* cfg, double* dE0, double* 
 }
 
 }  // extern "C"
+
+extern "C" esc_status esc_plan(const esc_params* p, int tile_bits, int low_bits, int* bit_of_site, int* npasses) {
+    if (!p) return finish(nullptr, ESC_ERR_PARAM, "null argument");
+    return guarded(nullptr, [&]() {
+        esc::Lattice L;
+        std::vector<esc::Bond> bonds;
+        esc::build_lattice(*p, L);
+        esc::build_bonds(*p, L, bonds);
+        std::vector<std::pair<int, int>> pairs;
+        for (const auto& b : bonds)
+            if (b.kx - b.ky != 0.0 || b.kx + b.ky != 0.0) pairs.push_back({b.i, b.j});
+        esc::Plan P = esc::make_plan(L.N, pairs, tile_bits > 0 ? tile_bits : 13, low_bits > 0 ? low_bits : 3, 200);
+        std::vector<esc::Bond> rb(bonds);
+        for (auto& b : rb) { b.i = P.perm[b.i]; b.j = P.perm[b.j]; }
+        const esc::DevModel m = esc::make_dev_model(*p, L, rb, p->Bxx, p->Byy, p->Bzz);
+        const auto passes = esc::make_passes(P, m);   // throws if a term fits no tile
+        if (bit_of_site) std::copy(P.perm.begin(), P.perm.end(), bit_of_site);
+        if (npasses) *npasses = (int)passes.size();
+    });
+}

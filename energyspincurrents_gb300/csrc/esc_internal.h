@@ -85,6 +85,36 @@ void build_bonds(const esc_params& p, const Lattice& L, std::vector<Bond>& bonds
 DevModel make_dev_model(const esc_params& p, const Lattice& L, const std::vector<Bond>& bonds,
                         double Bx, double By, double Bz);
 
+// ---------------------------------------------------------------------------------------------
+// Tiled H.v (hv_tiled.cu, planner.cpp)
+// ---------------------------------------------------------------------------------------------
+struct Plan {
+    int N = 0, T = 0, c = 0;
+    std::vector<int> perm;                 // site -> bit position of the internal basis index
+    std::vector<std::vector<int>> tiles;   // per pass: sorted tile bit positions (include [0,c))
+};
+Plan make_plan(int N, const std::vector<std::pair<int, int>>& bonds, int T, int c, int restarts);
+
+constexpr int MAX_PTERMS = 96;
+struct DevPass {
+    int Tp, c, nrest, nbond, nfield, diag, accumulate, pad;
+    unsigned long long tabLo[64], tabHi[64];   // run index -> global offset (low / high 6 bits)
+    unsigned char rest[MAX_SITES];             // bit positions of the tile number, ascending
+    unsigned int blm[MAX_PTERMS];              // bond masks in tile-local bits
+    double ceq[MAX_PTERMS], cdiff[MAX_PTERMS];
+    unsigned int flm[MAX_SITES];               // field-term masks in tile-local bits
+};
+// Builds one DevPass per plan pass from the relabelled model; throws if a term fits no tile.
+std::vector<DevPass> make_passes(const Plan& P, const DevModel& m);
+template <typename R> void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in,
+                                           void* out, int64_t D, cudaStream_t s);
+// Basis permutation: out[j] = in[src(j)], src assembled bitwise from five 8-bit tables.
+struct DevPerm {
+    unsigned long long tab[5][256];
+};
+DevPerm make_perm_table(const std::vector<int>& bit_of_src_bit);   // tab maps dst index bits -> src index
+template <typename R> void launch_permute(const DevPerm& p, const void* in, void* out, int64_t D, cudaStream_t s);
+
 struct OpTerm {
     cplx coef;
     int nf;
@@ -93,7 +123,8 @@ struct OpTerm {
 };
 // Throws std::invalid_argument for unknown operators / missing neighbours.
 std::vector<OpTerm> operator_terms(int op, int site, const esc_params& p, const Lattice& L);
-DevOp make_dev_op(const std::vector<OpTerm>& terms);
+// perm (optional): site -> internal bit position
+DevOp make_dev_op(const std::vector<OpTerm>& terms, const std::vector<int>* perm = nullptr);
 
 // ---------------------------------------------------------------------------------------------
 // Kernel launchers (kernels.cu).  R = double (complex128 vectors) or float (complex64 vectors).

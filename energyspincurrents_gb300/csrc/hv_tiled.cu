@@ -1,0 +1,214 @@
+// hv_tiled.cu -- shared-memory tiled H.v for sm_103a.
+//
+// One launch per pass of the plan (planner.cpp).  A CTA owns one tile at a time: the 2^Tp basis
+// states that differ only in the pass's tile bits.  It loads the tile (runs of 2^c consecutive
+// states) into shared memory, applies every term assigned to the pass by gathering partners from
+// shared memory, and writes (pass 1) or accumulates (later passes) the result.  Coefficients come
+// from the tile-local bits; the diagonal (pass 1) from the global index.  Each output element is
+// written by one thread: no atomics, deterministic.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "esc_internal.h"
+
+namespace esc {
+
+template <typename R> struct V2T;
+template <> struct V2T<double> { typedef double2 T; };
+template <> struct V2T<float> { typedef float2 T; };
+
+static constexpr int TILE_THREADS = 512;
+
+template <typename R>
+__global__ void __launch_bounds__(TILE_THREADS) k_hv_pass(const __grid_constant__ DevModel m,
+                                                           const __grid_constant__ DevPass p,
+                                                           const typename V2T<R>::T* __restrict__ in,
+                                                           typename V2T<R>::T* __restrict__ out,
+                                                           long long ntiles) {
+    typedef typename V2T<R>::T C;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* tile = reinterpret_cast<C*>(smem_raw);
+    const int Tn = 1 << p.Tp;
+    const int cm = (1 << p.c) - 1;
+    const R fx = (R)m.fx, fy = (R)m.fy;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        unsigned long long base = 0;
+        for (int q = 0; q < p.nrest; q++) base |= (((unsigned long long)t >> q) & 1ull) << p.rest[q];
+        for (int e = threadIdx.x; e < Tn; e += blockDim.x) {
+            const int r = e >> p.c;
+            const unsigned long long k = base | p.tabLo[r & 63] | p.tabHi[r >> 6] | (unsigned long long)(e & cm);
+            tile[e] = in[k];
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < Tn; e += blockDim.x) {
+            const int r = e >> p.c;
+            const unsigned long long k = base | p.tabLo[r & 63] | p.tabHi[r >> 6] | (unsigned long long)(e & cm);
+            R ar = 0, ai = 0;
+            if (p.diag) {
+                double dg = 0.0;
+                for (int b = 0; b < m.nd; b++) {
+                    const double q = 0.25 * m.d[b].dz;
+                    dg += (__popcll(k & m.d[b].mask) == 1) ? -q : q;
+                }
+                dg = __dadd_rn(dg, __dmul_rn(m.fz, (double)(m.N - 2 * __popcll(k))));
+                const C v = tile[e];
+                ar = (R)dg * v.x;
+                ai = (R)dg * v.y;
+            }
+#pragma unroll 4
+            for (int b = 0; b < p.nbond; b++) {
+                const unsigned int lm = p.blm[b];
+                const R c = (R)((__popc((unsigned)e & lm) == 1) ? p.cdiff[b] : p.ceq[b]);
+                const C w = tile[e ^ lm];
+                ar = fma(c, w.x, ar);
+                ai = fma(c, w.y, ai);
+            }
+            R Fr = 0, Fi = 0, Gr = 0, Gi = 0;
+#pragma unroll 4
+            for (int f = 0; f < p.nfield; f++) {
+                const unsigned int lm = p.flm[f];
+                const C w = tile[e ^ lm];
+                const R sg = ((unsigned)e & lm) ? (R)1 : (R)-1;
+                Fr += w.x; Fi += w.y;
+                Gr = fma(sg, w.x, Gr); Gi = fma(sg, w.y, Gi);
+            }
+            if (p.nfield) {
+                ar = fma(fx, Fr, ar); ar = fma(-fy, Gi, ar);
+                ai = fma(fx, Fi, ai); ai = fma(fy, Gr, ai);
+            }
+            if (p.accumulate) {
+                const C o = out[k];
+                ar += o.x;
+                ai += o.y;
+            }
+            C o;
+            o.x = ar; o.y = ai;
+            out[k] = o;
+        }
+        __syncthreads();
+    }
+}
+
+std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
+    const int np = (int)P.tiles.size();
+    std::vector<DevPass> out(np);
+    std::vector<char> bdone(m.nb, 0), fdone(P.N, 0);
+    for (int pi = 0; pi < np; pi++) {
+        DevPass& d = out[pi];
+        std::memset(&d, 0, sizeof(d));
+        const std::vector<int>& B = P.tiles[pi];
+        d.Tp = (int)B.size();
+        d.c = std::min(P.c, d.Tp);
+        if (d.Tp - d.c > 12) throw std::invalid_argument("tile too large for the run-offset tables");
+        unsigned long long tmask = 0;
+        int local_of[64];
+        for (int q = 0; q < 64; q++) local_of[q] = -1;
+        for (int q = 0; q < d.Tp; q++) { tmask |= 1ull << B[q]; local_of[B[q]] = q; }
+        for (int q = 0; q < d.c; q++)
+            if (B[q] != q) throw std::invalid_argument("tile must contain the lowest c bits");
+        for (int r = 0; r < 64; r++) {
+            unsigned long long lo = 0, hi = 0;
+            for (int q = 0; q < 6; q++) {
+                if (d.c + q < d.Tp && ((r >> q) & 1)) lo |= 1ull << B[d.c + q];
+                if (d.c + 6 + q < d.Tp && ((r >> q) & 1)) hi |= 1ull << B[d.c + 6 + q];
+            }
+            d.tabLo[r] = lo; d.tabHi[r] = hi;
+        }
+        d.nrest = 0;
+        for (int q = 0; q < P.N; q++) if (!((tmask >> q) & 1ull)) d.rest[d.nrest++] = (unsigned char)q;
+        auto local = [&](unsigned long long gm) {
+            unsigned int lm = 0;
+            for (int q = 0; q < P.N; q++) if ((gm >> q) & 1ull) lm |= 1u << local_of[q];
+            return lm;
+        };
+        d.diag = (pi == 0);
+        d.accumulate = (pi > 0);
+        for (int b = 0; b < m.nb; b++) {
+            if (bdone[b] || (m.b[b].mask & ~tmask)) continue;
+            if (d.nbond >= MAX_PTERMS) throw std::invalid_argument("too many bonds in one pass");
+            d.blm[d.nbond] = local(m.b[b].mask);
+            d.ceq[d.nbond] = m.b[b].ceq;
+            d.cdiff[d.nbond] = m.b[b].cdiff;
+            d.nbond++;
+            bdone[b] = 1;
+        }
+        if (m.fx != 0.0 || m.fy != 0.0)
+            for (int s = 0; s < P.N; s++) {
+                if (fdone[s] || !((tmask >> s) & 1ull)) continue;
+                d.flm[d.nfield++] = local(1ull << s);
+                fdone[s] = 1;
+            }
+    }
+    for (int b = 0; b < m.nb; b++)
+        if (!bdone[b]) throw std::invalid_argument("plan leaves a bond outside every tile");
+    return out;
+}
+
+template <typename R>
+void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in, void* out, int64_t D,
+                     cudaStream_t s) {
+    typedef typename V2T<R>::T C;
+    for (const DevPass& p : passes) {
+        const size_t smem = (size_t(1) << p.Tp) * sizeof(C);
+        if (smem > 48 * 1024)
+            ESC_CUDA(cudaFuncSetAttribute(k_hv_pass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0;
+        ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass<R>, TILE_THREADS, smem));
+        int dev = 0, sms = 0;
+        ESC_CUDA(cudaGetDevice(&dev));
+        ESC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const long long ntiles = (long long)(D >> p.Tp);
+        const long long g = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
+        k_hv_pass<R><<<(unsigned)g, TILE_THREADS, smem, s>>>(m, p, (const C*)in, (C*)out, ntiles);
+        ESC_CUDA(cudaGetLastError());
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Basis permutation (reference order <-> internal order)
+// ---------------------------------------------------------------------------------------------
+DevPerm make_perm_table(const std::vector<int>& src_bit_of_dst_bit) {
+    DevPerm t;
+    std::memset(&t, 0, sizeof(t));
+    const int N = (int)src_bit_of_dst_bit.size();
+    for (int chunk = 0; chunk < 5; chunk++)
+        for (int v = 0; v < 256; v++) {
+            unsigned long long s = 0;
+            for (int q = 0; q < 8; q++) {
+                const int b = chunk * 8 + q;
+                if (b < N && ((v >> q) & 1)) s |= 1ull << src_bit_of_dst_bit[b];
+            }
+            t.tab[chunk][v] = s;
+        }
+    return t;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_permute(const __grid_constant__ DevPerm p, const typename V2T<R>::T* __restrict__ in,
+                                                 typename V2T<R>::T* __restrict__ out, long long D) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < D; j += stride) {
+        const unsigned long long u = (unsigned long long)j;
+        const unsigned long long src = p.tab[0][u & 255] | p.tab[1][(u >> 8) & 255] | p.tab[2][(u >> 16) & 255] |
+                                       p.tab[3][(u >> 24) & 255] | p.tab[4][(u >> 32) & 255];
+        out[j] = in[src];
+    }
+}
+
+template <typename R>
+void launch_permute(const DevPerm& p, const void* in, void* out, int64_t D, cudaStream_t s) {
+    typedef typename V2T<R>::T C;
+    long long g = (D + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    k_permute<R><<<(unsigned)g, 256, 0, s>>>(p, (const C*)in, (C*)out, (long long)D);
+    ESC_CUDA(cudaGetLastError());
+}
+
+template void launch_hv_tiled<double>(const DevModel&, const std::vector<DevPass>&, const void*, void*, int64_t, cudaStream_t);
+template void launch_hv_tiled<float>(const DevModel&, const std::vector<DevPass>&, const void*, void*, int64_t, cudaStream_t);
+template void launch_permute<double>(const DevPerm&, const void*, void*, int64_t, cudaStream_t);
+template void launch_permute<float>(const DevPerm&, const void*, void*, int64_t, cudaStream_t);
+
+}  // namespace esc

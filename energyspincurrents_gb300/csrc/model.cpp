@@ -246,7 +246,7 @@ std::vector<OpTerm> operator_terms(int op, int site, const esc_params& p, const 
     return b.t;
 }
 
-DevOp make_dev_op(const std::vector<OpTerm>& terms) {
+DevOp make_dev_op(const std::vector<OpTerm>& terms, const std::vector<int>* perm) {
     DevOp d;
     std::memset(&d, 0, sizeof(d));
     if ((int)terms.size() > MAX_TERMS) throw std::invalid_argument("operator has too many terms");
@@ -257,8 +257,9 @@ DevOp make_dev_op(const std::vector<OpTerm>& terms) {
         unsigned int fac = (unsigned)o.nf;
         for (int f = 0; f < o.nf; f++) {
             const int code = o.op[f] == 'x' ? 1 : o.op[f] == 'y' ? 2 : 3;
-            if (code != 3) flip ^= 1ull << o.site[f];
-            fac |= (unsigned)(o.site[f] & 63) << (2 + 8 * f);
+            const int bit = perm ? (*perm)[o.site[f]] : o.site[f];
+            if (code != 3) flip ^= 1ull << bit;
+            fac |= (unsigned)(bit & 63) << (2 + 8 * f);
             fac |= (unsigned)code << (8 + 8 * f);
         }
         d.flip[t] = flip;

@@ -42,7 +42,11 @@ typedef enum {
 
 typedef enum { ESC_C128 = 0, ESC_C64 = 1 } esc_dtype;
 
-enum { ESC_DEVICE_PTR = 1, ESC_ASYNC = 2 };
+/* ESC_INTERNAL_ORDER: the vectors are in the handle's internal basis order (sites relabelled so
+ * that the tiled H.v keeps bonds inside shared-memory tiles; see esc_basis_permutation).
+ * Inner products and spectra do not depend on the order, so callers that keep vectors resident
+ * can skip the permutation at the boundary. */
+enum { ESC_DEVICE_PTR = 1, ESC_ASYNC = 2, ESC_INTERNAL_ORDER = 4 };
 
 /* Operator identifiers for esc_apply_op (reference: Observables::ApplyOp, src/Observables.h:24-67,
  * plus the totals of :448-470, :664-699). */
@@ -132,6 +136,11 @@ esc_status esc_params_from_file(const char* path, esc_params* p, char* errbuf, s
  * (src/Lattice.h:434-576, :60-136). */
 esc_status esc_lattice(const esc_params* p, int* neigh, int* nsites);
 
+/* Site relabelling and pass count of the tiled H.v for the model in `p` with tiles of 2^tile_bits
+ * states (0 = default 13) whose lowest low_bits bits are shared (0 = default 3); host only.
+ * bit_of_site (N entries, may be NULL), npasses (may be NULL).  No reference counterpart. */
+esc_status esc_plan(const esc_params* p, int tile_bits, int low_bits, int* bit_of_site, int* npasses);
+
 /* ---- handle --------------------------------------------------------------------------------- */
 
 /* Build lattice, bond tables and device state.  Replaces the construction sequence
@@ -146,6 +155,8 @@ int64_t esc_dim(const esc_handle* h);
 /* Neighbour table N x 3 (columns 0=z, 1=y, 2=x; -1 = none), Lattice::N1neigh_
  * (src/Lattice.h:29, :497-564). */
 esc_status esc_neighbors(const esc_handle* h, int* neigh);
+/* bit_of_site[s] = position of site s's bit in the internal basis index (N entries). */
+esc_status esc_basis_permutation(const esc_handle* h, int* bit_of_site);
 /* The handle's CUDA stream (cudaStream_t), for callers that order their own work with it. */
 void* esc_stream(esc_handle* h);
 

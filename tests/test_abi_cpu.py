@@ -140,3 +140,18 @@ def test_device_entry_points_fail_loudly_without_gpu():
         pass
     with pytest.raises(esc.EscError, match="no CUDA device"):
         esc.Handle(dict(Lx=2, Ly=4))
+
+
+@pytest.mark.parametrize("shape,J", [((3, 4), 0.0), ((4, 4), 0.1), ((3, 6), 0.1), ((3, 8), 0.1), ((7, 4), 0.05),
+                                     ((4, 8), 0.05), ((5, 6), 0.05)])
+@pytest.mark.parametrize("tile", [(13, 3), (10, 3), (14, 4)])
+def test_planner_covers_every_term(shape, J, tile):
+    """esc_plan builds the pass list (make_passes throws if any bond fits no tile) and a bijective
+    site -> bit relabelling; pass counts stay small."""
+    Lx, Ly = shape
+    b = -0.02 / 3 ** 0.5
+    perm, npass = esc.plan(dict(Lx=Lx, Ly=Ly, Kxx=-1.0, Kyy=-1.0, Kzz=-1.0, Bxx=b, Byy=b, Bzz=b, jheis=J), *tile)
+    assert sorted(perm.tolist()) == list(range(Lx * Ly))
+    N = Lx * Ly
+    T = tile[0]
+    assert npass == 1 if N <= T else 2 <= npass <= 2 + 2 * (N - T)

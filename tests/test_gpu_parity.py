@@ -225,3 +225,24 @@ def test_errors_are_reported():
     with pytest.raises(esc.EscError, match="neighbour"):
         ho = esc.Handle(dict(kitaev(Lx=4, Ly=4), pbcx=0))
         ho.apply("JexTotal", 0, np.zeros(ho.D, np.complex128))
+
+
+@pytest.mark.parametrize("tile_bits", [6, 9, 13])
+@pytest.mark.parametrize("shape", [(3, 4), (4, 4), (3, 6)])
+def test_tiled_multipass_vs_oracle(tile_bits, shape, monkeypatch):
+    """Small tiles force many passes (and the site relabelling) on small clusters."""
+    monkeypatch.setenv("ESC_TILE_BITS", str(tile_bits))
+    monkeypatch.setenv("ESC_TILE_LOW", "3")
+    Lx, Ly = shape
+    p = kitaev(Lx=Lx, Ly=Ly, J=0.1)
+    h = esc.Handle(p)
+    m = O.Model("Kitaev", Lx, Ly, 1, 1, -1.0, -1.0, -1.0, p["Bxx"], p["Byy"], p["Bzz"], 0.1, 4, False)
+    x = O.random_start(11, h.D, normalize=False)
+    ref = m.hv(x)
+    assert relerr(h.hv(x), ref) < 1e-14
+    assert relerr(h.hv(x.astype(np.complex64)).astype(np.complex128), ref) < 2e-6
+    # internal-order round trip: H in the relabelled basis = relabelled H
+    xi = h.to_internal(x)
+    assert relerr(h.hv(xi, flags=esc.INTERNAL_ORDER), h.to_internal(ref)) < 1e-14
+    # operators go through the same relabelling
+    assert relerr(h.apply("JexTotal", 0, x), m.apply("JexTotal", 0, x)) < 1e-14
