@@ -497,6 +497,7 @@ esc_status esc_hv_batched(esc_handle* h, const void* in, void* out, int ncols, i
             f.fx[c] = 0.5 * (b ? b[0] : h->p.Bxx);
             f.fy[c] = 0.5 * (b ? b[1] : h->p.Byy);
             f.fz[c] = 0.5 * (b ? b[2] : h->p.Bzz);
+            f.fxf[c] = (float)f.fx[c]; f.fyf[c] = (float)f.fy[c]; f.fzf[c] = (float)f.fz[c];
         }
         Staged s = stage(h, in, out, ncols, ld, dt, flags);
         if (dt == ESC_C64) esc::launch_hv_batched<float>(h->dm, f, s.in, s.out, ncols, s.ld, h->D, h->stream);

@@ -47,10 +47,17 @@ struct DevModel {
     double fx, fy, fz;   // Bx/2, By/2, Bz/2
     DevBond b[MAX_BONDS];
     DevDiagBond d[MAX_BONDS];
+    // float copies for the complex64 path (GB300 runs FP64 and FP64<->FP32 conversions at a small
+    // fraction of the FP32 rate, so the float kernels must not touch a double per term)
+    float fxf, fyf, fzf, padf;
+    float ceqf[MAX_BONDS], cdifff[MAX_BONDS];
+    float dqf[MAX_BONDS];   // dz/4
 };
+void fill_float_copies(DevModel& m);
 // Per-column field (batched H.V with one field per column).
 struct DevFields {
     double fx[MAX_COLS], fy[MAX_COLS], fz[MAX_COLS];
+    float fxf[MAX_COLS], fyf[MAX_COLS], fzf[MAX_COLS];
 };
 
 // Operator = sum of terms; term t = coef * f_{n-1} ... f_0 (f_0 applied first), each factor a
@@ -61,6 +68,7 @@ struct DevOp {
     unsigned long long flip[MAX_TERMS];
     unsigned int fac[MAX_TERMS];   // bits 0-1 nf; factor f at bits 2+8f: 6 bits site, 2 bits op (1 x, 2 y, 3 z)
     double cre[MAX_TERMS], cim[MAX_TERMS];
+    float cref[MAX_TERMS], cimf[MAX_TERMS];
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -102,6 +110,7 @@ struct DevPass {
     unsigned char rest[MAX_SITES];             // bit positions of the tile number, ascending
     unsigned int blm[MAX_PTERMS];              // bond masks in tile-local bits
     double ceq[MAX_PTERMS], cdiff[MAX_PTERMS];
+    float ceqf[MAX_PTERMS], cdifff[MAX_PTERMS];   // the same in float for the complex64 path
     unsigned int flm[MAX_SITES];               // field-term masks in tile-local bits
 };
 // Builds one DevPass per plan pass from the relabelled model; throws if a term fits no tile.

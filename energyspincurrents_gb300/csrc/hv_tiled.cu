@@ -32,7 +32,8 @@ __global__ void __launch_bounds__(TILE_THREADS) k_hv_pass(const __grid_constant_
     C* tile = reinterpret_cast<C*>(smem_raw);
     const int Tn = 1 << p.Tp;
     const int cm = (1 << p.c) - 1;
-    const R fx = (R)m.fx, fy = (R)m.fy;
+    constexpr bool F32 = sizeof(R) == 4;
+    const R fx = F32 ? (R)m.fxf : (R)m.fx, fy = F32 ? (R)m.fyf : (R)m.fy;
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
         unsigned long long base = 0;
         for (int q = 0; q < p.nrest; q++) base |= (((unsigned long long)t >> q) & 1ull) << p.rest[q];
@@ -47,20 +48,31 @@ __global__ void __launch_bounds__(TILE_THREADS) k_hv_pass(const __grid_constant_
             const unsigned long long k = base | p.tabLo[r & 63] | p.tabHi[r >> 6] | (unsigned long long)(e & cm);
             R ar = 0, ai = 0;
             if (p.diag) {
-                double dg = 0.0;
-                for (int b = 0; b < m.nd; b++) {
-                    const double q = 0.25 * m.d[b].dz;
-                    dg += (__popcll(k & m.d[b].mask) == 1) ? -q : q;
+                R dg;
+                if constexpr (F32) {
+                    float d = 0.0f;
+                    for (int b = 0; b < m.nd; b++) d += (__popcll(k & m.d[b].mask) == 1) ? -m.dqf[b] : m.dqf[b];
+                    dg = fmaf(m.fzf, (float)(m.N - 2 * __popcll(k)), d);
+                } else {
+                    // same operations and order as HDiag (src/Hamiltonian.h:344-375): bit-identical
+                    double d = 0.0;
+                    for (int b = 0; b < m.nd; b++) {
+                        const double q = 0.25 * m.d[b].dz;
+                        d += (__popcll(k & m.d[b].mask) == 1) ? -q : q;
+                    }
+                    dg = __dadd_rn(d, __dmul_rn(m.fz, (double)(m.N - 2 * __popcll(k))));
                 }
-                dg = __dadd_rn(dg, __dmul_rn(m.fz, (double)(m.N - 2 * __popcll(k))));
                 const C v = tile[e];
-                ar = (R)dg * v.x;
-                ai = (R)dg * v.y;
+                ar = dg * v.x;
+                ai = dg * v.y;
             }
 #pragma unroll 4
             for (int b = 0; b < p.nbond; b++) {
                 const unsigned int lm = p.blm[b];
-                const R c = (R)((__popc((unsigned)e & lm) == 1) ? p.cdiff[b] : p.ceq[b]);
+                const bool df = __popc((unsigned)e & lm) == 1;
+                R c;
+                if constexpr (F32) c = df ? p.cdifff[b] : p.ceqf[b];
+                else c = df ? p.cdiff[b] : p.ceq[b];
                 const C w = tile[e ^ lm];
                 ar = fma(c, w.x, ar);
                 ai = fma(c, w.y, ai);
@@ -131,6 +143,8 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
             d.blm[d.nbond] = local(m.b[b].mask);
             d.ceq[d.nbond] = m.b[b].ceq;
             d.cdiff[d.nbond] = m.b[b].cdiff;
+            d.ceqf[d.nbond] = (float)m.b[b].ceq;
+            d.cdifff[d.nbond] = (float)m.b[b].cdiff;
             d.nbond++;
             bdone[b] = 1;
         }

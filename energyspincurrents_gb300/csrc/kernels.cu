@@ -14,6 +14,23 @@ template <typename R> struct V2;
 template <> struct V2<double> { typedef double2 T; };
 template <> struct V2<float> { typedef float2 T; };
 
+// Float-float accumulation (Dekker/Knuth error-free transforms): the complex64 path keeps its
+// reductions at ~2^-44 relative accuracy without FP64 arithmetic, which GB300 executes at a small
+// fraction of the FP32 rate.
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    const float err = (hi - (s - bp)) + (x - bp);
+    hi = s;
+    lo += err;
+}
+__device__ __forceinline__ void ff_addprod(float& hi, float& lo, float a, float b) {
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    ff_add(hi, lo, p);
+    lo += e;
+}
+
 static inline int grid_for(int64_t n, int tpb, int max_blocks) {
     int64_t g = (n + tpb - 1) / tpb;
     if (g > max_blocks) g = max_blocks;
@@ -35,21 +52,32 @@ __global__ void __launch_bounds__(256) k_hv(const __grid_constant__ DevModel m,
                                             const typename V2<R>::T* __restrict__ in,
                                             typename V2<R>::T* __restrict__ out, long long D) {
     typedef typename V2<R>::T C;
+    constexpr bool F32 = sizeof(R) == 4;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < D; k += stride) {
         const unsigned long long uk = (unsigned long long)k;
-        double dg = 0.0;
-        for (int b = 0; b < m.nd; b++) {
-            const double q = 0.25 * m.d[b].dz;
-            dg += (__popcll(uk & m.d[b].mask) == 1) ? -q : q;
+        R dg;
+        if constexpr (F32) {
+            float d = 0.0f;
+            for (int b = 0; b < m.nd; b++) d += (__popcll(uk & m.d[b].mask) == 1) ? -m.dqf[b] : m.dqf[b];
+            dg = fmaf(m.fzf, (float)(m.N - 2 * __popcll(uk)), d);
+        } else {
+            double d = 0.0;
+            for (int b = 0; b < m.nd; b++) {
+                const double q = 0.25 * m.d[b].dz;
+                d += (__popcll(uk & m.d[b].mask) == 1) ? -q : q;
+            }
+            // product rounded before the sum (no FMA contraction), as HDiag += Bzz*SzT does
+            dg = __dadd_rn(d, __dmul_rn(m.fz, (double)(m.N - 2 * __popcll(uk))));
         }
-        // product rounded before the sum (no FMA contraction), as HDiag += Bzz*SzT does
-        dg = __dadd_rn(dg, __dmul_rn(m.fz, (double)(m.N - 2 * __popcll(uk))));
         const C v = in[k];
-        R ar = (R)dg * v.x, ai = (R)dg * v.y;
+        R ar = dg * v.x, ai = dg * v.y;
         for (int b = 0; b < m.nb; b++) {
             const unsigned long long mk = m.b[b].mask;
-            const R c = (R)((__popcll(uk & mk) == 1) ? m.b[b].cdiff : m.b[b].ceq);
+            const bool df = __popcll(uk & mk) == 1;
+            R c;
+            if constexpr (F32) c = df ? m.cdifff[b] : m.ceqf[b];
+            else c = df ? m.b[b].cdiff : m.b[b].ceq;
             const C w = in[uk ^ mk];
             ar = fma(c, w.x, ar);
             ai = fma(c, w.y, ai);
@@ -61,7 +89,7 @@ __global__ void __launch_bounds__(256) k_hv(const __grid_constant__ DevModel m,
             Fr += w.x; Fi += w.y;
             if ((uk >> s) & 1ull) { Gr += w.x; Gi += w.y; } else { Gr -= w.x; Gi -= w.y; }
         }
-        const R fx = (R)m.fx, fy = (R)m.fy;
+        const R fx = F32 ? (R)m.fxf : (R)m.fx, fy = F32 ? (R)m.fyf : (R)m.fy;
         ar = fma(fx, Fr, ar); ar = fma(-fy, Gi, ar);
         ai = fma(fx, Fi, ai); ai = fma(fy, Gr, ai);
         C o; o.x = ar; o.y = ai;
@@ -80,25 +108,31 @@ __global__ void __launch_bounds__(256) k_hv_batched(const __grid_constant__ DevM
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < D; k += stride) {
         const unsigned long long uk = (unsigned long long)k;
-        double dgb = 0.0;
+        constexpr bool F32 = sizeof(R) == 4;
+        R dgb = 0;
         for (int b = 0; b < m.nd; b++) {
-            const double q = 0.25 * m.d[b].dz;
+            const R q = F32 ? (R)m.dqf[b] : (R)(0.25 * m.d[b].dz);
             dgb += (__popcll(uk & m.d[b].mask) == 1) ? -q : q;
         }
-        const double nz = (double)(m.N - 2 * __popcll(uk));
+        const R nz = (R)(m.N - 2 * __popcll(uk));
         R ar[NC], ai[NC], Fr[NC], Fi[NC], Gr[NC], Gi[NC];
 #pragma unroll
         for (int c = 0; c < NC; c++) {
             ar[c] = ai[c] = Fr[c] = Fi[c] = Gr[c] = Gi[c] = (R)0;
             if (c < ncols) {
-                const R dg = (R)__dadd_rn(dgb, __dmul_rn(f.fz[c], nz));
+                R dg;
+                if constexpr (F32) dg = fmaf(f.fzf[c], nz, dgb);
+                else dg = __dadd_rn(dgb, __dmul_rn(f.fz[c], nz));
                 const C v = in[c * ld + k];
                 ar[c] = dg * v.x; ai[c] = dg * v.y;
             }
         }
         for (int b = 0; b < m.nb; b++) {
             const unsigned long long mk = m.b[b].mask;
-            const R cc = (R)((__popcll(uk & mk) == 1) ? m.b[b].cdiff : m.b[b].ceq);
+            const bool df = __popcll(uk & mk) == 1;
+            R cc;
+            if constexpr (F32) cc = df ? m.cdifff[b] : m.ceqf[b];
+            else cc = df ? m.b[b].cdiff : m.b[b].ceq;
             const unsigned long long kp = uk ^ mk;
 #pragma unroll
             for (int c = 0; c < NC; c++)
@@ -122,7 +156,7 @@ __global__ void __launch_bounds__(256) k_hv_batched(const __grid_constant__ DevM
 #pragma unroll
         for (int c = 0; c < NC; c++)
             if (c < ncols) {
-                const R fx = (R)f.fx[c], fy = (R)f.fy[c];
+                const R fx = F32 ? (R)f.fxf[c] : (R)f.fx[c], fy = F32 ? (R)f.fyf[c] : (R)f.fy[c];
                 C o;
                 o.x = fma(-fy, Gi[c], fma(fx, Fr[c], ar[c]));
                 o.y = fma(fy, Gr[c], fma(fx, Fi[c], ai[c]));
@@ -168,18 +202,18 @@ __global__ void __launch_bounds__(256) k_apply(const __grid_constant__ DevOp op,
             const unsigned long long k0 = (unsigned long long)k ^ op.flip[t];
             const unsigned int fac = op.fac[t];
             const int nf = fac & 3;
-            double cr = op.cre[t], ci = op.cim[t];
+            R cr = sizeof(R) == 4 ? (R)op.cref[t] : (R)op.cre[t], ci = sizeof(R) == 4 ? (R)op.cimf[t] : (R)op.cim[t];
             unsigned long long ket = k0;
             for (int q = 0; q < nf; q++) {
                 const int s = (fac >> (2 + 8 * q)) & 63;
                 const int o = (fac >> (8 + 8 * q)) & 3;
-                const double h = ((ket >> s) & 1ull) ? -0.5 : 0.5;
-                if (o == 1) { cr *= 0.5; ci *= 0.5; ket ^= 1ull << s; }               // S^x: 1/2, flip
-                else if (o == 2) { const double nr = -ci * h, ni = cr * h; cr = nr; ci = ni; ket ^= 1ull << s; }  // S^y: +-i/2
+                const R h = ((ket >> s) & 1ull) ? (R)-0.5 : (R)0.5;
+                if (o == 1) { cr *= (R)0.5; ci *= (R)0.5; ket ^= 1ull << s; }         // S^x: 1/2, flip
+                else if (o == 2) { const R nr = -ci * h, ni = cr * h; cr = nr; ci = ni; ket ^= 1ull << s; }  // S^y: +-i/2
                 else { cr *= h; ci *= h; }                                            // S^z: +-1/2
             }
             const C w = in[k0];
-            const R r = (R)cr, i = (R)ci;
+            const R r = cr, i = ci;
             ar = fma(r, w.x, ar); ar = fma(-i, w.y, ar);
             ai = fma(r, w.y, ai); ai = fma(i, w.x, ai);
         }
@@ -225,10 +259,21 @@ __global__ void __launch_bounds__(256) k_dot_partial(const typename V2<R>::T* __
                                                      double* __restrict__ partials) {
     double v[2] = {0.0, 0.0};
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const double xr = a[i].x, xi = a[i].y, yr = b[i].x, yi = b[i].y;
-        v[0] += xr * yr + xi * yi;
-        v[1] += xr * yi - xi * yr;
+    if constexpr (sizeof(R) == 4) {
+        float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            const float2 x = a[i], y = b[i];
+            ff_addprod(rh, rl, x.x, y.x); ff_addprod(rh, rl, x.y, y.y);
+            ff_addprod(ih, il, x.x, y.y); ff_addprod(ih, il, -x.y, y.x);
+        }
+        v[0] = (double)rh + (double)rl;
+        v[1] = (double)ih + (double)il;
+    } else {
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            const double xr = a[i].x, xi = a[i].y, yr = b[i].x, yi = b[i].y;
+            v[0] += xr * yr + xi * yi;
+            v[1] += xr * yi - xi * yr;
+        }
     }
     block_reduce_store<2>(v, partials + 2 * blockIdx.x);
 }
@@ -238,9 +283,18 @@ __global__ void __launch_bounds__(256) k_nrm2_partial(const typename V2<R>::T* _
                                                       double* __restrict__ partials) {
     double v[1] = {0.0};
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const double xr = a[i].x, xi = a[i].y;
-        v[0] += xr * xr + xi * xi;
+    if constexpr (sizeof(R) == 4) {
+        float hh = 0.f, ll = 0.f;
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            const float2 x = a[i];
+            ff_addprod(hh, ll, x.x, x.x); ff_addprod(hh, ll, x.y, x.y);
+        }
+        v[0] = (double)hh + (double)ll;
+    } else {
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            const double xr = a[i].x, xi = a[i].y;
+            v[0] += xr * xr + xi * xi;
+        }
     }
     block_reduce_store<1>(v, partials + blockIdx.x);
 }
@@ -289,6 +343,7 @@ __global__ void __launch_bounds__(256) k_lanczos_update(typename V2<R>::T* __res
     const R are = (R)d_alpha[0], aim = (R)d_alpha[1];
     const R be = d_beta2 ? (R)sqrt(d_beta2[0]) : (R)0;   // beta = |w_prev| = sqrt(|w_prev|^2)
     double acc[1] = {0.0};
+    float hh = 0.f, ll = 0.f;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         C x = w[i];
@@ -301,8 +356,10 @@ __global__ void __launch_bounds__(256) k_lanczos_update(typename V2<R>::T* __res
             x.y = x.y - be * z.y;
         }
         w[i] = x;
-        acc[0] += (double)x.x * (double)x.x + (double)x.y * (double)x.y;
+        if constexpr (sizeof(R) == 4) { ff_addprod(hh, ll, x.x, x.x); ff_addprod(hh, ll, x.y, x.y); }
+        else acc[0] += (double)x.x * (double)x.x + (double)x.y * (double)x.y;
     }
+    if constexpr (sizeof(R) == 4) acc[0] = (double)hh + (double)ll;
     block_reduce_store<1>(acc, partials + blockIdx.x);
 }
 
@@ -325,12 +382,24 @@ __global__ void __launch_bounds__(256) k_scale_rsqrt(const typename V2<R>::T* in
     const double inv_ok = nrm > 0.0 ? 1.0 : 0.0;
     const double den = nrm > 0.0 ? nrm : 1.0;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const C x = in[i];
-        C y;
-        y.x = (R)(inv_ok * ((double)x.x / den));
-        y.y = (R)(inv_ok * ((double)x.y / den));
-        out[i] = y;
+    if constexpr (sizeof(R) == 4) {
+        const float inv = (float)(inv_ok / den);
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            const C x = in[i];
+            C y;
+            y.x = x.x * inv;
+            y.y = x.y * inv;
+            out[i] = y;
+        }
+    } else {
+        // Eigen's normalize() divides by the norm (src/DynLanczosSolver.h:100)
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            const C x = in[i];
+            C y;
+            y.x = (R)(inv_ok * ((double)x.x / den));
+            y.y = (R)(inv_ok * ((double)x.y / den));
+            out[i] = y;
+        }
     }
 }
 
@@ -349,9 +418,10 @@ __global__ void __launch_bounds__(256) k_axpby(const typename V2<R>::T* x, const
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const C p = x[i], q = y[i];
+        const R a_r = (R)ar, a_i = (R)ai, b_r = (R)br, b_i = (R)bi;
         C o;
-        o.x = (R)(ar * p.x - ai * p.y + br * q.x - bi * q.y);
-        o.y = (R)(ar * p.y + ai * p.x + br * q.y + bi * q.x);
+        o.x = a_r * p.x - a_i * p.y + b_r * q.x - b_i * q.y;
+        o.y = a_r * p.y + a_i * p.x + b_r * q.y + b_i * q.x;
         out[i] = o;
     }
 }
@@ -375,15 +445,33 @@ __global__ void __launch_bounds__(256) k_gemv_h(const typename V2<R>::T* __restr
         double v[2 * JB];
 #pragma unroll
         for (int q = 0; q < 2 * JB; q++) v[q] = 0.0;
-        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-            const double yr = w[i].x, yi = w[i].y;
+        if constexpr (sizeof(R) == 4) {
+            float hv[2 * JB], lv[2 * JB];
 #pragma unroll
-            for (int q = 0; q < JB; q++)
-                if (j0 + q < m) {
-                    const typename V2<R>::T x = L[(long long)(j0 + q) * ld + i];
-                    v[2 * q] += (double)x.x * yr + (double)x.y * yi;
-                    v[2 * q + 1] += (double)x.x * yi - (double)x.y * yr;
-                }
+            for (int q = 0; q < 2 * JB; q++) hv[q] = lv[q] = 0.f;
+            for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+                const float2 y = w[i];
+#pragma unroll
+                for (int q = 0; q < JB; q++)
+                    if (j0 + q < m) {
+                        const float2 x = L[(long long)(j0 + q) * ld + i];
+                        ff_addprod(hv[2 * q], lv[2 * q], x.x, y.x); ff_addprod(hv[2 * q], lv[2 * q], x.y, y.y);
+                        ff_addprod(hv[2 * q + 1], lv[2 * q + 1], x.x, y.y); ff_addprod(hv[2 * q + 1], lv[2 * q + 1], -x.y, y.x);
+                    }
+            }
+#pragma unroll
+            for (int q = 0; q < 2 * JB; q++) v[q] = (double)hv[q] + (double)lv[q];
+        } else {
+            for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+                const double yr = w[i].x, yi = w[i].y;
+#pragma unroll
+                for (int q = 0; q < JB; q++)
+                    if (j0 + q < m) {
+                        const typename V2<R>::T x = L[(long long)(j0 + q) * ld + i];
+                        v[2 * q] += (double)x.x * yr + (double)x.y * yi;
+                        v[2 * q + 1] += (double)x.x * yi - (double)x.y * yr;
+                    }
+            }
         }
         __shared__ double out[2 * JB];
         block_reduce_store<2 * JB>(v, out);
@@ -426,16 +514,28 @@ __global__ void __launch_bounds__(256) k_gemv_sub(const typename V2<R>::T* __res
     __syncthreads();
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        double sr = 0.0, si = 0.0;
-        for (int j = 0; j < m; j++) {
-            const typename V2<R>::T x = L[(long long)j * ld + i];
-            const double cr = rs[2 * j], ci = rs[2 * j + 1];
-            sr += (double)x.x * cr - (double)x.y * ci;
-            si += (double)x.x * ci + (double)x.y * cr;
-        }
         typename V2<R>::T y = w[i];
-        y.x = (R)((double)y.x - sr);
-        y.y = (R)((double)y.y - si);
+        if constexpr (sizeof(R) == 4) {
+            float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+            for (int j = 0; j < m; j++) {
+                const float2 x = L[(long long)j * ld + i];
+                const float cr = (float)rs[2 * j], ci = (float)rs[2 * j + 1];
+                ff_addprod(rh, rl, x.x, cr); ff_addprod(rh, rl, -x.y, ci);
+                ff_addprod(ih, il, x.x, ci); ff_addprod(ih, il, x.y, cr);
+            }
+            y.x = y.x - (rh + rl);
+            y.y = y.y - (ih + il);
+        } else {
+            double sr = 0.0, si = 0.0;
+            for (int j = 0; j < m; j++) {
+                const typename V2<R>::T x = L[(long long)j * ld + i];
+                const double cr = rs[2 * j], ci = rs[2 * j + 1];
+                sr += (double)x.x * cr - (double)x.y * ci;
+                si += (double)x.x * ci + (double)x.y * cr;
+            }
+            y.x = (R)((double)y.x - sr);
+            y.y = (R)((double)y.y - si);
+        }
         w[i] = y;
     }
 }
@@ -457,15 +557,27 @@ __global__ void __launch_bounds__(256) k_lincomb(const typename V2<R>::T* __rest
     __syncthreads();
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        double sr = 0.0, si = 0.0;
-        for (int j = 0; j < m; j++) {
-            const typename V2<R>::T x = L[(long long)j * ld + i];
-            sr += (double)x.x * zs[j];
-            si += (double)x.y * zs[j];
-        }
         typename V2<R>::T y;
-        y.x = (R)sr;
-        y.y = (R)si;
+        if constexpr (sizeof(R) == 4) {
+            float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+            for (int j = 0; j < m; j++) {
+                const float2 x = L[(long long)j * ld + i];
+                const float z = (float)zs[j];
+                ff_addprod(rh, rl, x.x, z);
+                ff_addprod(ih, il, x.y, z);
+            }
+            y.x = rh + rl;
+            y.y = ih + il;
+        } else {
+            double sr = 0.0, si = 0.0;
+            for (int j = 0; j < m; j++) {
+                const typename V2<R>::T x = L[(long long)j * ld + i];
+                sr += (double)x.x * zs[j];
+                si += (double)x.y * zs[j];
+            }
+            y.x = (R)sr;
+            y.y = (R)si;
+        }
         out[i] = y;
     }
 }
@@ -511,14 +623,24 @@ __global__ void k_start_normal(unsigned long long seed, typename V2<R>::T* out, 
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const unsigned long long h1 = splitmix64(base ^ (2ull * (unsigned long long)i));
         const unsigned long long h2 = splitmix64(base ^ (2ull * (unsigned long long)i + 1ull));
-        const double u1 = (double)((h1 >> 11) + 1ull) * 0x1.0p-53;   // (0, 1]
-        const double u2 = (double)(h2 >> 11) * 0x1.0p-53;            // [0, 1)
-        const double r = sqrt(-2.0 * log(u1));
-        double sn, cs;
-        sincospi(2.0 * u2, &sn, &cs);
         typename V2<R>::T o;
-        o.x = (R)(r * cs);
-        o.y = (R)(r * sn);
+        if constexpr (sizeof(R) == 4) {
+            const float u1 = (float)((h1 >> 40) + 1ull) * 0x1.0p-24f;   // (0, 1]
+            const float u2 = (float)(h2 >> 40) * 0x1.0p-24f;            // [0, 1)
+            const float r = sqrtf(-2.0f * logf(u1));
+            float sn, cs;
+            sincospif(2.0f * u2, &sn, &cs);
+            o.x = r * cs;
+            o.y = r * sn;
+        } else {
+            const double u1 = (double)((h1 >> 11) + 1ull) * 0x1.0p-53;   // (0, 1]
+            const double u2 = (double)(h2 >> 11) * 0x1.0p-53;            // [0, 1)
+            const double r = sqrt(-2.0 * log(u1));
+            double sn, cs;
+            sincospi(2.0 * u2, &sn, &cs);
+            o.x = (R)(r * cs);
+            o.y = (R)(r * sn);
+        }
         out[i] = o;
     }
 }

@@ -152,7 +152,14 @@ DevModel make_dev_model(const esc_params& p, const Lattice& L, const std::vector
             m.d[m.nd++] = DevDiagBond{mask, b.kz};
         }
     }
+    fill_float_copies(m);
     return m;
+}
+
+void fill_float_copies(DevModel& m) {
+    m.fxf = (float)m.fx; m.fyf = (float)m.fy; m.fzf = (float)m.fz;
+    for (int b = 0; b < m.nb; b++) { m.ceqf[b] = (float)m.b[b].ceq; m.cdifff[b] = (float)m.b[b].cdiff; }
+    for (int b = 0; b < m.nd; b++) m.dqf[b] = (float)(0.25 * m.d[b].dz);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -266,6 +273,8 @@ DevOp make_dev_op(const std::vector<OpTerm>& terms, const std::vector<int>* perm
         d.fac[t] = fac;
         d.cre[t] = o.coef.real();
         d.cim[t] = o.coef.imag();
+        d.cref[t] = (float)o.coef.real();
+        d.cimf[t] = (float)o.coef.imag();
     }
     return d;
 }
