@@ -35,6 +35,8 @@ struct esc_handle {
     void* d_work = nullptr; size_t work_bytes = 0;     // work vectors
     void* d_gs = nullptr; size_t gs_bytes = 0;         // ground state
     void* d_io = nullptr; size_t io_bytes = 0;         // staging for host-pointer calls
+    void* d_diag[2] = {nullptr, nullptr};              // diagonal of the bond terms per dtype
+    size_t diag_bytes[2] = {0, 0};
     // ground-state Lanczos results
     int nsteps = 0;
     bool have_gs = false, have_basis = false;
@@ -100,6 +102,24 @@ void ensure_t(T*& p, size_t& cap, size_t need) {
 }
 
 void sync(esc_handle* h) { ESC_CUDA(cudaStreamSynchronize(h->stream)); }
+
+// Precomputed bond diagonal (the analogue of the reference's HDiag without the field term),
+// 4 B/state for complex64, 8 B/state for complex128; computed on first use.  If it cannot be
+// allocated the tiled kernel computes the diagonal itself (slower, same result).
+const void* diag_for(esc_handle* h, esc_dtype dt) {
+    const int i = dt == ESC_C64 ? 1 : 0;
+    if (h->d_diag[i]) return h->d_diag[i];
+    const size_t need = (size_t)h->D * (dt == ESC_C64 ? 4 : 8);
+    if (cudaMalloc(&h->d_diag[i], need) != cudaSuccess) {
+        (void)cudaGetLastError();
+        h->d_diag[i] = nullptr;
+        return nullptr;
+    }
+    h->diag_bytes[i] = need;
+    if (dt == ESC_C64) esc::launch_diag<float>(h->dm, h->d_diag[i], h->D, h->stream);
+    else esc::launch_diag<double>(h->dm, h->d_diag[i], h->D, h->stream);
+    return h->d_diag[i];
+}
 
 void ensure_partials(esc_handle* h, int rows) {
     const size_t need = (size_t)std::max(rows, 4) * esc::RED_MAX_BLOCKS * 2 * sizeof(double);
@@ -175,7 +195,10 @@ struct Pipe {
     static constexpr size_t ES = 2 * sizeof(R);
     int64_t D;
     explicit Pipe(esc_handle* hh) : h(hh), D(hh->D) {}
-    void hv(const void* in, void* out) { esc::launch_hv_tiled<R>(h->dm, h->passes, in, out, D, h->stream); }
+    void hv(const void* in, void* out) {
+        esc::launch_hv_tiled<R>(h->dm, h->passes, in, out, D, diag_for(h, sizeof(R) == 4 ? ESC_C64 : ESC_C128),
+                                h->stream);
+    }
     void apply(const esc::DevOp& op, const void* in, void* out) { esc::launch_apply<R>(op, in, out, D, h->stream); }
     void dot(const void* a, const void* b, double* dst) { esc::launch_dot<R>(a, b, D, h->d_part, dst, h->stream); }
     void nrm2(const void* a, double* dst) { esc::launch_nrm2<R>(a, D, h->d_part, dst, h->stream); }
@@ -441,7 +464,7 @@ esc_status esc_create(const esc_params* p, esc_handle** out) {
 
 esc_status esc_destroy(esc_handle* h) {
     if (!h) return ESC_OK;
-    for (void* p : {(void*)h->d_part, (void*)h->d_sc, h->d_L, h->d_work, h->d_gs, h->d_io})
+    for (void* p : {(void*)h->d_part, (void*)h->d_sc, h->d_L, h->d_work, h->d_gs, h->d_io, h->d_diag[0], h->d_diag[1]})
         if (p) cudaFree(p);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -479,8 +502,9 @@ esc_status esc_hv(esc_handle* h, const void* in, void* out, esc_dtype dt, int fl
     if (in == out) return finish(h, ESC_ERR_PARAM, "esc_hv: in and out must differ");
     return guarded(h, [&]() {
         Staged s = stage(h, in, out, 1, h->D, dt, flags);
-        if (dt == ESC_C64) esc::launch_hv_tiled<float>(h->dm, h->passes, s.in, s.out, h->D, h->stream);
-        else esc::launch_hv_tiled<double>(h->dm, h->passes, s.in, s.out, h->D, h->stream);
+        const void* dg = diag_for(h, dt);
+        if (dt == ESC_C64) esc::launch_hv_tiled<float>(h->dm, h->passes, s.in, s.out, h->D, dg, h->stream);
+        else esc::launch_hv_tiled<double>(h->dm, h->passes, s.in, s.out, h->D, dg, h->stream);
         unstage(h, s, out, 1, h->D, dt, flags);
     });
 }

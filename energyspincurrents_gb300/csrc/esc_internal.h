@@ -112,11 +112,18 @@ struct DevPass {
     double ceq[MAX_PTERMS], cdiff[MAX_PTERMS];
     float ceqf[MAX_PTERMS], cdifff[MAX_PTERMS];   // the same in float for the complex64 path
     unsigned int flm[MAX_SITES];               // field-term masks in tile-local bits
+    // fast kernel (512 threads, thread t owns tile states t + 512 j): parity of the bits of
+    // (512 j) under each term mask, bit j
+    unsigned int bjpar[MAX_PTERMS];
+    unsigned int fjbit[MAX_SITES];
 };
 // Builds one DevPass per plan pass from the relabelled model; throws if a term fits no tile.
 std::vector<DevPass> make_passes(const Plan& P, const DevModel& m);
+// diag: precomputed diagonal of the bond terms (no field), R per state (launch_diag); may be NULL,
+// then the diagonal is computed in the kernel.
 template <typename R> void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in,
-                                           void* out, int64_t D, cudaStream_t s);
+                                           void* out, int64_t D, const void* diag, cudaStream_t s);
+template <typename R> void launch_diag(const DevModel& m, void* diag, int64_t D, cudaStream_t s);
 // Basis permutation: out[j] = in[src(j)], src assembled bitwise from five 8-bit tables.
 struct DevPerm {
     unsigned long long tab[5][256];

@@ -103,6 +103,120 @@ __global__ void __launch_bounds__(TILE_THREADS) k_hv_pass(const __grid_constant_
     }
 }
 
+// Diagonal of the bond terms, R per state.  FP64: the reference's operations and order
+// (HDiag, src/Hamiltonian.h:344-360), so that adding Bz*SzT later reproduces HDiag bit for bit.
+template <typename R>
+__global__ void __launch_bounds__(256) k_diag(const __grid_constant__ DevModel m, R* __restrict__ diag, long long D) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < D; k += stride) {
+        const unsigned long long uk = (unsigned long long)k;
+        if constexpr (sizeof(R) == 4) {
+            float d = 0.0f;
+            for (int b = 0; b < m.nd; b++) d += (__popcll(uk & m.d[b].mask) == 1) ? -m.dqf[b] : m.dqf[b];
+            diag[k] = d;
+        } else {
+            double d = 0.0;
+            for (int b = 0; b < m.nd; b++) {
+                const double q = 0.25 * m.d[b].dz;
+                d += (__popcll(uk & m.d[b].mask) == 1) ? -q : q;
+            }
+            diag[k] = d;
+        }
+    }
+}
+
+// Fast pass: 512 threads, c = 3, thread t owns the E tile states t + 512 j (j < E), so a state's
+// tile-local index splits into thread bits (< 9) and j bits (>= 9).  Term parameters are read once
+// per thread per term; the parity of a term's mask over the j bits is a host-precomputed bit mask
+// (bjpar / fjbit), the thread-bit part one POPC.  Diagonal read from the precomputed vector.
+template <typename R, int E>
+__global__ void __launch_bounds__(TILE_THREADS) k_hv_pass_fast(const __grid_constant__ DevModel m,
+                                                                const __grid_constant__ DevPass p,
+                                                                const R* __restrict__ diag,
+                                                                const typename V2T<R>::T* __restrict__ in,
+                                                                typename V2T<R>::T* __restrict__ out,
+                                                                long long ntiles) {
+    typedef typename V2T<R>::T C;
+    constexpr bool F32 = sizeof(R) == 4;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* tile = reinterpret_cast<C*>(smem_raw);
+    __shared__ unsigned long long hi_off[E];
+    const int tid = threadIdx.x;
+    if (tid < E) hi_off[tid] = p.tabHi[tid];
+    const unsigned long long lo = p.tabLo[tid >> 3] | (unsigned long long)(tid & 7);
+    const R fx = F32 ? (R)m.fxf : (R)m.fx, fy = F32 ? (R)m.fyf : (R)m.fy;
+    const R fz = F32 ? (R)m.fzf : (R)m.fz;
+    __syncthreads();
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        unsigned long long base = lo;
+        for (int q = 0; q < p.nrest; q++) base |= (((unsigned long long)t >> q) & 1ull) << p.rest[q];
+#pragma unroll
+        for (int j = 0; j < E; j++) tile[tid + TILE_THREADS * j] = in[base | hi_off[j]];
+        __syncthreads();
+        R ar[E], ai[E];
+        if (p.diag) {
+#pragma unroll
+            for (int j = 0; j < E; j++) {
+                const unsigned long long k = base | hi_off[j];
+                const R d = diag[k];
+                const R nz = (R)(m.N - 2 * __popcll(k));
+                R dg;
+                if constexpr (F32) dg = fmaf(fz, nz, d);
+                else dg = __dadd_rn(d, __dmul_rn(fz, nz));    // HDiag += Bzz*SzT (src/Hamiltonian.h:374)
+                const C v = tile[tid + TILE_THREADS * j];
+                ar[j] = dg * v.x;
+                ai[j] = dg * v.y;
+            }
+        } else if (p.accumulate) {
+#pragma unroll
+            for (int j = 0; j < E; j++) {
+                const C o = out[base | hi_off[j]];
+                ar[j] = o.x;
+                ai[j] = o.y;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < E; j++) ar[j] = ai[j] = (R)0;
+        }
+        for (int b = 0; b < p.nbond; b++) {
+            const unsigned int lm = p.blm[b];
+            const unsigned int jp = p.bjpar[b];
+            const unsigned int pb = __popc((unsigned)tid & lm) & 1u;
+            R c0, c1;
+            if constexpr (F32) { c0 = p.ceqf[b]; c1 = p.cdifff[b]; }
+            else { c0 = p.ceq[b]; c1 = p.cdiff[b]; }
+#pragma unroll
+            for (int j = 0; j < E; j++) {
+                const R c = (pb ^ ((jp >> j) & 1u)) ? c1 : c0;
+                const C w = tile[(tid + TILE_THREADS * j) ^ lm];
+                ar[j] = fma(c, w.x, ar[j]);
+                ai[j] = fma(c, w.y, ai[j]);
+            }
+        }
+        for (int f = 0; f < p.nfield; f++) {
+            const unsigned int lm = p.flm[f];
+            const unsigned int jb = p.fjbit[f];
+            const bool tb = ((unsigned)tid & lm) != 0u;
+#pragma unroll
+            for (int j = 0; j < E; j++) {
+                // (Bx/2 + i By/2 (bit ? +1 : -1)) v[k ^ 2^s]
+                const R sfy = (tb || ((jb >> j) & 1u)) ? fy : -fy;
+                const C w = tile[(tid + TILE_THREADS * j) ^ lm];
+                ar[j] = fma(fx, w.x, ar[j]); ar[j] = fma(-sfy, w.y, ar[j]);
+                ai[j] = fma(fx, w.y, ai[j]); ai[j] = fma(sfy, w.x, ai[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < E; j++) {
+            C o;
+            o.x = ar[j];
+            o.y = ai[j];
+            out[base | hi_off[j]] = o;
+        }
+        __syncthreads();
+    }
+}
+
 std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
     const int np = (int)P.tiles.size();
     std::vector<DevPass> out(np);
@@ -145,13 +259,18 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
             d.cdiff[d.nbond] = m.b[b].cdiff;
             d.ceqf[d.nbond] = (float)m.b[b].ceq;
             d.cdifff[d.nbond] = (float)m.b[b].cdiff;
+            for (int j = 0; j < 32; j++)
+                d.bjpar[d.nbond] |= (unsigned)(__builtin_popcount(((unsigned)j << 9) & d.blm[d.nbond]) & 1) << j;
             d.nbond++;
             bdone[b] = 1;
         }
         if (m.fx != 0.0 || m.fy != 0.0)
             for (int s = 0; s < P.N; s++) {
                 if (fdone[s] || !((tmask >> s) & 1ull)) continue;
-                d.flm[d.nfield++] = local(1ull << s);
+                d.flm[d.nfield] = local(1ull << s);
+                for (int j = 0; j < 32; j++)
+                    d.fjbit[d.nfield] |= (unsigned)((((unsigned)j << 9) & d.flm[d.nfield]) != 0u) << j;
+                d.nfield++;
                 fdone[s] = 1;
             }
     }
@@ -161,18 +280,50 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
 }
 
 template <typename R>
-void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in, void* out, int64_t D,
-                     cudaStream_t s) {
+void launch_diag(const DevModel& m, void* diag, int64_t D, cudaStream_t s) {
+    long long g = (D + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    k_diag<R><<<(unsigned)g, 256, 0, s>>>(m, (R*)diag, (long long)D);
+    ESC_CUDA(cudaGetLastError());
+}
+
+template <typename R, int E>
+static void run_fast(const DevModel& m, const DevPass& p, const void* diag, const void* in, void* out, int64_t D,
+                     int sms, cudaStream_t s) {
     typedef typename V2T<R>::T C;
+    const size_t smem = (size_t)TILE_THREADS * E * sizeof(C);
+    if (smem > 48 * 1024)
+        ESC_CUDA(cudaFuncSetAttribute(k_hv_pass_fast<R, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass_fast<R, E>, TILE_THREADS, smem));
+    const long long ntiles = (long long)(D >> p.Tp);
+    const long long g = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
+    k_hv_pass_fast<R, E><<<(unsigned)g, TILE_THREADS, smem, s>>>(m, p, (const R*)diag, (const C*)in, (C*)out, ntiles);
+    ESC_CUDA(cudaGetLastError());
+}
+
+template <typename R>
+void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in, void* out, int64_t D,
+                     const void* diag, cudaStream_t s) {
+    typedef typename V2T<R>::T C;
+    int dev = 0, sms = 0;
+    ESC_CUDA(cudaGetDevice(&dev));
+    ESC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     for (const DevPass& p : passes) {
+        if (diag && p.c == 3 && p.Tp >= 10 && p.Tp <= 13) {
+            switch (p.Tp) {
+                case 10: run_fast<R, 2>(m, p, diag, in, out, D, sms, s); break;
+                case 11: run_fast<R, 4>(m, p, diag, in, out, D, sms, s); break;
+                case 12: run_fast<R, 8>(m, p, diag, in, out, D, sms, s); break;
+                default: run_fast<R, 16>(m, p, diag, in, out, D, sms, s); break;
+            }
+            continue;
+        }
         const size_t smem = (size_t(1) << p.Tp) * sizeof(C);
         if (smem > 48 * 1024)
             ESC_CUDA(cudaFuncSetAttribute(k_hv_pass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         int per_sm = 0;
         ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass<R>, TILE_THREADS, smem));
-        int dev = 0, sms = 0;
-        ESC_CUDA(cudaGetDevice(&dev));
-        ESC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         const long long ntiles = (long long)(D >> p.Tp);
         const long long g = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
         k_hv_pass<R><<<(unsigned)g, TILE_THREADS, smem, s>>>(m, p, (const C*)in, (C*)out, ntiles);
@@ -220,8 +371,12 @@ void launch_permute(const DevPerm& p, const void* in, void* out, int64_t D, cuda
     ESC_CUDA(cudaGetLastError());
 }
 
-template void launch_hv_tiled<double>(const DevModel&, const std::vector<DevPass>&, const void*, void*, int64_t, cudaStream_t);
-template void launch_hv_tiled<float>(const DevModel&, const std::vector<DevPass>&, const void*, void*, int64_t, cudaStream_t);
+template void launch_hv_tiled<double>(const DevModel&, const std::vector<DevPass>&, const void*, void*, int64_t,
+                                      const void*, cudaStream_t);
+template void launch_hv_tiled<float>(const DevModel&, const std::vector<DevPass>&, const void*, void*, int64_t,
+                                     const void*, cudaStream_t);
+template void launch_diag<double>(const DevModel&, void*, int64_t, cudaStream_t);
+template void launch_diag<float>(const DevModel&, void*, int64_t, cudaStream_t);
 template void launch_permute<double>(const DevPerm&, const void*, void*, int64_t, cudaStream_t);
 template void launch_permute<float>(const DevPerm&, const void*, void*, int64_t, cudaStream_t);
 
