@@ -217,6 +217,127 @@ __global__ void __launch_bounds__(TILE_THREADS) k_hv_pass_fast(const __grid_cons
     }
 }
 
+// Complex64 pass, v2.  Same ownership as k_hv_pass_fast (thread t owns states t + 512 j), but each
+// term is dispatched on the high part of its tile-local mask (bits >= 9, LMH < E): the partner of
+// state t + 512 j is (t ^ lm_lo) + 512 (j ^ LMH) and the j part of the bond parity is
+// popcount(j & LMH), both compile-time after unrolling.  Per state and term this leaves one shared
+// load and one packed FFMA2 (bond) or one FFMA2 + one FADD2 (field: acc += fx w, G += +-w; the
+// i*By/2*G part is added once at the end).
+template <int E, int LMH>
+__device__ __forceinline__ void bond_f32(const float2* __restrict__ tile, int tid, unsigned lm_lo, float cA, float cB,
+                                         float2 (&acc)[E]) {
+    const float2* src = tile + (tid ^ (int)lm_lo);
+    const float2 vA = make_float2(cA, cA), vB = make_float2(cB, cB);
+#pragma unroll
+    for (int j = 0; j < E; j++) {
+        const float2 w = src[TILE_THREADS * (j ^ LMH)];
+        acc[j] = __ffma2_rn((__builtin_popcount(j & LMH) & 1) ? vB : vA, w, acc[j]);
+    }
+}
+template <int E, int FB>
+__device__ __forceinline__ void field_f32(const float2* __restrict__ tile, int tid, unsigned lm_lo, bool tb,
+                                          float2 vfx, float2 (&acc)[E], float2 (&G)[E]) {
+    const float2* src = tile + (tid ^ (int)lm_lo);
+#pragma unroll
+    for (int j = 0; j < E; j++) {
+        const int jj = FB < 0 ? j : (j ^ (1 << FB));
+        const float2 w = src[TILE_THREADS * jj];
+        const bool bit = FB < 0 ? tb : ((j >> FB) & 1);
+        acc[j] = __ffma2_rn(vfx, w, acc[j]);
+        G[j] = bit ? __fadd2_rn(G[j], w) : __fadd2_rn(G[j], make_float2(-w.x, -w.y));
+    }
+}
+
+template <int E, int L = 0>
+__device__ __forceinline__ void bond_dispatch(int lmh, const float2* tile, int tid, unsigned lm_lo, float cA, float cB,
+                                              float2 (&acc)[E]) {
+    if constexpr (L < E) {
+        if (lmh == L) bond_f32<E, L>(tile, tid, lm_lo, cA, cB, acc);
+        else bond_dispatch<E, L + 1>(lmh, tile, tid, lm_lo, cA, cB, acc);
+    }
+}
+template <int E, int FB = -1>
+__device__ __forceinline__ void field_dispatch(int fb, const float2* tile, int tid, unsigned lm_lo, bool tb, float2 vfx,
+                                               float2 (&acc)[E], float2 (&G)[E]) {
+    if constexpr ((1 << (FB < 0 ? 0 : FB)) < E || FB < 0) {
+        if (fb == FB) field_f32<E, FB>(tile, tid, lm_lo, tb, vfx, acc, G);
+        else if constexpr ((2 << (FB < 0 ? -1 + 1 : FB)) < E || FB < 0) field_dispatch<E, FB + 1>(fb, tile, tid, lm_lo, tb, vfx, acc, G);
+    }
+}
+
+template <int E>
+__global__ void __launch_bounds__(TILE_THREADS) k_hv_pass_f32(const __grid_constant__ DevModel m,
+                                                               const __grid_constant__ DevPass p,
+                                                               const float* __restrict__ diag,
+                                                               const float2* __restrict__ in,
+                                                               float2* __restrict__ out, long long ntiles) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* tile = reinterpret_cast<float2*>(smem_raw);
+    __shared__ unsigned long long hi_off[E];
+    const int tid = threadIdx.x;
+    if (tid < E) hi_off[tid] = p.tabHi[tid];
+    const unsigned long long lo = p.tabLo[tid >> 3] | (unsigned long long)(tid & 7);
+    // 16-byte loads: thread t copies states 2t' and 2t'+1, t' = t + 512 i (runs of 8 never split)
+    const unsigned long long lo2 = p.tabLo[(tid >> 2) & 63] | (unsigned long long)((2 * tid) & 7);
+    const int hi2 = tid >> 8;
+    const float2 vfx = make_float2(m.fxf, m.fxf);
+    const float fy = m.fyf, fz = m.fzf;
+    __syncthreads();
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        unsigned long long tb_bits = 0;
+        for (int q = 0; q < p.nrest; q++) tb_bits |= (((unsigned long long)t >> q) & 1ull) << p.rest[q];
+        const unsigned long long base = tb_bits | lo;
+        {
+            const unsigned long long b2 = tb_bits | lo2;
+            float4* t4 = reinterpret_cast<float4*>(tile);
+#pragma unroll
+            for (int i = 0; i < E / 2; i++)
+                t4[tid + TILE_THREADS * i] = *reinterpret_cast<const float4*>(in + (b2 | hi_off[hi2 + 2 * i]));
+        }
+        __syncthreads();
+        float2 acc[E], G[E];
+#pragma unroll
+        for (int j = 0; j < E; j++) G[j] = make_float2(0.f, 0.f);
+        if (p.diag) {
+#pragma unroll
+            for (int j = 0; j < E; j++) {
+                const unsigned long long k = base | hi_off[j];
+                const float dg = fmaf(fz, (float)(m.N - 2 * __popcll(k)), diag[k]);
+                const float2 v = tile[tid + TILE_THREADS * j];
+                acc[j] = make_float2(dg * v.x, dg * v.y);
+            }
+        } else if (p.accumulate) {
+#pragma unroll
+            for (int j = 0; j < E; j++) acc[j] = out[base | hi_off[j]];
+        } else {
+#pragma unroll
+            for (int j = 0; j < E; j++) acc[j] = make_float2(0.f, 0.f);
+        }
+        for (int b = 0; b < p.nbond; b++) {
+            const unsigned int lm = p.blm[b];
+            const bool pb = __popc((unsigned)tid & lm & (TILE_THREADS - 1)) & 1;
+            const float cA = pb ? p.cdifff[b] : p.ceqf[b], cB = pb ? p.ceqf[b] : p.cdifff[b];
+            bond_dispatch<E>((int)(lm >> 9), tile, tid, lm & (TILE_THREADS - 1), cA, cB, acc);
+        }
+        for (int f = 0; f < p.nfield; f++) {
+            const unsigned int lm = p.flm[f];
+            const unsigned int lo9 = lm & (TILE_THREADS - 1);
+            const bool tb = ((unsigned)tid & lo9) != 0u;
+            const int fb = lo9 ? -1 : (31 - __clz((int)(lm >> 9)));
+            field_dispatch<E>(fb, tile, tid, lo9, tb, vfx, acc, G);
+        }
+#pragma unroll
+        for (int j = 0; j < E; j++) {
+            // acc += i fy G
+            float2 o = acc[j];
+            o.x = fmaf(-fy, G[j].y, o.x);
+            o.y = fmaf(fy, G[j].x, o.y);
+            out[base | hi_off[j]] = o;
+        }
+        __syncthreads();
+    }
+}
+
 std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
     const int np = (int)P.tiles.size();
     std::vector<DevPass> out(np);
@@ -302,6 +423,21 @@ static void run_fast(const DevModel& m, const DevPass& p, const void* diag, cons
     ESC_CUDA(cudaGetLastError());
 }
 
+template <int E>
+static void run_f32(const DevModel& m, const DevPass& p, const void* diag, const void* in, void* out, int64_t D, int sms,
+                    cudaStream_t s) {
+    const size_t smem = (size_t)TILE_THREADS * E * sizeof(float2);
+    if (smem > 48 * 1024)
+        ESC_CUDA(cudaFuncSetAttribute(k_hv_pass_f32<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass_f32<E>, TILE_THREADS, smem));
+    const long long ntiles = (long long)(D >> p.Tp);
+    const long long g = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
+    k_hv_pass_f32<E><<<(unsigned)g, TILE_THREADS, smem, s>>>(m, p, (const float*)diag, (const float2*)in, (float2*)out,
+                                                             ntiles);
+    ESC_CUDA(cudaGetLastError());
+}
+
 template <typename R>
 void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in, void* out, int64_t D,
                      const void* diag, cudaStream_t s) {
@@ -310,6 +446,16 @@ void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, cons
     ESC_CUDA(cudaGetDevice(&dev));
     ESC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     for (const DevPass& p : passes) {
+        if constexpr (sizeof(R) == 4) {
+            if (diag && p.c == 3 && p.Tp >= 11 && p.Tp <= 13) {
+                switch (p.Tp) {
+                    case 11: run_f32<4>(m, p, diag, in, out, D, sms, s); break;
+                    case 12: run_f32<8>(m, p, diag, in, out, D, sms, s); break;
+                    default: run_f32<16>(m, p, diag, in, out, D, sms, s); break;
+                }
+                continue;
+            }
+        }
         if (diag && p.c == 3 && p.Tp >= 10 && p.Tp <= 13) {
             switch (p.Tp) {
                 case 10: run_fast<R, 2>(m, p, diag, in, out, D, sms, s); break;
