@@ -69,7 +69,7 @@ _lib = None
 # every symbol declared in include/esc.h
 EXPORTS = ["esc_params_default", "esc_params_from_file", "esc_lattice", "esc_plan", "esc_create", "esc_destroy", "esc_last_error",
            "esc_num_sites", "esc_dim", "esc_neighbors", "esc_basis_permutation", "esc_stream", "esc_hv", "esc_hv_batched", "esc_apply_op",
-           "esc_start_vector", "esc_lanczos_gs", "esc_spectrum", "esc_measure_local", "esc_grad"]
+           "esc_start_vector", "esc_rayleigh", "esc_lanczos_gs", "esc_spectrum", "esc_measure_local", "esc_grad"]
 
 
 def lib_path():
@@ -104,6 +104,7 @@ def lib():
     L.esc_hv_batched.argtypes = [vp, vp, vp, ci, i64, vp, ci, ci]
     L.esc_apply_op.argtypes = [vp, ci, ci, vp, vp, ci, ci]
     L.esc_start_vector.argtypes = [vp, ci, ci, vp, ci, ci]
+    L.esc_rayleigh.argtypes = [vp, vp, ci, ci, P(cd)]
     L.esc_lanczos_gs.argtypes = [vp, P(LanczosCfg), vp, ci, P(cd), vp, vp, vp, P(ci), vp]
     L.esc_spectrum.argtypes = [vp, P(DynCfg), vp, P(ci), P(ci)]
     L.esc_measure_local.argtypes = [vp, vp, vp]
@@ -285,6 +286,13 @@ class Handle:
                                             ctypes.byref(E0), _ptr(a), _ptr(b), _ptr(r), ctypes.byref(n), _ptr(gs)))
         n = n.value
         return dict(E0=E0.value, alpha=a[:n], beta=b[: n + 1], ritz=r[:n], steps=n, gs=gs)
+
+    def rayleigh(self, v, flags=0):
+        """<v|H|v>/<v|v> in FP64 arithmetic (v complex128 or complex64)."""
+        v = np.ascontiguousarray(v)
+        E = ctypes.c_double()
+        _check(self.h, lib().esc_rayleigh(self.h, _ptr(v), _dt(v), flags, ctypes.byref(E)))
+        return E.value
 
     def spectrum(self, kind, mode="Ritz", omega_steps=None, domega=None, eta=None, cf_steps=0):
         p = self.params.p

@@ -212,7 +212,11 @@ void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) 
     const int64_t D = h->D;
     const size_t ES = Pipe<R>::ES;
     const int M = cfg.steps;
-    const bool store = cfg.lanctype != 0;                // OnlyEgs keeps no basis (returns a zero vector)
+    // GS without reorthogonalisation keeps three vectors and rebuilds |gs> in a second pass
+    // (the Lanczos vectors are recomputed from the recorded alpha/beta, not stored): the mode for
+    // bases too large to hold M+1 vectors (N = 28..32).
+    const bool recompute = cfg.lanctype == 1 && !cfg.reortho;
+    const bool store = cfg.lanctype != 0 && !recompute;  // OnlyEgs keeps no basis (returns a zero vector)
     const bool reo = store && cfg.reortho;
     const int nvec = store ? M + 1 : 3;
     h->have_gs = h->have_basis = false;
@@ -296,7 +300,21 @@ void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) 
     h->ritz = d;
     h->nsteps = n;
     ensure(h->d_gs, h->gs_bytes, (size_t)D * 16);
-    if (store) {
+    if (recompute) {
+        // second pass: identical kernels on identical inputs regenerate L_0..L_{n-1} bit for bit
+        ESC_CUDA(cudaMemcpyAsync(d_z, h->Z.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        ESC_CUDA(cudaMemsetAsync(h->d_gs, 0, (size_t)D * ES, h->stream));
+        P.nrm2(d_start, d_tmp);
+        P.scale(d_start, Lv(0), d_tmp);
+        esc::launch_axpy_dev<R>(Lv(0), h->d_gs, d_z, D, h->stream);
+        for (int it = 0; it + 1 < n; it++) {
+            P.hv(Lv(it), w);
+            esc::launch_lanczos_update<R>(w, Lv(it), it ? Lv(it - 1) : nullptr, d_alpha + 2 * it, it ? d_b2 + it : nullptr,
+                                          D, h->d_part, d_tmp + 2, h->stream);
+            P.scale(w, Lv(it + 1), d_b2 + it + 1);
+            esc::launch_axpy_dev<R>(Lv(it + 1), h->d_gs, d_z + it + 1, D, h->stream);
+        }
+    } else if (store) {
         // PsiAll[0] = sum_m L_m Z(m,0) (:208-234), without forming the other Ritz vectors
         ESC_CUDA(cudaMemcpyAsync(d_z, h->Z.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
         esc::launch_lincomb<R>(h->d_L, D, n, d_z, h->d_gs, D, h->stream);
@@ -431,7 +449,7 @@ esc_status esc_create(const esc_params* p, esc_handle** out) {
         std::vector<std::pair<int, int>> pairs;
         for (const auto& b : h->bonds)
             if (b.kx - b.ky != 0.0 || b.kx + b.ky != 0.0) pairs.push_back({b.i, b.j});
-        int T = 13, c = 3;
+        int T = 12, c = 3;
         if (const char* e = std::getenv("ESC_TILE_BITS")) T = std::atoi(e);
         if (const char* e = std::getenv("ESC_TILE_LOW")) c = std::atoi(e);
         h->plan = esc::make_plan(h->N, pairs, T, c, 200);
@@ -901,12 +919,31 @@ extern "C" esc_status esc_plan(const esc_params* p, int tile_bits, int low_bits,
         std::vector<std::pair<int, int>> pairs;
         for (const auto& b : bonds)
             if (b.kx - b.ky != 0.0 || b.kx + b.ky != 0.0) pairs.push_back({b.i, b.j});
-        esc::Plan P = esc::make_plan(L.N, pairs, tile_bits > 0 ? tile_bits : 13, low_bits > 0 ? low_bits : 3, 200);
+        esc::Plan P = esc::make_plan(L.N, pairs, tile_bits > 0 ? tile_bits : 12, low_bits > 0 ? low_bits : 3, 200);
         std::vector<esc::Bond> rb(bonds);
         for (auto& b : rb) { b.i = P.perm[b.i]; b.j = P.perm[b.j]; }
         const esc::DevModel m = esc::make_dev_model(*p, L, rb, p->Bxx, p->Byy, p->Bzz);
         const auto passes = esc::make_passes(P, m);   // throws if a term fits no tile
         if (bit_of_site) std::copy(P.perm.begin(), P.perm.end(), bit_of_site);
         if (npasses) *npasses = (int)passes.size();
+    });
+}
+
+extern "C" esc_status esc_rayleigh(esc_handle* h, const void* v, esc_dtype dt, int flags, double* E) {
+    if (!h || !v || !E) return finish(h, ESC_ERR_PARAM, "null argument");
+    return guarded(h, [&]() {
+        Staged s = stage(h, v, nullptr, 1, h->D, dt, flags);
+        ensure_partials(h, 4);
+        std::vector<double> num;
+        const int maxb = esc::RED_MAX_BLOCKS;
+        if (dt == ESC_C64) esc::launch_energy<float>(h->dm, h->passes, s.in, h->D, h->d_part, maxb, num, h->stream);
+        else esc::launch_energy<double>(h->dm, h->passes, s.in, h->D, h->d_part, maxb, num, h->stream);
+        ensure_t(h->d_sc, h->sc_bytes, std::max<size_t>(h->sc_bytes, 64));
+        if (dt == ESC_C64) esc::launch_dot<float>(s.in, s.in, h->D, h->d_part, h->d_sc, h->stream);
+        else esc::launch_dot<double>(s.in, s.in, h->D, h->d_part, h->d_sc, h->stream);
+        double nn[2];
+        ESC_CUDA(cudaMemcpyAsync(nn, h->d_sc, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        sync(h);
+        *E = num[0] / nn[0];
     });
 }

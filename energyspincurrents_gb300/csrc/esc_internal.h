@@ -124,6 +124,12 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m);
 template <typename R> void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in,
                                            void* out, int64_t D, const void* diag, cudaStream_t s);
 template <typename R> void launch_diag(const DevModel& m, void* diag, int64_t D, cudaStream_t s);
+// host_sum = <v|H|v> (re, im) computed in FP64 pass by pass; S = storage precision of v.
+template <typename S> void launch_energy(const DevModel& m, const std::vector<DevPass>& passes, const void* in,
+                                         int64_t D, double* partials, int max_blocks, std::vector<double>& host_sum,
+                                         cudaStream_t s);
+// y += z[idx] * x  (real coefficient read from device memory)
+template <typename R> void launch_axpy_dev(const void* x, void* y, const double* d_coef, int64_t n, cudaStream_t s);
 // Basis permutation: out[j] = in[src(j)], src assembled bitwise from five 8-bit tables.
 struct DevPerm {
     unsigned long long tab[5][256];

@@ -265,53 +265,71 @@ __device__ __forceinline__ void field_dispatch(int fb, const float2* tile, int t
     }
 }
 
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int NPEND>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(NPEND) : "memory"); }
+
 template <int E>
-__global__ void __launch_bounds__(TILE_THREADS) k_hv_pass_f32(const __grid_constant__ DevModel m,
+__device__ __forceinline__ unsigned long long tile_bits_of(const DevPass& p, long long t) {
+    unsigned long long b = 0;
+    for (int q = 0; q < p.nrest; q++) b |= (((unsigned long long)t >> q) & 1ull) << p.rest[q];
+    return b;
+}
+
+// Double-buffered: tile t+G is copied into the other buffer (cp.async, 16 B per copy) while tile t
+// is computed; the diagonal / partial-sum loads of tile t are issued before the term loops and
+// consumed after them.
+template <int E>
+__global__ void __launch_bounds__(TILE_THREADS, 2) k_hv_pass_f32(const __grid_constant__ DevModel m,
                                                                const __grid_constant__ DevPass p,
                                                                const float* __restrict__ diag,
                                                                const float2* __restrict__ in,
                                                                float2* __restrict__ out, long long ntiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2* tile = reinterpret_cast<float2*>(smem_raw);
+    float2* bufs = reinterpret_cast<float2*>(smem_raw);   // 2 x (512 E) states
     __shared__ unsigned long long hi_off[E];
     const int tid = threadIdx.x;
     if (tid < E) hi_off[tid] = p.tabHi[tid];
     const unsigned long long lo = p.tabLo[tid >> 3] | (unsigned long long)(tid & 7);
-    // 16-byte loads: thread t copies states 2t' and 2t'+1, t' = t + 512 i (runs of 8 never split)
+    // 16-byte copies: thread t moves states 2t' and 2t'+1, t' = t + 512 i (runs of 8 never split)
     const unsigned long long lo2 = p.tabLo[(tid >> 2) & 63] | (unsigned long long)((2 * tid) & 7);
     const int hi2 = tid >> 8;
     const float2 vfx = make_float2(m.fxf, m.fxf);
     const float fy = m.fyf, fz = m.fzf;
     __syncthreads();
-    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        unsigned long long tb_bits = 0;
-        for (int q = 0; q < p.nrest; q++) tb_bits |= (((unsigned long long)t >> q) & 1ull) << p.rest[q];
-        const unsigned long long base = tb_bits | lo;
-        {
-            const unsigned long long b2 = tb_bits | lo2;
-            float4* t4 = reinterpret_cast<float4*>(tile);
+    auto issue = [&](long long t, float2* dst) {
+        const unsigned long long b2 = tile_bits_of<E>(p, t) | lo2;
 #pragma unroll
-            for (int i = 0; i < E / 2; i++)
-                t4[tid + TILE_THREADS * i] = *reinterpret_cast<const float4*>(in + (b2 | hi_off[hi2 + 2 * i]));
+        for (int i = 0; i < E / 2; i++)
+            cp_async16(dst + 2 * (tid + TILE_THREADS * i), in + (b2 | hi_off[hi2 + 2 * i]));
+        cp_async_commit();
+    };
+    long long t = blockIdx.x;
+    int cur = 0;
+    if (t < ntiles) issue(t, bufs);
+    for (; t < ntiles; t += gridDim.x, cur ^= 1) {
+        float2* tile = bufs + cur * (TILE_THREADS * E);
+        const long long tn = t + gridDim.x;
+        if (tn < ntiles) {
+            issue(tn, bufs + (cur ^ 1) * (TILE_THREADS * E));
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
         __syncthreads();
-        float2 acc[E], G[E];
+        const unsigned long long base = tile_bits_of<E>(p, t) | lo;
+        float2 acc[E], G[E], pre[E];
+        float dpre[E];
 #pragma unroll
-        for (int j = 0; j < E; j++) G[j] = make_float2(0.f, 0.f);
-        if (p.diag) {
-#pragma unroll
-            for (int j = 0; j < E; j++) {
-                const unsigned long long k = base | hi_off[j];
-                const float dg = fmaf(fz, (float)(m.N - 2 * __popcll(k)), diag[k]);
-                const float2 v = tile[tid + TILE_THREADS * j];
-                acc[j] = make_float2(dg * v.x, dg * v.y);
-            }
-        } else if (p.accumulate) {
-#pragma unroll
-            for (int j = 0; j < E; j++) acc[j] = out[base | hi_off[j]];
-        } else {
-#pragma unroll
-            for (int j = 0; j < E; j++) acc[j] = make_float2(0.f, 0.f);
+        for (int j = 0; j < E; j++) {
+            acc[j] = make_float2(0.f, 0.f);
+            G[j] = make_float2(0.f, 0.f);
+            if (p.diag) dpre[j] = diag[base | hi_off[j]];
+            else if (p.accumulate) pre[j] = out[base | hi_off[j]];
         }
         for (int b = 0; b < p.nbond; b++) {
             const unsigned int lm = p.blm[b];
@@ -328,15 +346,120 @@ __global__ void __launch_bounds__(TILE_THREADS) k_hv_pass_f32(const __grid_const
         }
 #pragma unroll
         for (int j = 0; j < E; j++) {
-            // acc += i fy G
+            const unsigned long long k = base | hi_off[j];
             float2 o = acc[j];
-            o.x = fmaf(-fy, G[j].y, o.x);
+            o.x = fmaf(-fy, G[j].y, o.x);      // + i fy G
             o.y = fmaf(fy, G[j].x, o.y);
-            out[base | hi_off[j]] = o;
+            if (p.diag) {
+                const float dg = fmaf(fz, (float)(m.N - 2 * __popcll(k)), dpre[j]);
+                const float2 v = tile[tid + TILE_THREADS * j];
+                o.x = fmaf(dg, v.x, o.x);
+                o.y = fmaf(dg, v.y, o.y);
+            } else if (p.accumulate) {
+                o.x += pre[j].x;
+                o.y += pre[j].y;
+            }
+            out[k] = o;
+        }
+        __syncthreads();   // buffer `cur` is refilled by the next iteration's prefetch
+    }
+}
+
+// FP64 energy sweep: sum over one pass of conj(v[k]) (H_pass v)[k], computed in FP64 from a
+// complex64 or complex128 vector, without writing H v.  The passes of a plan add up to
+// <v|H|v>.  One (re, im) partial per CTA (fixed grid: deterministic).
+template <typename S>
+__global__ void __launch_bounds__(TILE_THREADS) k_energy_pass(const __grid_constant__ DevModel m,
+                                                               const __grid_constant__ DevPass p,
+                                                               const typename V2T<S>::T* __restrict__ in,
+                                                               double* __restrict__ partials, long long ntiles) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double2* tile = reinterpret_cast<double2*>(smem_raw);
+    const int Tn = 1 << p.Tp;
+    const int cm = (1 << p.c) - 1;
+    double er = 0.0, ei = 0.0;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        unsigned long long base = 0;
+        for (int q = 0; q < p.nrest; q++) base |= (((unsigned long long)t >> q) & 1ull) << p.rest[q];
+        for (int e = threadIdx.x; e < Tn; e += blockDim.x) {
+            const int r = e >> p.c;
+            const unsigned long long k = base | p.tabLo[r & 63] | p.tabHi[r >> 6] | (unsigned long long)(e & cm);
+            const typename V2T<S>::T x = in[k];
+            tile[e] = make_double2((double)x.x, (double)x.y);
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < Tn; e += blockDim.x) {
+            const int r = e >> p.c;
+            const unsigned long long k = base | p.tabLo[r & 63] | p.tabHi[r >> 6] | (unsigned long long)(e & cm);
+            const double2 v = tile[e];
+            double ar = 0.0, ai = 0.0;
+            if (p.diag) {
+                double d = 0.0;
+                for (int b = 0; b < m.nd; b++) {
+                    const double q = 0.25 * m.d[b].dz;
+                    d += (__popcll(k & m.d[b].mask) == 1) ? -q : q;
+                }
+                d = __dadd_rn(d, __dmul_rn(m.fz, (double)(m.N - 2 * __popcll(k))));
+                ar = d * v.x;
+                ai = d * v.y;
+            }
+            for (int b = 0; b < p.nbond; b++) {
+                const unsigned int lm = p.blm[b];
+                const double c = (__popc((unsigned)e & lm) == 1) ? p.cdiff[b] : p.ceq[b];
+                const double2 w = tile[e ^ lm];
+                ar = fma(c, w.x, ar);
+                ai = fma(c, w.y, ai);
+            }
+            for (int f = 0; f < p.nfield; f++) {
+                const unsigned int lm = p.flm[f];
+                const double2 w = tile[e ^ lm];
+                const double sfy = ((unsigned)e & lm) ? m.fy : -m.fy;
+                ar = fma(m.fx, w.x, ar); ar = fma(-sfy, w.y, ar);
+                ai = fma(m.fx, w.y, ai); ai = fma(sfy, w.x, ai);
+            }
+            er += v.x * ar + v.y * ai;
+            ei += v.x * ai - v.y * ar;
         }
         __syncthreads();
     }
+    __shared__ double red[2][TILE_THREADS / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        er += __shfl_xor_sync(0xffffffffu, er, o);
+        ei += __shfl_xor_sync(0xffffffffu, ei, o);
+    }
+    if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = er; red[1][threadIdx.x >> 5] = ei; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < TILE_THREADS / 32; w++) { a += red[0][w]; b += red[1][w]; }
+        partials[2 * blockIdx.x] = a;
+        partials[2 * blockIdx.x + 1] = b;
+    }
 }
+
+template <typename S>
+void launch_energy(const DevModel& m, const std::vector<DevPass>& passes, const void* in, int64_t D,
+                   double* partials, int max_blocks, std::vector<double>& host_sum, cudaStream_t s) {
+    typedef typename V2T<S>::T C;
+    host_sum.assign(2, 0.0);
+    for (const DevPass& p : passes) {
+        const size_t smem = (size_t(1) << p.Tp) * sizeof(double2);
+        if (smem > 48 * 1024)
+            ESC_CUDA(cudaFuncSetAttribute(k_energy_pass<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const long long ntiles = (long long)(D >> p.Tp);
+        const int g = (int)std::min<long long>(ntiles, max_blocks);
+        k_energy_pass<S><<<g, TILE_THREADS, smem, s>>>(m, p, (const C*)in, partials, ntiles);
+        ESC_CUDA(cudaGetLastError());
+        std::vector<double> h(2 * (size_t)g);
+        ESC_CUDA(cudaMemcpyAsync(h.data(), partials, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+        ESC_CUDA(cudaStreamSynchronize(s));
+        for (int i = 0; i < g; i++) { host_sum[0] += h[2 * i]; host_sum[1] += h[2 * i + 1]; }
+    }
+}
+template void launch_energy<float>(const DevModel&, const std::vector<DevPass>&, const void*, int64_t, double*, int,
+                                   std::vector<double>&, cudaStream_t);
+template void launch_energy<double>(const DevModel&, const std::vector<DevPass>&, const void*, int64_t, double*, int,
+                                    std::vector<double>&, cudaStream_t);
 
 std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
     const int np = (int)P.tiles.size();
@@ -426,7 +549,7 @@ static void run_fast(const DevModel& m, const DevPass& p, const void* diag, cons
 template <int E>
 static void run_f32(const DevModel& m, const DevPass& p, const void* diag, const void* in, void* out, int64_t D, int sms,
                     cudaStream_t s) {
-    const size_t smem = (size_t)TILE_THREADS * E * sizeof(float2);
+    const size_t smem = 2 * (size_t)TILE_THREADS * E * sizeof(float2);   // double buffer
     if (smem > 48 * 1024)
         ESC_CUDA(cudaFuncSetAttribute(k_hv_pass_f32<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;

@@ -589,6 +589,28 @@ void launch_lincomb(const void* L, int64_t ld, int m, const double* z, void* out
     ESC_CUDA(cudaGetLastError());
 }
 
+template <typename R>
+__global__ void __launch_bounds__(256) k_axpy_dev(const typename V2<R>::T* __restrict__ x, typename V2<R>::T* __restrict__ y,
+                                                  const double* __restrict__ d_coef, long long n) {
+    const R c = (R)d_coef[0];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        typename V2<R>::T a = y[i];
+        const typename V2<R>::T b = x[i];
+        a.x = fma(c, b.x, a.x);
+        a.y = fma(c, b.y, a.y);
+        y[i] = a;
+    }
+}
+template <typename R>
+void launch_axpy_dev(const void* x, void* y, const double* d_coef, int64_t n, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    k_axpy_dev<R><<<grid_for(n, 256, SMS * 16), 256, 0, s>>>((const C*)x, (C*)y, d_coef, n);
+    ESC_CUDA(cudaGetLastError());
+}
+template void launch_axpy_dev<double>(const void*, void*, const double*, int64_t, cudaStream_t);
+template void launch_axpy_dev<float>(const void*, void*, const double*, int64_t, cudaStream_t);
+
 __global__ void k_c128_to_c64(const double2* in, float2* out, long long n) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)

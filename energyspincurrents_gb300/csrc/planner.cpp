@@ -12,6 +12,7 @@
 //   4. assigns every term to the first pass whose tile contains it (the diagonal to pass 1).
 // The relabelled model is the same Hamiltonian; only vectors crossing the C ABI are permuted.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <random>
@@ -118,6 +119,8 @@ Plan make_plan(int N, const std::vector<std::pair<int, int>>& bonds, int T, int 
     P.T = T; P.c = c;
     std::vector<std::vector<int>> adj(N);
     for (auto& b : bonds) { adj[b.first].push_back(b.second); adj[b.second].push_back(b.first); }
+    if (N >= 26) restarts = std::max(restarts, 20000);   // large bases: fewer passes are worth ~3 s here
+    if (const char* e = std::getenv("ESC_PLAN_RESTARTS")) restarts = std::max(1, std::atoi(e));
     std::mt19937_64 rng(0x5eed1234u);
     Cand best;
     size_t best_cost = ~size_t(0);

@@ -137,7 +137,7 @@ esc_status esc_params_from_file(const char* path, esc_params* p, char* errbuf, s
 esc_status esc_lattice(const esc_params* p, int* neigh, int* nsites);
 
 /* Site relabelling and pass count of the tiled H.v for the model in `p` with tiles of 2^tile_bits
- * states (0 = default 13) whose lowest low_bits bits are shared (0 = default 3); host only.
+ * states (0 = default 12) whose lowest low_bits bits are shared (0 = default 3); host only.
  * bit_of_site (N entries, may be NULL), npasses (may be NULL).  No reference counterpart. */
 esc_status esc_plan(const esc_params* p, int tile_bits, int low_bits, int* bit_of_site, int* npasses);
 
@@ -179,6 +179,11 @@ esc_status esc_apply_op(esc_handle* h, int op, int site, const void* in, void* o
 /* Reference start vector (src/DynLanczosSolver.h:57-59, :465-474) or the counter-based normal
  * start vector, normalised, in basis order. */
 esc_status esc_start_vector(esc_handle* h, int kind, int seed, void* out, esc_dtype dt, int flags);
+
+/* E = <v|H|v>/<v|v> evaluated in FP64 from a complex128 or complex64 vector, pass by pass without
+ * forming H v (the FP64 refinement of a mixed-precision ground-state energy).  No reference
+ * counterpart. */
+esc_status esc_rayleigh(esc_handle* h, const void* v, esc_dtype dt, int flags, double* E);
 
 /* ---- solvers ----------------------------------------------------------------------------------- */
 

@@ -246,3 +246,43 @@ def test_tiled_multipass_vs_oracle(tile_bits, shape, monkeypatch):
     assert relerr(h.hv(xi, flags=esc.INTERNAL_ORDER), h.to_internal(ref)) < 1e-14
     # operators go through the same relabelling
     assert relerr(h.apply("JexTotal", 0, x), m.apply("JexTotal", 0, x)) < 1e-14
+
+
+@pytest.mark.parametrize("dt", [np.complex128, np.complex64])
+def test_recompute_mode_matches_stored_basis(dt):
+    """LancType=GS without reorthogonalisation keeps 3 vectors and rebuilds |gs> in a second pass;
+    it must give the ground state of the stored-basis run (same alpha/beta, same Ritz vector)."""
+    h = esc.Handle(kitaev(J=0.1, seed=0, lanczos_steps=80))
+    v0 = O.random_start(0, h.D)
+    a = h.lanczos_gs(start=v0, lanctype="GS", reortho=0, dtype=dt)
+    b = h.lanczos_gs(start=v0, lanctype="All", reortho=0, dtype=dt)
+    assert np.array_equal(a["alpha"], b["alpha"]) and a["E0"] == b["E0"]
+    ga, gb = a["gs"].astype(np.complex128), b["gs"].astype(np.complex128)
+    tol = 1e-12 if dt == np.complex128 else 1e-5
+    assert abs(abs(np.vdot(ga, gb)) / (np.linalg.norm(ga) * np.linalg.norm(gb)) - 1) < tol
+
+
+def test_rayleigh_fp64():
+    p = kitaev(J=0.1)
+    h = esc.Handle(p)
+    m = O.Model("Kitaev", 3, 4, 1, 1, -1.0, -1.0, -1.0, p["Bxx"], p["Byy"], p["Bzz"], 0.1, 4, True)
+    x = O.random_start(9, h.D)
+    ref = np.vdot(x, m.hv(x)).real / np.vdot(x, x).real
+    assert abs(h.rayleigh(x) - ref) < 1e-13
+    x32 = x.astype(np.complex64)
+    x32d = x32.astype(np.complex128)
+    ref32 = np.vdot(x32d, m.hv(x32d)).real / np.vdot(x32d, x32d).real
+    assert abs(h.rayleigh(x32) - ref32) < 1e-12
+
+
+def test_mixed_precision_e0_refined_to_fp64():
+    """complex64 Lanczos (three vectors, recomputed ground state) + FP64 Rayleigh sweep reaches the
+    FP64 ground-state energy to 1e-10 relative."""
+    p = kitaev(J=0.1, seed=0)
+    h = esc.Handle(p)
+    m = O.Model("Kitaev", 3, 4, 1, 1, -1.0, -1.0, -1.0, p["Bxx"], p["Byy"], p["Bzz"], 0.1, 4, True)
+    e_exact = np.linalg.eigvalsh(m.dense())[0]
+    r = h.lanczos_gs(start=O.random_start(0, h.D), steps=150, lanctype="GS", reortho=0, dtype=np.complex64)
+    e_ref = h.rayleigh(r["gs"])
+    assert abs(r["E0"] - e_exact) < 1e-5 * abs(e_exact)          # complex64 recurrence
+    assert abs(e_ref - e_exact) < 1e-10 * abs(e_exact)           # after the FP64 sweep
