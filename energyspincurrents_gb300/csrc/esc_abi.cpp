@@ -54,6 +54,12 @@ struct Fail : std::runtime_error {
     Fail(esc_status s, const std::string& m) : std::runtime_error(m), st(s) {}
 };
 
+}  // namespace
+
+void esc::set_last_error(const std::string& msg) { g_err = msg; }
+
+namespace {
+
 esc_status finish(esc_handle* h, esc_status st, const std::string& msg) {
     g_err = msg;
     if (h) h->err = msg;
@@ -296,7 +302,7 @@ void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) 
     std::vector<double> d(h->alpha), e(n, 0.0);
     for (int i = 0; i < n - 1; i++) e[i] = h->beta[i + 1];
     h->Z.clear();
-    if (!esc::tridiag_eig(n, d, e, store ? &h->Z : nullptr)) throw Fail(ESC_ERR_NUMERIC, "diag: tridiagonal eigensolver failed");
+    if (!esc::tridiag_eig(n, d, e, (store || recompute) ? &h->Z : nullptr)) throw Fail(ESC_ERR_NUMERIC, "diag: tridiagonal eigensolver failed");
     h->ritz = d;
     h->nsteps = n;
     ensure(h->d_gs, h->gs_bytes, (size_t)D * 16);
