@@ -58,6 +58,12 @@ class LanczosCfg(ctypes.Structure):
                 ("reortho", ctypes.c_int), ("dtype", ctypes.c_int)]
 
 
+class CFBatchCfg(ctypes.Structure):
+    _fields_ = [("ncols", ctypes.c_int), ("max_steps", ctypes.c_int), ("steps", ctypes.c_void_p),
+                ("fields", ctypes.c_void_p), ("tol", ctypes.c_double), ("dtype", ctypes.c_int),
+                ("use_graph", ctypes.c_int)]
+
+
 class DynCfg(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("mode", ctypes.c_int), ("omega_steps", ctypes.c_int),
                 ("domega", ctypes.c_double), ("eta", ctypes.c_double), ("cf_steps", ctypes.c_int),
@@ -69,7 +75,7 @@ _lib = None
 # every symbol declared in include/esc.h
 EXPORTS = ["esc_params_default", "esc_params_from_file", "esc_lattice", "esc_plan", "esc_create", "esc_destroy", "esc_last_error",
            "esc_num_sites", "esc_dim", "esc_neighbors", "esc_basis_permutation", "esc_stream", "esc_hv", "esc_hv_batched", "esc_apply_op",
-           "esc_start_vector", "esc_rayleigh", "esc_lanczos_gs", "esc_spectrum", "esc_measure_local", "esc_grad"]
+           "esc_start_vector", "esc_rayleigh", "esc_lanczos_gs", "esc_cf_batched", "esc_spectrum", "esc_measure_local", "esc_grad"]
 
 
 def lib_path():
@@ -107,6 +113,7 @@ def lib():
     L.esc_rayleigh.argtypes = [vp, vp, ci, ci, P(cd)]
     L.esc_lanczos_gs.argtypes = [vp, P(LanczosCfg), vp, ci, P(cd), vp, vp, vp, P(ci), vp]
     L.esc_spectrum.argtypes = [vp, P(DynCfg), vp, P(ci), P(ci)]
+    L.esc_cf_batched.argtypes = [vp, P(CFBatchCfg), vp, i64, ci, vp, vp, vp]
     L.esc_measure_local.argtypes = [vp, vp, vp]
     L.esc_grad.argtypes = [vp, P(DynCfg), vp, vp]
     _lib = L
@@ -293,6 +300,19 @@ class Handle:
         E = ctypes.c_double()
         _check(self.h, lib().esc_rayleigh(self.h, _ptr(v), _dt(v), flags, ctypes.byref(E)))
         return E.value
+
+    def cf_batched(self, starts, max_steps, steps=None, fields=None, tol=1e-10, use_graph=True, flags=0):
+        """Batched continued-fraction Lanczos; starts (ncols, D).  Returns [(a, b)] per column."""
+        V = np.ascontiguousarray(starts)
+        nc = V.shape[0]
+        st = None if steps is None else np.ascontiguousarray(steps, dtype=np.int32)
+        fl = None if fields is None else np.ascontiguousarray(fields, dtype=np.float64)
+        cfg = CFBatchCfg(nc, max_steps, _ptr(st).value if st is not None else None,
+                         _ptr(fl).value if fl is not None else None, tol, _dt(V), 1 if use_graph else 0)
+        a = np.zeros((nc, max_steps)); b = np.zeros((nc, max_steps + 1)); lens = np.zeros(nc, dtype=np.int32)
+        _check(self.h, lib().esc_cf_batched(self.h, ctypes.byref(cfg), _ptr(V), V.shape[1], flags, _ptr(a), _ptr(b),
+                                            _ptr(lens)))
+        return [(a[c, : lens[c]], b[c, : lens[c] + 1]) for c in range(nc)]
 
     def spectrum(self, kind, mode="Ritz", omega_steps=None, domega=None, eta=None, cf_steps=0):
         p = self.params.p

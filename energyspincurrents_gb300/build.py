@@ -23,8 +23,8 @@ LIB = os.path.join(OUT, "libesc.so")
 EXE = os.path.join(OUT, "LanczosCond")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kernels.cu", "hv_tiled.cu"]
-CPP_SOURCES = ["esc_abi.cpp", "params.cpp", "model.cpp", "numerics.cpp", "planner.cpp", "batched.cpp"]
+CU_SOURCES = ["kernels.cu", "hv_tiled.cu", "batched.cu"]
+CPP_SOURCES = ["esc_abi.cpp", "params.cpp", "model.cpp", "numerics.cpp", "planner.cpp"]
 
 
 def _nvcc():

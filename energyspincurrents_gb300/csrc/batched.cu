@@ -1,0 +1,275 @@
+// batched.cu -- batched continued-fraction Lanczos: independent three-term recurrences on up to
+// 16 columns (each column its own start vector and its own field), run in lockstep with all
+// recurrence state on the device so that one iteration can be captured in a CUDA graph and
+// replayed.  A column stops when beta_k < tol * |phi| or at its own step limit; stopped columns
+// skip their work (every kernel checks the column's flag).
+//
+// Buffers: three sets V[0..2] of ncols vectors (stride D).  At iteration it the roles are
+// prev = V[it % 3], cur = V[(it + 1) % 3], w = V[(it + 2) % 3]; a graph holds three unrolled
+// iterations (one per rotation), so every kernel parameter is fixed and the iteration counter is
+// read from device memory.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "esc_internal.h"
+
+namespace esc {
+
+template <typename R> struct V2B;
+template <> struct V2B<double> { typedef double2 T; };
+template <> struct V2B<float> { typedef float2 T; };
+
+__device__ __forceinline__ void bff_add(float& hi, float& lo, float x) {
+    const float s = hi + x;
+    const float bp = s - hi;
+    lo += (hi - (s - bp)) + (x - bp);
+    hi = s;
+}
+__device__ __forceinline__ void bff_addprod(float& hi, float& lo, float a, float b) {
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    bff_add(hi, lo, p);
+    lo += e;
+}
+
+static constexpr int BTPB = 256;
+static constexpr int BGRID = 304;   // blocks per column for the reductions (2 x 152 SMs)
+
+__device__ __forceinline__ void block_sum2(double& a, double& b, double* dst) {
+    __shared__ double sm[2][BTPB / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) { sm[0][threadIdx.x >> 5] = a; sm[1][threadIdx.x >> 5] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double x = 0.0, y = 0.0;
+        for (int w = 0; w < BTPB / 32; w++) { x += sm[0][w]; y += sm[1][w]; }
+        dst[0] = x;
+        dst[1] = y;
+    }
+    __syncthreads();
+}
+
+// alpha partials: blockIdx.y = column; partial (re, im) of <cur|w>
+template <typename R>
+__global__ void __launch_bounds__(BTPB) kb_dot(const typename V2B<R>::T* __restrict__ cur,
+                                               const typename V2B<R>::T* __restrict__ w, long long D,
+                                               const int* __restrict__ active, double* __restrict__ part) {
+    const int c = blockIdx.y;
+    if (!active[c]) return;
+    const typename V2B<R>::T* x = cur + (size_t)c * D;
+    const typename V2B<R>::T* y = w + (size_t)c * D;
+    double re = 0.0, im = 0.0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    if constexpr (sizeof(R) == 4) {
+        float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) {
+            const float2 a = x[i], b = y[i];
+            bff_addprod(rh, rl, a.x, b.x); bff_addprod(rh, rl, a.y, b.y);
+            bff_addprod(ih, il, a.x, b.y); bff_addprod(ih, il, -a.y, b.x);
+        }
+        re = (double)rh + (double)rl;
+        im = (double)ih + (double)il;
+    } else {
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) {
+            const double2 a = x[i], b = y[i];
+            re += a.x * b.x + a.y * b.y;
+            im += a.x * b.y - a.y * b.x;
+        }
+    }
+    block_sum2(re, im, part + ((size_t)c * gridDim.x + blockIdx.x) * 2);
+}
+
+// alpha_c[it] = sum of partials (one block per column)
+__global__ void __launch_bounds__(BTPB) kb_alpha(const double* __restrict__ part, int G, const int* __restrict__ it_p,
+                                                 const int* __restrict__ active, double* __restrict__ alpha, int kmax) {
+    const int c = blockIdx.x;
+    if (!active[c]) return;
+    double re = 0.0, im = 0.0;
+    for (int i = threadIdx.x; i < G; i += blockDim.x) {
+        re += part[((size_t)c * G + i) * 2];
+        im += part[((size_t)c * G + i) * 2 + 1];
+    }
+    __shared__ double out[2];
+    block_sum2(re, im, out);
+    if (threadIdx.x == 0) {
+        const int it = *it_p;
+        alpha[((size_t)c * kmax + it) * 2] = out[0];
+        alpha[((size_t)c * kmax + it) * 2 + 1] = out[1];
+    }
+}
+
+// w -= alpha cur + beta prev (beta = sqrt(b2[it]), none at it = 0); |w|^2 partials
+template <typename R>
+__global__ void __launch_bounds__(BTPB) kb_update(typename V2B<R>::T* __restrict__ w,
+                                                  const typename V2B<R>::T* __restrict__ cur,
+                                                  const typename V2B<R>::T* __restrict__ prev, long long D,
+                                                  const int* __restrict__ it_p, const int* __restrict__ active,
+                                                  const double* __restrict__ alpha, const double* __restrict__ b2,
+                                                  int kmax, double* __restrict__ part) {
+    const int c = blockIdx.y;
+    if (!active[c]) return;
+    const int it = *it_p;
+    const R ar = (R)alpha[((size_t)c * kmax + it) * 2], ai = (R)alpha[((size_t)c * kmax + it) * 2 + 1];
+    const R be = it > 0 ? (R)sqrt(b2[(size_t)c * (kmax + 1) + it]) : (R)0;
+    typename V2B<R>::T* W = w + (size_t)c * D;
+    const typename V2B<R>::T* X = cur + (size_t)c * D;
+    const typename V2B<R>::T* P = prev + (size_t)c * D;
+    double acc = 0.0, dummy = 0.0;
+    float hh = 0.f, ll = 0.f;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) {
+        typename V2B<R>::T a = W[i];
+        const typename V2B<R>::T x = X[i];
+        a.x = a.x - (ar * x.x - ai * x.y);
+        a.y = a.y - (ar * x.y + ai * x.x);
+        if (it > 0) {
+            const typename V2B<R>::T p = P[i];
+            a.x = a.x - be * p.x;
+            a.y = a.y - be * p.y;
+        }
+        W[i] = a;
+        if constexpr (sizeof(R) == 4) { bff_addprod(hh, ll, a.x, a.x); bff_addprod(hh, ll, a.y, a.y); }
+        else acc += (double)a.x * a.x + (double)a.y * a.y;
+    }
+    if constexpr (sizeof(R) == 4) acc = (double)hh + (double)ll;
+    block_sum2(acc, dummy, part + ((size_t)c * gridDim.x + blockIdx.x) * 2);
+}
+
+// b2_c[it+1] = |w|^2; stop test; iteration counter advanced by block 0 after all columns
+__global__ void __launch_bounds__(BTPB) kb_beta(const double* __restrict__ part, int G, const int* __restrict__ it_p,
+                                                int* __restrict__ active, double* __restrict__ b2, int kmax,
+                                                const int* __restrict__ steps, double tol) {
+    const int c = blockIdx.x;
+    if (!active[c]) return;
+    double s = 0.0, dummy = 0.0;
+    for (int i = threadIdx.x; i < G; i += blockDim.x) s += part[((size_t)c * G + i) * 2];
+    __shared__ double out[2];
+    block_sum2(s, dummy, out);
+    if (threadIdx.x == 0) {
+        const int it = *it_p;
+        b2[(size_t)c * (kmax + 1) + it + 1] = out[0];
+        const double b0 = sqrt(b2[(size_t)c * (kmax + 1)]);
+        if (!(sqrt(out[0]) > tol * b0) || it + 1 >= steps[c]) active[c] = 0;
+    }
+}
+
+// w /= beta (columns still active, and the column that just stopped: harmless)
+template <typename R>
+__global__ void __launch_bounds__(BTPB) kb_scale(typename V2B<R>::T* __restrict__ w, long long D,
+                                                 const int* __restrict__ it_p, const int* __restrict__ active,
+                                                 const double* __restrict__ b2, int kmax) {
+    const int c = blockIdx.y;
+    if (!active[c]) return;
+    const int it = *it_p;
+    const double nb = sqrt(b2[(size_t)c * (kmax + 1) + it + 1]);
+    const R inv = (R)(nb > 0.0 ? 1.0 / nb : 0.0);
+    typename V2B<R>::T* W = w + (size_t)c * D;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) {
+        typename V2B<R>::T a = W[i];
+        a.x *= inv;
+        a.y *= inv;
+        W[i] = a;
+    }
+}
+
+__global__ void kb_advance(int* it_p) { *it_p += 1; }
+
+// |phi_c|^2 -> b2[c][0]; cur_c /= |phi_c|
+template <typename R>
+__global__ void __launch_bounds__(BTPB) kb_norm0(const typename V2B<R>::T* __restrict__ v, long long D,
+                                                 double* __restrict__ part) {
+    const int c = blockIdx.y;
+    const typename V2B<R>::T* X = v + (size_t)c * D;
+    double acc = 0.0, dummy = 0.0;
+    float hh = 0.f, ll = 0.f;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) {
+        const typename V2B<R>::T a = X[i];
+        if constexpr (sizeof(R) == 4) { bff_addprod(hh, ll, a.x, a.x); bff_addprod(hh, ll, a.y, a.y); }
+        else acc += (double)a.x * a.x + (double)a.y * a.y;
+    }
+    if constexpr (sizeof(R) == 4) acc = (double)hh + (double)ll;
+    block_sum2(acc, dummy, part + ((size_t)c * gridDim.x + blockIdx.x) * 2);
+}
+__global__ void __launch_bounds__(BTPB) kb_norm0_final(const double* __restrict__ part, int G, double* __restrict__ b2,
+                                                       int kmax, int* __restrict__ active) {
+    const int c = blockIdx.x;
+    double s = 0.0, dummy = 0.0;
+    for (int i = threadIdx.x; i < G; i += blockDim.x) s += part[((size_t)c * G + i) * 2];
+    __shared__ double out[2];
+    block_sum2(s, dummy, out);
+    if (threadIdx.x == 0) {
+        b2[(size_t)c * (kmax + 1)] = out[0];
+        active[c] = out[0] > 0.0 ? 1 : 0;
+    }
+}
+template <typename R>
+__global__ void __launch_bounds__(BTPB) kb_scale0(typename V2B<R>::T* __restrict__ w, long long D,
+                                                  const double* __restrict__ b2, int kmax) {
+    const int c = blockIdx.y;
+    const double nb = sqrt(b2[(size_t)c * (kmax + 1)]);
+    const R inv = (R)(nb > 0.0 ? 1.0 / nb : 0.0);
+    typename V2B<R>::T* W = w + (size_t)c * D;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) {
+        typename V2B<R>::T a = W[i];
+        a.x *= inv;
+        a.y *= inv;
+        W[i] = a;
+    }
+}
+
+template <typename R>
+void CFBatch<R>::run(cudaStream_t s) {
+    typedef typename V2B<R>::T C;
+    const size_t vs = (size_t)ncols * D;
+    C* V[3] = {(C*)bufs, (C*)bufs + vs, (C*)bufs + 2 * vs};
+    const dim3 gcol(BGRID, ncols);
+    // start: cur = V[1] holds phi
+    ESC_CUDA(cudaMemsetAsync(d_it, 0, sizeof(int), s));
+    kb_norm0<R><<<gcol, BTPB, 0, s>>>(V[1], D, d_part);
+    kb_norm0_final<<<ncols, BTPB, 0, s>>>(d_part, BGRID, d_b2, kmax, d_active);
+    kb_scale0<R><<<gcol, BTPB, 0, s>>>(V[1], D, d_b2, kmax);
+    ESC_CUDA(cudaGetLastError());
+    auto iteration = [&](int r) {
+        C* prev = V[r % 3];
+        C* cur = V[(r + 1) % 3];
+        C* w = V[(r + 2) % 3];
+        for (int c = 0; c < ncols; c++) hv_column(c, cur + (size_t)c * D, w + (size_t)c * D, d_active + c, s);
+        kb_dot<R><<<gcol, BTPB, 0, s>>>(cur, w, D, d_active, d_part);
+        kb_alpha<<<ncols, BTPB, 0, s>>>(d_part, BGRID, d_it, d_active, d_alpha, kmax);
+        kb_update<R><<<gcol, BTPB, 0, s>>>(w, cur, prev, D, d_it, d_active, d_alpha, d_b2, kmax, d_part);
+        kb_beta<<<ncols, BTPB, 0, s>>>(d_part, BGRID, d_it, d_active, d_b2, kmax, d_steps, tol);
+        kb_scale<R><<<gcol, BTPB, 0, s>>>(w, D, d_it, d_active, d_b2, kmax);
+        kb_advance<<<1, 1, 0, s>>>(d_it);
+        ESC_CUDA(cudaGetLastError());
+    };
+    const int rounds = (kmax + 2) / 3;
+    if (use_graph) {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        ESC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        for (int r = 0; r < 3; r++) iteration(r);
+        ESC_CUDA(cudaStreamEndCapture(s, &g));
+        ESC_CUDA(cudaGraphInstantiate(&ge, g, 0));
+        for (int q = 0; q < rounds; q++) ESC_CUDA(cudaGraphLaunch(ge, s));
+        ESC_CUDA(cudaStreamSynchronize(s));
+        cudaGraphExecDestroy(ge);
+        cudaGraphDestroy(g);
+    } else {
+        for (int q = 0; q < rounds; q++)
+            for (int r = 0; r < 3; r++) iteration(r);
+        ESC_CUDA(cudaStreamSynchronize(s));
+    }
+}
+
+template struct CFBatch<float>;
+template struct CFBatch<double>;
+
+}  // namespace esc

@@ -35,6 +35,9 @@ struct esc_handle {
     void* d_work = nullptr; size_t work_bytes = 0;     // work vectors
     void* d_gs = nullptr; size_t gs_bytes = 0;         // ground state
     void* d_io = nullptr; size_t io_bytes = 0;         // staging for host-pointer calls
+    void* d_cfb = nullptr; size_t cfb_bytes = 0;       // batched CF vectors (3 x ncols x D)
+    double* d_cfs = nullptr; size_t cfs_bytes = 0;     // batched CF scalars
+    int* d_cfi = nullptr; size_t cfi_bytes = 0;        // batched CF flags / counters
     void* d_diag[2] = {nullptr, nullptr};              // diagonal of the bond terms per dtype
     size_t diag_bytes[2] = {0, 0};
     // ground-state Lanczos results
@@ -335,6 +338,68 @@ void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) 
 }
 
 // ---------------------------------------------------------------------------------------------
+// Batched continued-fraction Lanczos (batched.cu)
+// ---------------------------------------------------------------------------------------------
+int cf_batch_width(esc_handle* h, size_t es, int want) {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { (void)cudaGetLastError(); fr = 0; }
+    const size_t per = 3 * (size_t)h->D * es;
+    const size_t have = fr + h->cfb_bytes;
+    int w = (int)std::min<size_t>((size_t)want, have > (size_t)1 << 30 ? (have - ((size_t)1 << 30)) / per : 0);
+    return std::max(1, std::min(w, esc::MAX_COLS));
+}
+
+// Start vectors must already be in column slots of set 1 of d_cfb.  Returns a (Re alpha),
+// b (b[0] = |phi|) and the number of steps per column.
+template <typename R>
+void cf_batch_run(esc_handle* h, int ncols, int kmax, const std::vector<int>& steps, const std::vector<esc::DevModel>& ms,
+                  double tol, bool graph, std::vector<std::vector<double>>& A, std::vector<std::vector<double>>& B) {
+    esc::CFBatch<R> cb;
+    cb.ncols = ncols; cb.kmax = kmax; cb.D = h->D; cb.tol = tol; cb.use_graph = graph;
+    cb.bufs = h->d_cfb;
+    const size_t nd = (size_t)ncols * esc::CFB_GRID * 2 + (size_t)ncols * kmax * 2 + (size_t)ncols * (kmax + 1);
+    ensure_t(h->d_cfs, h->cfs_bytes, nd * sizeof(double));
+    ensure_t(h->d_cfi, h->cfi_bytes, (2 * (size_t)ncols + 2) * sizeof(int));
+    cb.d_part = h->d_cfs;
+    cb.d_alpha = cb.d_part + (size_t)ncols * esc::CFB_GRID * 2;
+    cb.d_b2 = cb.d_alpha + (size_t)ncols * kmax * 2;
+    cb.d_active = h->d_cfi;
+    cb.d_steps = h->d_cfi + ncols;
+    cb.d_it = h->d_cfi + 2 * ncols;
+    ESC_CUDA(cudaMemsetAsync(h->d_cfs, 0, nd * sizeof(double), h->stream));
+    ESC_CUDA(cudaMemcpyAsync(cb.d_steps, steps.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    const void* dg = diag_for(h, sizeof(R) == 4 ? ESC_C64 : ESC_C128);
+    cb.hv_column = [&](int c, const void* in, void* out, const int* active, cudaStream_t s) {
+        esc::launch_hv_tiled<R>(ms[c], h->passes, in, out, h->D, dg, s, active);
+    };
+    cb.run(h->stream);
+    std::vector<double> al((size_t)ncols * kmax * 2), b2((size_t)ncols * (kmax + 1));
+    ESC_CUDA(cudaMemcpyAsync(al.data(), cb.d_alpha, al.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    ESC_CUDA(cudaMemcpyAsync(b2.data(), cb.d_b2, b2.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    sync(h);
+    A.assign(ncols, {});
+    B.assign(ncols, {});
+    for (int c = 0; c < ncols; c++) {
+        const double b0 = std::sqrt(b2[(size_t)c * (kmax + 1)]);
+        B[c].push_back(b0);
+        if (b0 == 0.0) continue;
+        for (int k = 0; k < kmax; k++) {
+            A[c].push_back(al[((size_t)c * kmax + k) * 2]);
+            const double bn = std::sqrt(b2[(size_t)c * (kmax + 1) + k + 1]);
+            B[c].push_back(bn);
+            if (k + 1 >= steps[c] || !(bn > tol * b0)) break;
+        }
+    }
+}
+
+esc::DevModel model_with_field(const esc_handle* h, double bx, double by, double bz) {
+    esc::DevModel m = h->dm;
+    m.fx = 0.5 * bx; m.fy = 0.5 * by; m.fz = 0.5 * bz;
+    esc::fill_float_copies(m);
+    return m;
+}
+
+// ---------------------------------------------------------------------------------------------
 // Spectra
 // ---------------------------------------------------------------------------------------------
 struct Grid {
@@ -488,7 +553,8 @@ esc_status esc_create(const esc_params* p, esc_handle** out) {
 
 esc_status esc_destroy(esc_handle* h) {
     if (!h) return ESC_OK;
-    for (void* p : {(void*)h->d_part, (void*)h->d_sc, h->d_L, h->d_work, h->d_gs, h->d_io, h->d_diag[0], h->d_diag[1]})
+    for (void* p : {(void*)h->d_part, (void*)h->d_sc, h->d_L, h->d_work, h->d_gs, h->d_io, h->d_diag[0], h->d_diag[1],
+                    h->d_cfb, (void*)h->d_cfs, (void*)h->d_cfi})
         if (p) cudaFree(p);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -663,14 +729,31 @@ void spectrum_impl(esc_handle* h, const esc_dyn_cfg& cfg, std::vector<double>& o
     auto T = [&](int op, int site) { return esc::operator_terms(op, site, h->p, h->L); };
     auto omega = [&](int k) { return cfg.domega * k; };
 
-    // CF resolvent G_A(omega) = <A gs|(z-H)^-1|A gs>, z = omega + E0 - i eta
-    auto cf_run = [&](const std::vector<esc::OpTerm>& t) {
-        std::vector<double> a, b;
-        S.cf_coeffs(t, K, d_cf, a, b);
-        std::vector<cplx> g(nw);
-        for (int k = 0; k < nw; k++) g[k] = esc::cf_eval(a.data(), b.data(), (int)a.size(), cplx(omega(k) + Eg, -eta));
-        return g;
+    // CF resolvents G_A(omega) = <A gs|(z-H)^-1|A gs>, z = omega + E0 - i eta, for a list of
+    // operators, run as columns of the batched CF Lanczos (batched.cu)
+    auto cf_runs = [&](const std::vector<std::vector<esc::OpTerm>>& ts) {
+        std::vector<std::vector<cplx>> G(ts.size());
+        const int width = cf_batch_width(h, Pipe<R>::ES, (int)ts.size());
+        ensure(h->d_cfb, h->cfb_bytes, std::max(h->cfb_bytes, 3 * (size_t)width * D * Pipe<R>::ES));
+        for (size_t r0 = 0; r0 < ts.size(); r0 += width) {
+            const int nc = (int)std::min<size_t>(width, ts.size() - r0);
+            char* set1 = (char*)h->d_cfb + (size_t)nc * D * Pipe<R>::ES;
+            for (int c = 0; c < nc; c++)
+                S.P.apply(esc::make_dev_op(ts[r0 + c], &h->plan.perm), h->d_gs, set1 + (size_t)c * D * Pipe<R>::ES);
+            std::vector<int> steps(nc, K);
+            std::vector<esc::DevModel> ms(nc, h->dm);
+            std::vector<std::vector<double>> A, B;
+            cf_batch_run<R>(h, nc, K, steps, ms, 1e-10, true, A, B);
+            for (int c = 0; c < nc; c++) {
+                std::vector<cplx> g(nw);
+                for (int k = 0; k < nw; k++)
+                    g[k] = esc::cf_eval(A[c].data(), B[c].data(), (int)A[c].size(), cplx(omega(k) + Eg, -eta));
+                G[r0 + c] = g;
+            }
+        }
+        return G;
     };
+    auto cf_run = [&](const std::vector<esc::OpTerm>& t) { return cf_runs({t})[0]; };
 
     if (cfg.kind == ESC_DYN_JEJE || cfg.kind == ESC_DYN_JSJS) {
         const bool je = cfg.kind == ESC_DYN_JEJE;
@@ -707,14 +790,21 @@ void spectrum_impl(esc_handle* h, const esc_dyn_cfg& cfg, std::vector<double>& o
                     }
             }
         } else {
+            std::vector<std::vector<esc::OpTerm>> runs;
             for (int c = 0; c < nc; c++) {
                 el[c] = S.expect(ch[c], 0, d_tmp);
-                Sab[c][c] = cf_run(ch[c]);
+                runs.push_back(ch[c]);
             }
             for (auto pr : pairs) {
-                const int a = pr.first, b = pr.second;
-                auto Sp = cf_run(combine(ch[a], ch[b], 1.0));
-                auto Sq = cf_run(combine(ch[a], ch[b], cplx(0, 1)));
+                runs.push_back(combine(ch[pr.first], ch[pr.second], 1.0));
+                runs.push_back(combine(ch[pr.first], ch[pr.second], cplx(0, 1)));
+            }
+            auto G = cf_runs(runs);
+            for (int c = 0; c < nc; c++) Sab[c][c] = G[c];
+            for (size_t q = 0; q < pairs.size(); q++) {
+                const int a = pairs[q].first, b = pairs[q].second;
+                const auto& Sp = G[nc + 2 * q];
+                const auto& Sq = G[nc + 2 * q + 1];
                 for (int k = 0; k < nw; k++) {
                     const cplx X = Sp[k] - Sab[a][a][k] - Sab[b][b][k];
                     const cplx Y = Sq[k] - Sab[a][a][k] - Sab[b][b][k];
@@ -778,16 +868,22 @@ void spectrum_impl(esc_handle* h, const esc_dyn_cfg& cfg, std::vector<double>& o
                     R9[q][k] = s;
                 }
         } else {
-            std::vector<std::vector<cplx>> G(6);
+            std::vector<std::vector<esc::OpTerm>> runs;
             for (int c = 0; c < 6; c++) {
                 el[c] = S.expect(ch[c], 0, d_tmp);
-                if (c == 0 || c == 1 || c == 2 || c == 3 || c == 4 || c == 5) G[c] = cf_run(ch[c]);
+                runs.push_back(ch[c]);
             }
-            R9[0] = G[0]; R9[1] = G[1]; R9[2] = G[2]; R9[6] = G[3]; R9[7] = G[4]; R9[8] = G[5];
             const int pp[3][3] = {{0, 1, 3}, {0, 2, 4}, {1, 2, 5}};
             for (auto& q : pp) {
-                auto Sp = cf_run(combine(ch[q[0]], ch[q[1]], 1.0));
-                auto Sq = cf_run(combine(ch[q[0]], ch[q[1]], cplx(0, 1)));
+                runs.push_back(combine(ch[q[0]], ch[q[1]], 1.0));
+                runs.push_back(combine(ch[q[0]], ch[q[1]], cplx(0, 1)));
+            }
+            auto G = cf_runs(runs);   // 12 columns per site
+            R9[0] = G[0]; R9[1] = G[1]; R9[2] = G[2]; R9[6] = G[3]; R9[7] = G[4]; R9[8] = G[5];
+            for (int qi = 0; qi < 3; qi++) {
+                const auto& q = pp[qi];
+                const auto& Sp = G[6 + 2 * qi];
+                const auto& Sq = G[7 + 2 * qi];
                 for (int k = 0; k < nw; k++) {
                     const cplx X = Sp[k] - G[q[0]][k] - G[q[1]][k];
                     const cplx Y = Sq[k] - G[q[0]][k] - G[q[1]][k];
@@ -951,5 +1047,48 @@ extern "C" esc_status esc_rayleigh(esc_handle* h, const void* v, esc_dtype dt, i
         ESC_CUDA(cudaMemcpyAsync(nn, h->d_sc, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
         sync(h);
         *E = num[0] / nn[0];
+    });
+}
+
+extern "C" esc_status esc_cf_batched(esc_handle* h, const esc_cf_batch_cfg* cfg, const void* starts, int64_t ld,
+                                     int flags, double* a, double* b, int* lens) {
+    if (!h || !cfg || !starts) return finish(h, ESC_ERR_PARAM, "null argument");
+    if (cfg->ncols < 1 || cfg->ncols > esc::MAX_COLS) return finish(h, ESC_ERR_PARAM, "ncols must be 1..16");
+    if (cfg->max_steps < 1) return finish(h, ESC_ERR_PARAM, "max_steps must be >= 1");
+    if (ld < h->D) return finish(h, ESC_ERR_PARAM, "ld must be >= 2^N");
+    return guarded(h, [&]() {
+        const int nc = cfg->ncols, K = cfg->max_steps;
+        const esc_dtype dt = cfg->dtype;
+        const size_t es = esize(dt), vb = (size_t)h->D * es;
+        ensure(h->d_cfb, h->cfb_bytes, std::max(h->cfb_bytes, 3 * (size_t)nc * vb));
+        char* set1 = (char*)h->d_cfb + (size_t)nc * vb;
+        for (int c = 0; c < nc; c++) {
+            const char* src = (const char*)starts + (size_t)c * ld * es;
+            const bool dev = flags & ESC_DEVICE_PTR, internal = flags & ESC_INTERNAL_ORDER;
+            if (internal) {
+                ESC_CUDA(cudaMemcpyAsync(set1 + c * vb, src, vb, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+            } else if (dev) {
+                permute(h, h->to_int, src, set1 + c * vb, h->D, dt);
+            } else {
+                ensure(h->d_io, h->io_bytes, std::max(h->io_bytes, vb));
+                ESC_CUDA(cudaMemcpyAsync(h->d_io, src, vb, cudaMemcpyHostToDevice, h->stream));
+                permute(h, h->to_int, h->d_io, set1 + c * vb, h->D, dt);
+            }
+        }
+        std::vector<int> steps(nc, K);
+        if (cfg->steps)
+            for (int c = 0; c < nc; c++) steps[c] = std::max(1, std::min(K, cfg->steps[c]));
+        std::vector<esc::DevModel> ms(nc, h->dm);
+        if (cfg->fields)
+            for (int c = 0; c < nc; c++) ms[c] = model_with_field(h, cfg->fields[3 * c], cfg->fields[3 * c + 1], cfg->fields[3 * c + 2]);
+        const double tol = cfg->tol > 0 ? cfg->tol : 1e-10;
+        std::vector<std::vector<double>> A, B;
+        if (dt == ESC_C64) cf_batch_run<float>(h, nc, K, steps, ms, tol, cfg->use_graph != 0, A, B);
+        else cf_batch_run<double>(h, nc, K, steps, ms, tol, cfg->use_graph != 0, A, B);
+        for (int c = 0; c < nc; c++) {
+            if (lens) lens[c] = (int)A[c].size();
+            if (a) for (size_t k = 0; k < A[c].size(); k++) a[(size_t)c * K + k] = A[c][k];
+            if (b) for (size_t k = 0; k < B[c].size(); k++) b[(size_t)c * (K + 1) + k] = B[c][k];
+        }
     });
 }

@@ -4,6 +4,7 @@
 
 #include <complex>
 #include <cstdint>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -102,6 +103,8 @@ struct Plan {
     std::vector<std::vector<int>> tiles;   // per pass: sorted tile bit positions (include [0,c))
 };
 Plan make_plan(int N, const std::vector<std::pair<int, int>>& bonds, int T, int c, int restarts);
+// Same covering with no relabelling: the shared sites are 0..c-1 and tiles are sets of reference bits.
+Plan make_plan_reference_order(int N, const std::vector<std::pair<int, int>>& bonds, int T, int c, int restarts);
 
 constexpr int MAX_PTERMS = 96;
 struct DevPass {
@@ -121,8 +124,10 @@ struct DevPass {
 std::vector<DevPass> make_passes(const Plan& P, const DevModel& m);
 // diag: precomputed diagonal of the bond terms (no field), R per state (launch_diag); may be NULL,
 // then the diagonal is computed in the kernel.
+// active (optional, device int): the launches do nothing when *active == 0 (batched recurrences).
 template <typename R> void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in,
-                                           void* out, int64_t D, const void* diag, cudaStream_t s);
+                                           void* out, int64_t D, const void* diag, cudaStream_t s,
+                                           const int* active = nullptr);
 template <typename R> void launch_diag(const DevModel& m, void* diag, int64_t D, cudaStream_t s);
 // host_sum = <v|H|v> (re, im) computed in FP64 pass by pass; S = storage precision of v.
 template <typename S> void launch_energy(const DevModel& m, const std::vector<DevPass>& passes, const void* in,
@@ -189,6 +194,26 @@ void launch_convert_c128_to_c64(const void* in, void* out, int64_t n, cudaStream
 void launch_convert_c64_to_c128(const void* in, void* out, int64_t n, cudaStream_t s);
 template <typename R> void launch_start_normal(uint64_t seed, void* out, int64_t n, cudaStream_t s);
 
+// Batched continued-fraction Lanczos (batched.cu).  Caller fills the pointers (device memory) and
+// the per-column H.v callback; run() executes kmax iterations (CUDA graph if use_graph).
+template <typename R>
+struct CFBatch {
+    int ncols = 0, kmax = 0;
+    int64_t D = 0;
+    double tol = 1e-10;
+    bool use_graph = true;
+    void* bufs = nullptr;        // 3 sets of ncols vectors; set 1 holds the start vectors on entry
+    double* d_part = nullptr;    // ncols * 304 * 2 doubles
+    double* d_alpha = nullptr;   // ncols * kmax * 2
+    double* d_b2 = nullptr;      // ncols * (kmax + 1); [c][0] = |phi_c|^2
+    int* d_active = nullptr;     // ncols
+    int* d_it = nullptr;         // 1
+    int* d_steps = nullptr;      // ncols (per-column step limit <= kmax)
+    std::function<void(int, const void*, void*, const int*, cudaStream_t)> hv_column;
+    void run(cudaStream_t s);
+};
+constexpr int CFB_GRID = 304;
+
 // ---------------------------------------------------------------------------------------------
 // Host numerics
 // ---------------------------------------------------------------------------------------------
@@ -201,6 +226,9 @@ cplx cf_eval(const double* a, const double* b, int n, cplx z);
 
 // Reference start vector: mt19937_64(seed), generate_canonical<double,53> draws, re then im.
 void ref_uniform_start(int seed, int64_t D, cplx* out);
+
+// Sets the message that esc_last_error(NULL) returns on this thread.
+void set_last_error(const std::string& msg);
 
 struct CudaError : std::runtime_error {
     using std::runtime_error::runtime_error;

@@ -26,8 +26,9 @@ __global__ void __launch_bounds__(TILE_THREADS) k_hv_pass(const __grid_constant_
                                                            const __grid_constant__ DevPass p,
                                                            const typename V2T<R>::T* __restrict__ in,
                                                            typename V2T<R>::T* __restrict__ out,
-                                                           long long ntiles) {
+                                                           long long ntiles, const int* __restrict__ active) {
     typedef typename V2T<R>::T C;
+    if (active && *active == 0) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* tile = reinterpret_cast<C*>(smem_raw);
     const int Tn = 1 << p.Tp;
@@ -135,8 +136,9 @@ __global__ void __launch_bounds__(TILE_THREADS) k_hv_pass_fast(const __grid_cons
                                                                 const R* __restrict__ diag,
                                                                 const typename V2T<R>::T* __restrict__ in,
                                                                 typename V2T<R>::T* __restrict__ out,
-                                                                long long ntiles) {
+                                                                long long ntiles, const int* __restrict__ active) {
     typedef typename V2T<R>::T C;
+    if (active && *active == 0) return;
     constexpr bool F32 = sizeof(R) == 4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* tile = reinterpret_cast<C*>(smem_raw);
@@ -288,7 +290,9 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) k_hv_pass_f32(const __grid_co
                                                                const __grid_constant__ DevPass p,
                                                                const float* __restrict__ diag,
                                                                const float2* __restrict__ in,
-                                                               float2* __restrict__ out, long long ntiles) {
+                                                               float2* __restrict__ out, long long ntiles,
+                                                               const int* __restrict__ active) {
+    if (active && *active == 0) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* bufs = reinterpret_cast<float2*>(smem_raw);   // 2 x (512 E) states
     __shared__ unsigned long long hi_off[E];
@@ -533,7 +537,7 @@ void launch_diag(const DevModel& m, void* diag, int64_t D, cudaStream_t s) {
 
 template <typename R, int E>
 static void run_fast(const DevModel& m, const DevPass& p, const void* diag, const void* in, void* out, int64_t D,
-                     int sms, cudaStream_t s) {
+                     int sms, cudaStream_t s, const int* active) {
     typedef typename V2T<R>::T C;
     const size_t smem = (size_t)TILE_THREADS * E * sizeof(C);
     if (smem > 48 * 1024)
@@ -542,13 +546,14 @@ static void run_fast(const DevModel& m, const DevPass& p, const void* diag, cons
     ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass_fast<R, E>, TILE_THREADS, smem));
     const long long ntiles = (long long)(D >> p.Tp);
     const long long g = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
-    k_hv_pass_fast<R, E><<<(unsigned)g, TILE_THREADS, smem, s>>>(m, p, (const R*)diag, (const C*)in, (C*)out, ntiles);
+    k_hv_pass_fast<R, E><<<(unsigned)g, TILE_THREADS, smem, s>>>(m, p, (const R*)diag, (const C*)in, (C*)out, ntiles,
+                                                                 active);
     ESC_CUDA(cudaGetLastError());
 }
 
 template <int E>
 static void run_f32(const DevModel& m, const DevPass& p, const void* diag, const void* in, void* out, int64_t D, int sms,
-                    cudaStream_t s) {
+                    cudaStream_t s, const int* active) {
     const size_t smem = 2 * (size_t)TILE_THREADS * E * sizeof(float2);   // double buffer
     if (smem > 48 * 1024)
         ESC_CUDA(cudaFuncSetAttribute(k_hv_pass_f32<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -557,13 +562,13 @@ static void run_f32(const DevModel& m, const DevPass& p, const void* diag, const
     const long long ntiles = (long long)(D >> p.Tp);
     const long long g = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
     k_hv_pass_f32<E><<<(unsigned)g, TILE_THREADS, smem, s>>>(m, p, (const float*)diag, (const float2*)in, (float2*)out,
-                                                             ntiles);
+                                                             ntiles, active);
     ESC_CUDA(cudaGetLastError());
 }
 
 template <typename R>
 void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in, void* out, int64_t D,
-                     const void* diag, cudaStream_t s) {
+                     const void* diag, cudaStream_t s, const int* active) {
     typedef typename V2T<R>::T C;
     int dev = 0, sms = 0;
     ESC_CUDA(cudaGetDevice(&dev));
@@ -572,19 +577,19 @@ void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, cons
         if constexpr (sizeof(R) == 4) {
             if (diag && p.c == 3 && p.Tp >= 11 && p.Tp <= 13) {
                 switch (p.Tp) {
-                    case 11: run_f32<4>(m, p, diag, in, out, D, sms, s); break;
-                    case 12: run_f32<8>(m, p, diag, in, out, D, sms, s); break;
-                    default: run_f32<16>(m, p, diag, in, out, D, sms, s); break;
+                    case 11: run_f32<4>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 12: run_f32<8>(m, p, diag, in, out, D, sms, s, active); break;
+                    default: run_f32<16>(m, p, diag, in, out, D, sms, s, active); break;
                 }
                 continue;
             }
         }
         if (diag && p.c == 3 && p.Tp >= 10 && p.Tp <= 13) {
             switch (p.Tp) {
-                case 10: run_fast<R, 2>(m, p, diag, in, out, D, sms, s); break;
-                case 11: run_fast<R, 4>(m, p, diag, in, out, D, sms, s); break;
-                case 12: run_fast<R, 8>(m, p, diag, in, out, D, sms, s); break;
-                default: run_fast<R, 16>(m, p, diag, in, out, D, sms, s); break;
+                case 10: run_fast<R, 2>(m, p, diag, in, out, D, sms, s, active); break;
+                case 11: run_fast<R, 4>(m, p, diag, in, out, D, sms, s, active); break;
+                case 12: run_fast<R, 8>(m, p, diag, in, out, D, sms, s, active); break;
+                default: run_fast<R, 16>(m, p, diag, in, out, D, sms, s, active); break;
             }
             continue;
         }
@@ -595,7 +600,7 @@ void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, cons
         ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass<R>, TILE_THREADS, smem));
         const long long ntiles = (long long)(D >> p.Tp);
         const long long g = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
-        k_hv_pass<R><<<(unsigned)g, TILE_THREADS, smem, s>>>(m, p, (const C*)in, (C*)out, ntiles);
+        k_hv_pass<R><<<(unsigned)g, TILE_THREADS, smem, s>>>(m, p, (const C*)in, (C*)out, ntiles, active);
         ESC_CUDA(cudaGetLastError());
     }
 }
@@ -641,9 +646,9 @@ void launch_permute(const DevPerm& p, const void* in, void* out, int64_t D, cuda
 }
 
 template void launch_hv_tiled<double>(const DevModel&, const std::vector<DevPass>&, const void*, void*, int64_t,
-                                      const void*, cudaStream_t);
+                                      const void*, cudaStream_t, const int*);
 template void launch_hv_tiled<float>(const DevModel&, const std::vector<DevPass>&, const void*, void*, int64_t,
-                                     const void*, cudaStream_t);
+                                     const void*, cudaStream_t, const int*);
 template void launch_diag<double>(const DevModel&, void*, int64_t, cudaStream_t);
 template void launch_diag<float>(const DevModel&, void*, int64_t, cudaStream_t);
 template void launch_permute<double>(const DevPerm&, const void*, void*, int64_t, cudaStream_t);

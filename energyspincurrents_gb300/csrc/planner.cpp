@@ -30,11 +30,14 @@ struct Cand {
 };
 
 Cand greedy(int N, int T, int c, const std::vector<std::pair<int, int>>& bonds, const std::vector<std::vector<int>>& adj,
-            std::mt19937_64& rng) {
+            std::mt19937_64& rng, bool low_sites_shared = false) {
     Cand r;
     std::vector<char> inC(N, 0), covered_site(N, 0);
-    // shared sites: a BFS path from a random start
-    {
+    if (low_sites_shared) {
+        // shared sites fixed to 0..c-1 (identity labelling: the reference basis order)
+        for (int i = 0; i < c; i++) { r.C.push_back(i); inC[i] = 1; covered_site[i] = 1; }
+    } else {
+        // shared sites: a BFS path from a random start
         std::uniform_int_distribution<int> U(0, N - 1);
         int s = U(rng);
         std::vector<int> q{s};
@@ -102,6 +105,37 @@ Cand greedy(int N, int T, int c, const std::vector<std::pair<int, int>>& bonds, 
 }
 
 }  // namespace
+
+Plan make_plan_reference_order(int N, const std::vector<std::pair<int, int>>& bonds, int T, int c, int restarts) {
+    Plan P;
+    P.N = N;
+    P.perm.resize(N);
+    std::iota(P.perm.begin(), P.perm.end(), 0);
+    if (N <= T) {
+        P.T = N; P.c = std::min(c, N);
+        P.tiles.push_back(P.perm);
+        return P;
+    }
+    P.T = T; P.c = c;
+    std::vector<std::vector<int>> adj(N);
+    for (auto& b : bonds) { adj[b.first].push_back(b.second); adj[b.second].push_back(b.first); }
+    std::mt19937_64 rng(0x5eed1234u);
+    Cand best;
+    size_t best_cost = ~size_t(0);
+    for (int t = 0; t < restarts; t++) {
+        Cand cd = greedy(N, T, c, bonds, adj, rng, true);
+        size_t cost = cd.S.size() * 1000;
+        for (auto& s : cd.S) cost += s.size();
+        if (cost < best_cost) { best_cost = cost; best = cd; }
+    }
+    for (auto& S : best.S) {
+        std::vector<int> bits(best.C);
+        bits.insert(bits.end(), S.begin(), S.end());
+        std::sort(bits.begin(), bits.end());
+        P.tiles.push_back(bits);
+    }
+    return P;
+}
 
 Plan make_plan(int N, const std::vector<std::pair<int, int>>& bonds, int T, int c, int restarts) {
     Plan P;

@@ -117,6 +117,18 @@ typedef struct {
     esc_dtype dtype;            /* CF mode: precision of the CF Lanczos vectors                */
 } esc_dyn_cfg;
 
+/* Batched continued-fraction Lanczos: ncols independent three-term recurrences (no
+ * reorthogonalisation) from ncols start vectors, column c with its own field. */
+typedef struct {
+    int ncols;              /* 1..16                                                             */
+    int max_steps;          /* recurrence steps per column (upper bound)                         */
+    const int* steps;       /* per-column step limits (NULL: max_steps for every column)         */
+    const double* fields;   /* ncols x 3 (Bxx, Byy, Bzz), NULL: the handle's field               */
+    double tol;             /* a column stops when beta_k < tol * |phi|  (<= 0: 1e-10)           */
+    esc_dtype dtype;        /* storage/arithmetic of the recurrence vectors                      */
+    int use_graph;          /* 1: one iteration captured in a CUDA graph and replayed            */
+} esc_cf_batch_cfg;
+
 typedef struct esc_handle esc_handle;
 
 /* ---- parameters -------------------------------------------------------------------------- */
@@ -196,6 +208,13 @@ esc_status esc_rayleigh(esc_handle* h, const void* v, esc_dtype dt, int flags, d
 esc_status esc_lanczos_gs(esc_handle* h, const esc_lanczos_cfg* cfg, const void* start, int flags,
                           double* E0, double* alpha, double* beta, double* ritz, int* steps,
                           void* gs_out);
+
+/* Batched continued-fraction coefficients (extension; the reference has no continued fraction).
+ * starts: ncols vectors of 2^N states with stride ld (elements).  On return, for column c:
+ * a[c*max_steps + k] (k < lens[c]) and b[c*(max_steps+1) + k] (k <= lens[c]), b[.. + 0] = |phi_c|,
+ * so that <phi|(z-H)^-1|phi> = b0^2/(z - a0 - b1^2/(z - a1 - ...)). */
+esc_status esc_cf_batched(esc_handle* h, const esc_cf_batch_cfg* cfg, const void* starts, int64_t ld, int flags,
+                          double* a, double* b, int* lens);
 
 /* Dynamical correlations of the last ground state.  Replaces DynJeJe / DynJsJs / LocalDynSzSz
  * (src/dynamics.h:345-460, :222-341, :64-217).  `out` receives (omega_steps+1) x ncols doubles in

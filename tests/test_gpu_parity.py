@@ -286,3 +286,48 @@ def test_mixed_precision_e0_refined_to_fp64():
     e_ref = h.rayleigh(r["gs"])
     assert abs(r["E0"] - e_exact) < 1e-5 * abs(e_exact)          # complex64 recurrence
     assert abs(e_ref - e_exact) < 1e-10 * abs(e_exact)           # after the FP64 sweep
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_cf_batched_vs_oracle(use_graph):
+    """Batched CF Lanczos: per-column fields and step limits; each column against the oracle's
+    continued-fraction recurrence on the same start vector and field."""
+    base = kitaev(J=0.1)
+    h = esc.Handle(base)
+    rng = np.random.default_rng(3)
+    nc = 5
+    V = rng.standard_normal((nc, h.D)) + 1j * rng.standard_normal((nc, h.D))
+    fields = np.array([[base["Bxx"]] * 3, [0.0] * 3, [-0.02, -0.02, -0.02], [0.1, -0.2, 0.3], [-0.1] * 3])
+    steps = np.array([40, 7, 25, 40, 1], dtype=np.int32)
+    out = h.cf_batched(V, 40, steps=steps, fields=fields, use_graph=use_graph)
+    for c in range(nc):
+        a, b = out[c]
+        assert a.size == steps[c]
+        m = O.Model("Kitaev", 3, 4, 1, 1, -1.0, -1.0, -1.0, *fields[c], 0.1, 4, False)
+        ao, bo = m.cf_lanczos(V[c], int(steps[c]))
+        assert abs(b[0] - np.linalg.norm(V[c])) < 1e-12 * b[0]
+        # without reorthogonalisation the recurrence amplifies rounding; the first steps agree closely
+        k = min(10, a.size)
+        np.testing.assert_allclose(a[:k], ao[:k], atol=1e-10)
+        np.testing.assert_allclose(b[1:k], bo[1:k], atol=1e-10)
+
+
+def test_cf_batched_graph_is_bitwise_equal_to_stream():
+    h = esc.Handle(kitaev(J=0.1))
+    V = np.stack([O.random_start(s, h.D) for s in (1, 2, 3)])
+    g = h.cf_batched(V, 30, use_graph=True)
+    s = h.cf_batched(V, 30, use_graph=False)
+    for (a1, b1), (a2, b2) in zip(g, s):
+        assert np.array_equal(a1, a2) and np.array_equal(b1, b2)
+
+
+def test_cf_batched_stops_on_exhausted_krylov_space():
+    """A start vector in a 2-dimensional invariant subspace stops after two steps (beta < tol)."""
+    h = esc.Handle(kitaev(Lx=2, Ly=4, J=0.1))
+    m = O.Model("Kitaev", 2, 4, 1, 1, -1.0, -1.0, -1.0, *([-0.05 / S3] * 3), 0.1, 2, True)
+    w, Vv = np.linalg.eigh(m.dense())
+    phi = (Vv[:, 0] + Vv[:, 5]).astype(np.complex128)
+    (a, b), = h.cf_batched(phi[None, :], 50)
+    assert a.size == 2
+    np.testing.assert_allclose(sorted(np.linalg.eigvalsh(np.diag(a) + np.diag(b[1:2], 1) + np.diag(b[1:2], -1))),
+                               [w[0], w[5]], atol=1e-10)
