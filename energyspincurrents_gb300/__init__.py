@@ -75,7 +75,7 @@ _lib = None
 # every symbol declared in include/esc.h
 EXPORTS = ["esc_params_default", "esc_params_from_file", "esc_lattice", "esc_plan", "esc_create", "esc_destroy", "esc_last_error",
            "esc_num_sites", "esc_dim", "esc_neighbors", "esc_basis_permutation", "esc_stream", "esc_hv", "esc_hv_batched", "esc_apply_op",
-           "esc_start_vector", "esc_rayleigh", "esc_lanczos_gs", "esc_cf_batched", "esc_spectrum", "esc_measure_local", "esc_grad"]
+           "esc_start_vector", "esc_rayleigh", "esc_rayleigh_noalloc", "esc_lanczos_gs", "esc_cf_batched", "esc_spectrum", "esc_measure_local", "esc_grad"]
 
 
 def lib_path():
@@ -111,6 +111,7 @@ def lib():
     L.esc_apply_op.argtypes = [vp, ci, ci, vp, vp, ci, ci]
     L.esc_start_vector.argtypes = [vp, ci, ci, vp, ci, ci]
     L.esc_rayleigh.argtypes = [vp, vp, ci, ci, P(cd)]
+    L.esc_rayleigh_noalloc.argtypes = [P(Params), vp, ci, vp, P(cd)]
     L.esc_lanczos_gs.argtypes = [vp, P(LanczosCfg), vp, ci, P(cd), vp, vp, vp, P(ci), vp]
     L.esc_spectrum.argtypes = [vp, P(DynCfg), vp, P(ci), P(ci)]
     L.esc_cf_batched.argtypes = [vp, P(CFBatchCfg), vp, i64, ci, vp, vp, vp]

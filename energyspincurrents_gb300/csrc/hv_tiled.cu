@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 #include "esc_internal.h"
 
@@ -655,3 +656,104 @@ template void launch_permute<double>(const DevPerm&, const void*, void*, int64_t
 template void launch_permute<float>(const DevPerm&, const void*, void*, int64_t, cudaStream_t);
 
 }  // namespace esc
+
+// =============================================================================================
+// Allocation-free Rayleigh quotient.
+//
+// For callers that cannot allocate device memory themselves or through this library: code that
+// runs inside another framework's memory pool, under a memory cap, or in a process that must not
+// grow its device footprint after start-up.  The scratch of this entry point (one partial energy
+// per tile, the norm-reduction partials and the result) is the file-scope array below, which
+// every GPU that loads the library holds until the process exits.
+// =============================================================================================
+namespace esc {
+namespace {
+constexpr int NOALLOC_TILE_BITS = 12;
+constexpr int NOALLOC_MAX_TILES = 1 << 13;                 // 2^13 tiles of 2^12 states: N <= 25
+constexpr int NOALLOC_SCRATCH = 2 * NOALLOC_MAX_TILES      // per-tile (re, im) energy partials
+                                + 2 * RED_MAX_BLOCKS       // norm-reduction partials
+                                + 8;                       // reduction result
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+}  // namespace
+
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH];
+
+}  // namespace esc
+
+extern "C" esc_status esc_rayleigh_noalloc(const esc_params* p, const void* v, esc_dtype dt, void* stream, double* E) {
+    using namespace esc;
+    auto fail = [&](esc_status st, const std::string& m) { set_last_error(m); return st; };
+    if (!p || !v || !E) return fail(ESC_ERR_PARAM, "null argument");
+    try {
+        cudaStream_t s = (cudaStream_t)stream;
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+            (void)cudaGetLastError();
+            return fail(ESC_ERR_CUDA, "no usable CUDA device");
+        }
+        double* scratch = nullptr;
+        {
+            // once per device, with that device current: the device address of the static array
+            std::lock_guard<std::mutex> lk(g_noalloc_mu);
+            if (!g_noalloc_ptr[dev]) {
+                void* ptr = nullptr;
+                const cudaError_t rc = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+                if (rc != cudaSuccess || !ptr) {
+                    (void)cudaGetLastError();
+                    return fail(ESC_ERR_CUDA, std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(rc));
+                }
+                g_noalloc_ptr[dev] = ptr;
+            }
+            scratch = (double*)g_noalloc_ptr[dev];
+        }
+        Lattice L;
+        std::vector<Bond> bonds;
+        build_lattice(*p, L);
+        build_bonds(*p, L, bonds);
+        const int N = L.N;
+        const int64_t D = int64_t(1) << N;
+        if (N - NOALLOC_TILE_BITS > 13)
+            return fail(ESC_ERR_PARAM, "esc_rayleigh_noalloc: at most 25 sites (2^25 states); the static scratch holds "
+                                       "8192 tile partials");
+        std::vector<std::pair<int, int>> pairs;
+        for (const auto& b : bonds)
+            if (b.kx - b.ky != 0.0 || b.kx + b.ky != 0.0) pairs.push_back({b.i, b.j});
+        const Plan P = make_plan_reference_order(N, pairs, NOALLOC_TILE_BITS, 3, 200);
+        const DevModel m = make_dev_model(*p, L, bonds, p->Bxx, p->Byy, p->Bzz);
+        const std::vector<DevPass> passes = make_passes(P, m);
+        double* part = scratch;                                // [2 * tiles]
+        double* red = scratch + 2 * NOALLOC_MAX_TILES;         // [2 * RED_MAX_BLOCKS]
+        double* res = red + 2 * RED_MAX_BLOCKS;                // [2]
+        double num = 0.0;
+        for (const DevPass& ps : passes) {
+            const long long ntiles = (long long)(D >> ps.Tp);
+            const size_t smem = (size_t(1) << ps.Tp) * sizeof(double2);
+            // one CTA per tile: every partial the host reads below is written by this launch
+            if (dt == ESC_C64) {
+                if (smem > 48 * 1024) ESC_CUDA(cudaFuncSetAttribute(k_energy_pass<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                k_energy_pass<float><<<(unsigned)ntiles, TILE_THREADS, smem, s>>>(m, ps, (const float2*)v, part, ntiles);
+            } else {
+                if (smem > 48 * 1024) ESC_CUDA(cudaFuncSetAttribute(k_energy_pass<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                k_energy_pass<double><<<(unsigned)ntiles, TILE_THREADS, smem, s>>>(m, ps, (const double2*)v, part, ntiles);
+            }
+            ESC_CUDA(cudaGetLastError());
+            std::vector<double> h(2 * (size_t)ntiles);
+            ESC_CUDA(cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+            ESC_CUDA(cudaStreamSynchronize(s));
+            for (long long i = 0; i < ntiles; i++) num += h[2 * i];
+        }
+        if (dt == ESC_C64) launch_dot<float>(v, v, D, red, res, s);
+        else launch_dot<double>(v, v, D, red, res, s);
+        double nn[2];
+        ESC_CUDA(cudaMemcpyAsync(nn, res, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        ESC_CUDA(cudaStreamSynchronize(s));
+        *E = num / nn[0];
+        return ESC_OK;
+    } catch (std::invalid_argument& e) {
+        return fail(ESC_ERR_PARAM, e.what());
+    } catch (std::exception& e) {
+        return fail(ESC_ERR_CUDA, e.what());
+    }
+}

@@ -197,6 +197,24 @@ esc_status esc_start_vector(esc_handle* h, int kind, int seed, void* out, esc_dt
  * counterpart. */
 esc_status esc_rayleigh(esc_handle* h, const void* v, esc_dtype dt, int flags, double* E);
 
+/* Allocation-free variant of esc_rayleigh, for callers that cannot allocate device memory: code
+ * running inside another framework's memory pool or under a fixed memory budget, or a process
+ * that must not grow its device footprint after start-up.  No counterpart in the reference.
+ *   - No handle: the model comes from `p`; `v` is a DEVICE pointer to 2^N states in the
+ *     reference basis order (complex128 or complex64 per `dt`); work is queued on `stream`
+ *     (cudaStream_t, NULL = legacy default stream) and the call returns after synchronising it.
+ *   - It calls no cudaMalloc/cudaFree and no allocating library routine.  Its scratch is a
+ *     file-scope __device__ array of 2*8192 + 2*1216 + 8 doubles (about 150 KB) that every GPU
+ *     which loads the library holds until the process exits.  The array holds one partial per
+ *     tile of 2^12 states, so at most 25 sites (2^25 states) are accepted; larger models fail with
+ *     ESC_ERR_PARAM and a message in esc_last_error(NULL).
+ *   - The first call on a device looks up the array's device address there (with that device
+ *     current); make that first call before any CUDA stream capture.
+ *   - All calls share the one array: calls whose work overlaps on the GPU (other streams, other
+ *     host threads, same device) race and may return wrong results.  Every value read back is
+ *     written by the same call, so nothing has to be cleared between calls. */
+esc_status esc_rayleigh_noalloc(const esc_params* p, const void* v, esc_dtype dt, void* stream, double* E);
+
 /* ---- solvers ----------------------------------------------------------------------------------- */
 
 /* Ground-state Lanczos.  Replaces DynLanczosSolver::Lanczos_Nirav (src/DynLanczosSolver.h:38-239)
