@@ -152,6 +152,32 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def time_to_spectrum(esc, sites=24, gs_steps=300, cf_steps=500):
+    """time-to-S(omega) on the JeJe channels (CF mode, 2000 omega in [0,6], eta=0.05): mixed batched
+    (complex64 vectors, the four channels as columns of one batched CUDA-graph recurrence) against
+    plain FP64 (complex128, same path).  Ground states are computed first and are not timed."""
+    import numpy as np
+    params = workload(sites)
+    P = esc.ConstVariables(**params, omega_steps=1999, domega=6.0 / 1999, eta=0.05)
+    out = {"sites": sites, "kind": "JeJe, continued fraction", "gs_steps": gs_steps, "cf_steps": cf_steps,
+           "omega": "2000 points in [0,6]", "eta": 0.05}
+    res = {}
+    for name, dt in (("mixed", np.complex64), ("fp64", np.complex128)):
+        h = esc.Handle(P)
+        r = h.lanczos_gs(steps=gs_steps, lanctype="GS", reortho=0, dtype=dt, want_gs=False)
+        t0 = time.perf_counter()
+        S = h.spectrum("Energy Current", "CF", cf_steps=cf_steps)
+        res[name] = (time.perf_counter() - t0, S, r["E0"])
+        h.close()
+    out["mixed_batched_s"] = round(res["mixed"][0], 3)
+    out["fp64_s"] = round(res["fp64"][0], 3)
+    out["speedup"] = round(res["fp64"][0] / res["mixed"][0], 2)
+    out["max_abs_dS"] = float(np.abs(res["mixed"][1][:, 1:] - res["fp64"][1][:, 1:]).max())
+    out["max_abs_S"] = float(np.abs(res["fp64"][1][:, 1:]).max())
+    out["E0_mixed_minus_fp64"] = res["mixed"][2] - res["fp64"][2]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -161,6 +187,7 @@ def main():
     ap.add_argument("--sites", type=int, default=32)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-spectrum", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -185,14 +212,13 @@ def main():
     stream = torch.cuda.ExternalStream(h.stream())
     v = torch.empty(D, dtype=torch.complex64, device="cuda")
     out = torch.empty_like(v)
-    h_st = esc.lib().esc_start_vector(h.h, 1, 1, esc.ctypes.c_void_p(v.data_ptr()), esc.C64, esc.DEVICE_PTR)
-    assert h_st == 0, esc.lib().esc_last_error(h.h)
-    torch.cuda.synchronize()
-
     # vectors stay resident in the library's internal basis order (a fixed relabelling of the sites;
     # inner products and spectra do not depend on it), so a step is exactly the H.v kernels
     flags = esc.DEVICE_PTR | esc.ASYNC | esc.INTERNAL_ORDER
+    st = esc.lib().esc_start_vector(h.h, 1, 1, esc.ctypes.c_void_p(v.data_ptr()), esc.C64, flags)
+    assert st == 0, esc.lib().esc_last_error(h.h)
     npasses = esc.plan(esc.ConstVariables(**params))[1]
+    torch.cuda.synchronize()
 
     def step():
         h.hv_device(v.data_ptr(), out.data_ptr(), esc.C64, flags)
@@ -220,19 +246,25 @@ def main():
     kernel_gbs = algo_bytes / (ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
     prof = traffic_from_profile()
+    traffic = None
+    if prof and prof.get("bytes_per_state"):
+        traffic = int(prof["bytes_per_state"] * D)
     roof = {"bound": "hbm", "achieved": round(kernel_gbs, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(kernel_gbs / peak, 4), "peak_source": peak_kind,
-            "traffic": (prof or {}).get("bytes_per_launch"),
-            "kernel": "k_hv_pass<float>", "passes": npasses, "algorithmic_bytes_per_launch": algo_bytes}
+            "frac": round(kernel_gbs / peak, 4), "peak_source": peak_kind, "traffic": traffic,
+            "kernel": "k_hv_pass_f32 (all passes of one H.v)", "passes": npasses,
+            "algorithmic_bytes_per_launch": algo_bytes,
+            "traffic_source": (prof or {}).get("source")}
+    del v, out
+    torch.cuda.empty_cache()
 
-    # end to end through the C ABI with host buffers (pinned), copies inside the timed region
+    # end to end through the C ABI: host buffers (pinned) in the reference basis order; the host->
+    # device copy, the basis permutations, H.v and the device->host copy are inside the timed region
     e2e = None
     if not args.no_e2e:
         try:
             hin = torch.empty(D, dtype=torch.complex64, pin_memory=True)
             hout = torch.empty(D, dtype=torch.complex64, pin_memory=True)
-            del out
-            torch.cuda.empty_cache()
+            hin.zero_()
             h.hv(hin.numpy(), out=hout.numpy())   # warm-up (allocates the staging buffers)
             reps = max(1, min(args.steps, 3))
             t0 = time.perf_counter()
@@ -240,9 +272,19 @@ def main():
                 h.hv(hin.numpy(), out=hout.numpy())
             el = (time.perf_counter() - t0) / reps
             e2e = {"value": round(world * algo_bytes / el / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": D * 8,
-                   "d2h_bytes_per_step": D * 8, "ms_per_step": round(el * 1e3, 3)}
+                   "d2h_bytes_per_step": D * 8, "ms_per_step": round(el * 1e3, 3),
+                   "path": "esc_hv, host pointers, reference basis order"}
+            del hin, hout
         except Exception as ex:
             e2e = {"value": None, "unit": "GB/s", "error": str(ex)[:200]}
+    h.close()
+    torch.cuda.empty_cache()
+    tts = None
+    if rank == 0 and not args.no_spectrum:
+        try:
+            tts = time_to_spectrum(esc)
+        except Exception as ex:
+            tts = {"error": str(ex)[:200]}
     cb = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(params, args.sites)
@@ -251,10 +293,10 @@ def main():
                 "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "c64", "data": "synthetic",
                 "config": {"workload": f"Kitaev-Heisenberg honeycomb N={args.sites} ({params['Lx']}x{params['Ly']//2} "
-                                       f"unit cells, PBC), K=-1 J=0.05 h=0.02[111], one H.v per step",
+                                       f"unit cells, PBC), K=-1 J=0.05 h=0.02[111], one H.v per step (complex64)",
                            "states": D, "l2": "inputs larger than L2 (no flush needed)" if D * 8 > 129e6 else
                            "inputs smaller than L2", "parallelism": "replicas" if world > 1 else "single GPU"},
-                "roofline": roof, "cpu_baseline": cb, "e2e": e2e, "clocks": clk.summary(),
+                "roofline": roof, "cpu_baseline": cb, "e2e": e2e, "time_to_S": tts, "clocks": clk.summary(),
                 "gpu_launches": args.steps * npasses}
         print(json.dumps(line), flush=True)
     if dist:
