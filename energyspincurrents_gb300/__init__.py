@@ -336,6 +336,14 @@ class Handle:
         _check(self.h, lib().esc_grad(self.h, None, _ptr(d), None))
         return d
 
+    def grad(self, kind="Energy Current", cf_steps=200, omega_steps=499, domega=0.01, eta=0.05):
+        """(dE0/d{K,J,h}, dImS_tt(omega)/d{K,J,h}) of the CF-mode total-current spectrum (FP64)."""
+        cfg = DynCfg(DYN_KIND[kind], 1, omega_steps, domega, eta, cf_steps, C128)
+        d = np.zeros(3)
+        dS = np.zeros((omega_steps + 1, 3))
+        _check(self.h, lib().esc_grad(self.h, ctypes.byref(cfg), _ptr(d), _ptr(dS)))
+        return d, dS
+
 
 # ------------------------------------------------------------------------------------------------
 # Reference-named mirror

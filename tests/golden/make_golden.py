@@ -258,5 +258,27 @@ def main():
         print(name, "N=%d" % res["N"], "E0=%.15f" % res["ritz"][0], "steps=%d" % res["alpha"].size)
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and "--refout" not in sys.argv:
     main()
+
+
+def make_reference_outputs(name="kitaev12m60"):
+    """Run the reference's unmodified main (oracle/_ref/LanczosCond) and keep its output files
+    (format fixtures for the drop-in executable: default stream precision, ' \\t ' separators)."""
+    out = build_ref.build()
+    text = CASES[name][0]
+    work = tempfile.mkdtemp(prefix="refout_")
+    try:
+        with open(os.path.join(work, "params.inp"), "w") as f:
+            f.write(text)
+        subprocess.run([os.path.join(out, "LanczosCond"), "params.inp"], cwd=work, capture_output=True, check=True)
+        for fn in ("JeJe_outSpectrum.real", "JsJs_outSpectrum.real"):
+            shutil.copy(os.path.join(work, fn), os.path.join(HERE, f"refout_{name}_{fn}"))
+        with open(os.path.join(HERE, f"refout_{name}.inp"), "w") as f:
+            f.write(text)
+    finally:
+        shutil.rmtree(work, ignore_errors=True)
+
+
+if __name__ == "__main__" and "--refout" in sys.argv:
+    make_reference_outputs()

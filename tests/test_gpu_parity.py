@@ -331,3 +331,30 @@ def test_cf_batched_stops_on_exhausted_krylov_space():
     assert a.size == 2
     np.testing.assert_allclose(sorted(np.linalg.eigvalsh(np.diag(a) + np.diag(b[1:2], 1) + np.diag(b[1:2], -1))),
                                [w[0], w[5]], atol=1e-10)
+
+
+def _tt_spectrum(K, J, hf, nw, dw, eta, steps, kind="Energy Current", Lx=3, Ly=4):
+    b = -hf / S3
+    hh = esc.Handle(dict(Lx=Lx, Ly=Ly, Kxx=K, Kyy=K, Kzz=K, Bxx=b, Byy=b, Bzz=b, jheis=J, lanczos_steps=160))
+    hh.lanczos_gs(start=O.random_start(0, hh.D), lanctype="GS")
+    col = 5 if kind == "Energy Current" else 14
+    return hh, hh.spectrum(kind, "CF", omega_steps=nw - 1, domega=dw, eta=eta, cf_steps=steps)[:, col]
+
+
+@pytest.mark.parametrize("kind", ["Energy Current", "Spin Current"])
+def test_grad_spectrum_vs_central_differences(kind):
+    """d Im S_tt(omega)/d{K, J, h} (tangent-mode CF Lanczos + adjoint continued fraction +
+    Sternheimer ground-state derivative) against central differences, step 1e-5, FP64."""
+    K, J, hf, d = -1.0, 0.1, 0.05, 1e-5
+    nw, dw, eta, steps = 300, 0.02, 0.05, 80
+    hh, _ = _tt_spectrum(K, J, hf, nw, dw, eta, steps, kind)
+    dE, dS = hh.grad(kind, cf_steps=steps, omega_steps=nw - 1, domega=dw, eta=eta)
+    fd = []
+    for q in range(3):
+        e = np.zeros(3); e[q] = d
+        sp = _tt_spectrum(K + e[0], J + e[1], hf + e[2], nw, dw, eta, steps, kind)[1]
+        sm = _tt_spectrum(K - e[0], J - e[1], hf - e[2], nw, dw, eta, steps, kind)[1]
+        fd.append((sp - sm) / (2 * d))
+    fd = np.stack(fd, 1)
+    scale = max(1.0, np.abs(fd).max())
+    assert np.abs(dS - fd).max() <= 1e-5 * scale, (np.abs(dS - fd).max(), scale)
