@@ -67,7 +67,7 @@ class CFBatchCfg(ctypes.Structure):
 class DynCfg(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("mode", ctypes.c_int), ("omega_steps", ctypes.c_int),
                 ("domega", ctypes.c_double), ("eta", ctypes.c_double), ("cf_steps", ctypes.c_int),
-                ("dtype", ctypes.c_int)]
+                ("dtype", ctypes.c_int), ("fp64_head", ctypes.c_int)]
 
 
 _lib = None
@@ -315,10 +315,15 @@ class Handle:
                                             _ptr(lens)))
         return [(a[c, : lens[c]], b[c, : lens[c] + 1]) for c in range(nc)]
 
-    def spectrum(self, kind, mode="Ritz", omega_steps=None, domega=None, eta=None, cf_steps=0):
+    def spectrum(self, kind, mode="Ritz", omega_steps=None, domega=None, eta=None, cf_steps=0, dtype=None,
+                 fp64_head=0):
+        """Rows of the reference's output file.  CF mode runs in complex64 when the ground state is
+        complex64 or dtype is np.complex64; fp64_head: leading CF steps of a complex64 run done in
+        complex128 (0: library default, < 0: none)."""
         p = self.params.p
+        dt = C64 if dtype is not None and np.dtype(dtype) == np.complex64 else C128
         cfg = DynCfg(DYN_KIND[kind], {"Ritz": 0, "CF": 1}[mode], p.omega_steps if omega_steps is None else omega_steps,
-                     p.domega if domega is None else domega, p.eta if eta is None else eta, cf_steps, C128)
+                     p.domega if domega is None else domega, p.eta if eta is None else eta, cf_steps, dt, fp64_head)
         nr = ctypes.c_int(); nc = ctypes.c_int()
         _check(self.h, lib().esc_spectrum(self.h, ctypes.byref(cfg), None, ctypes.byref(nr), ctypes.byref(nc)))
         out = np.empty(nr.value * nc.value)

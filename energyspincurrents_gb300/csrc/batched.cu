@@ -35,7 +35,8 @@ __device__ __forceinline__ void bff_addprod(float& hi, float& lo, float a, float
 }
 
 static constexpr int BTPB = 256;
-static constexpr int BGRID = 304;   // blocks per column for the reductions (2 x 152 SMs)
+static constexpr int BGRID = CFB_GRID;   // blocks per column for the streaming kernels and reductions
+static constexpr int UNR = 4;            // independent elements in flight per thread
 
 __device__ __forceinline__ void block_sum2(double& a, double& b, double* dst) {
     __shared__ double sm[2][BTPB / 32];
@@ -54,32 +55,49 @@ __device__ __forceinline__ void block_sum2(double& a, double& b, double* dst) {
     __syncthreads();
 }
 
+// Grid-stride loop over [0, D) that hands UNR elements (i, i + stride, ...) to f at once, so
+// that each thread keeps UNR independent loads in flight; the visiting order is fixed by the
+// grid, which keeps the reductions built on it deterministic.
+template <typename F>
+__device__ __forceinline__ void stream_loop(long long D, F&& f) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + (UNR - 1) * stride < D; i += UNR * stride) f(i, stride, UNR);
+    for (; i < D; i += stride) f(i, stride, 1);
+}
+
 // alpha partials: blockIdx.y = column; partial (re, im) of <cur|w>
 template <typename R>
 __global__ void __launch_bounds__(BTPB) kb_dot(const typename V2B<R>::T* __restrict__ cur,
                                                const typename V2B<R>::T* __restrict__ w, long long D,
                                                const int* __restrict__ active, double* __restrict__ part) {
+    typedef typename V2B<R>::T C;
     const int c = blockIdx.y;
     if (!active[c]) return;
-    const typename V2B<R>::T* x = cur + (size_t)c * D;
-    const typename V2B<R>::T* y = w + (size_t)c * D;
+    const C* x = cur + (size_t)c * D;
+    const C* y = w + (size_t)c * D;
     double re = 0.0, im = 0.0;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    if constexpr (sizeof(R) == 4) {
-        float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) {
-            const float2 a = x[i], b = y[i];
-            bff_addprod(rh, rl, a.x, b.x); bff_addprod(rh, rl, a.y, b.y);
-            bff_addprod(ih, il, a.x, b.y); bff_addprod(ih, il, -a.y, b.x);
+    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+    stream_loop(D, [&](long long i, long long st, int n) {
+        C a[UNR], b[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; u++)
+            if (u < n) { a[u] = x[i + u * st]; b[u] = y[i + u * st]; }
+#pragma unroll
+        for (int u = 0; u < UNR; u++) {
+            if (u >= n) break;
+            if constexpr (sizeof(R) == 4) {
+                bff_addprod(rh, rl, a[u].x, b[u].x); bff_addprod(rh, rl, a[u].y, b[u].y);
+                bff_addprod(ih, il, a[u].x, b[u].y); bff_addprod(ih, il, -a[u].y, b[u].x);
+            } else {
+                re += a[u].x * b[u].x + a[u].y * b[u].y;
+                im += a[u].x * b[u].y - a[u].y * b[u].x;
+            }
         }
+    });
+    if constexpr (sizeof(R) == 4) {
         re = (double)rh + (double)rl;
         im = (double)ih + (double)il;
-    } else {
-        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) {
-            const double2 a = x[i], b = y[i];
-            re += a.x * b.x + a.y * b.y;
-            im += a.x * b.y - a.y * b.x;
-        }
     }
     block_sum2(re, im, part + ((size_t)c * gridDim.x + blockIdx.x) * 2);
 }
@@ -111,31 +129,39 @@ __global__ void __launch_bounds__(BTPB) kb_update(typename V2B<R>::T* __restrict
                                                   const int* __restrict__ it_p, const int* __restrict__ active,
                                                   const double* __restrict__ alpha, const double* __restrict__ b2,
                                                   int kmax, double* __restrict__ part) {
+    typedef typename V2B<R>::T C;
     const int c = blockIdx.y;
     if (!active[c]) return;
     const int it = *it_p;
     const R ar = (R)alpha[((size_t)c * kmax + it) * 2], ai = (R)alpha[((size_t)c * kmax + it) * 2 + 1];
     const R be = it > 0 ? (R)sqrt(b2[(size_t)c * (kmax + 1) + it]) : (R)0;
-    typename V2B<R>::T* W = w + (size_t)c * D;
-    const typename V2B<R>::T* X = cur + (size_t)c * D;
-    const typename V2B<R>::T* P = prev + (size_t)c * D;
+    C* W = w + (size_t)c * D;
+    const C* X = cur + (size_t)c * D;
+    const C* P = prev + (size_t)c * D;
     double acc = 0.0, dummy = 0.0;
     float hh = 0.f, ll = 0.f;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) {
-        typename V2B<R>::T a = W[i];
-        const typename V2B<R>::T x = X[i];
-        a.x = a.x - (ar * x.x - ai * x.y);
-        a.y = a.y - (ar * x.y + ai * x.x);
-        if (it > 0) {
-            const typename V2B<R>::T p = P[i];
-            a.x = a.x - be * p.x;
-            a.y = a.y - be * p.y;
+    stream_loop(D, [&](long long i, long long st, int n) {
+        C a[UNR], x[UNR], p[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; u++)
+            if (u < n) {
+                a[u] = W[i + u * st];
+                x[u] = X[i + u * st];
+                p[u] = it > 0 ? P[i + u * st] : C{(R)0, (R)0};
+            }
+#pragma unroll
+        for (int u = 0; u < UNR; u++) {
+            if (u >= n) break;
+            C o = a[u];
+            o.x = o.x - (ar * x[u].x - ai * x[u].y);
+            o.y = o.y - (ar * x[u].y + ai * x[u].x);
+            o.x = o.x - be * p[u].x;
+            o.y = o.y - be * p[u].y;
+            W[i + u * st] = o;
+            if constexpr (sizeof(R) == 4) { bff_addprod(hh, ll, o.x, o.x); bff_addprod(hh, ll, o.y, o.y); }
+            else acc += (double)o.x * o.x + (double)o.y * o.y;
         }
-        W[i] = a;
-        if constexpr (sizeof(R) == 4) { bff_addprod(hh, ll, a.x, a.x); bff_addprod(hh, ll, a.y, a.y); }
-        else acc += (double)a.x * a.x + (double)a.y * a.y;
-    }
+    });
     if constexpr (sizeof(R) == 4) acc = (double)hh + (double)ll;
     block_sum2(acc, dummy, part + ((size_t)c * gridDim.x + blockIdx.x) * 2);
 }
@@ -154,31 +180,43 @@ __global__ void __launch_bounds__(BTPB) kb_beta(const double* __restrict__ part,
         const int it = *it_p;
         b2[(size_t)c * (kmax + 1) + it + 1] = out[0];
         const double b0 = sqrt(b2[(size_t)c * (kmax + 1)]);
-        if (!(sqrt(out[0]) > tol * b0) || it + 1 >= steps[c]) active[c] = 0;
+        // 2: stops after this iteration; kb_scale still normalises its last vector, kb_advance clears it
+        if (!(sqrt(out[0]) > tol * b0) || it + 1 >= steps[c]) active[c] = 2;
     }
 }
 
-// w /= beta (columns still active, and the column that just stopped: harmless)
+// w /= beta (columns still active, and the column that just stopped)
 template <typename R>
 __global__ void __launch_bounds__(BTPB) kb_scale(typename V2B<R>::T* __restrict__ w, long long D,
                                                  const int* __restrict__ it_p, const int* __restrict__ active,
                                                  const double* __restrict__ b2, int kmax) {
+    typedef typename V2B<R>::T C;
     const int c = blockIdx.y;
     if (!active[c]) return;
     const int it = *it_p;
     const double nb = sqrt(b2[(size_t)c * (kmax + 1) + it + 1]);
     const R inv = (R)(nb > 0.0 ? 1.0 / nb : 0.0);
-    typename V2B<R>::T* W = w + (size_t)c * D;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) {
-        typename V2B<R>::T a = W[i];
-        a.x *= inv;
-        a.y *= inv;
-        W[i] = a;
-    }
+    C* W = w + (size_t)c * D;
+    stream_loop(D, [&](long long i, long long st, int n) {
+        C a[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; u++)
+            if (u < n) a[u] = W[i + u * st];
+#pragma unroll
+        for (int u = 0; u < UNR; u++)
+            if (u < n) {
+                a[u].x *= inv;
+                a[u].y *= inv;
+                W[i + u * st] = a[u];
+            }
+    });
 }
 
-__global__ void kb_advance(int* it_p) { *it_p += 1; }
+__global__ void kb_advance(int* it_p, int* active, int ncols) {
+    for (int c = 0; c < ncols; c++)
+        if (active[c] == 2) active[c] = 0;
+    *it_p += 1;
+}
 
 // |phi_c|^2 -> b2[c][0]; cur_c /= |phi_c|
 template <typename R>
@@ -231,12 +269,17 @@ void CFBatch<R>::run(cudaStream_t s) {
     const size_t vs = (size_t)ncols * D;
     C* V[3] = {(C*)bufs, (C*)bufs + vs, (C*)bufs + 2 * vs};
     const dim3 gcol(BGRID, ncols);
-    // start: cur = V[1] holds phi
-    ESC_CUDA(cudaMemsetAsync(d_it, 0, sizeof(int), s));
-    kb_norm0<R><<<gcol, BTPB, 0, s>>>(V[1], D, d_part);
-    kb_norm0_final<<<ncols, BTPB, 0, s>>>(d_part, BGRID, d_b2, kmax, d_active);
-    kb_scale0<R><<<gcol, BTPB, 0, s>>>(V[1], D, d_b2, kmax);
-    ESC_CUDA(cudaGetLastError());
+    if (start_it == 0) {
+        // start: cur = V[1] holds phi
+        ESC_CUDA(cudaMemsetAsync(d_it, 0, sizeof(int), s));
+        kb_norm0<R><<<gcol, BTPB, 0, s>>>(V[1], D, d_part);
+        kb_norm0_final<<<ncols, BTPB, 0, s>>>(d_part, BGRID, d_b2, kmax, d_active);
+        kb_scale0<R><<<gcol, BTPB, 0, s>>>(V[1], D, d_b2, kmax);
+        ESC_CUDA(cudaGetLastError());
+    } else {
+        // pageable source: the copy completes before cudaMemcpyAsync returns
+        ESC_CUDA(cudaMemcpyAsync(d_it, &start_it, sizeof(int), cudaMemcpyHostToDevice, s));
+    }
     auto iteration = [&](int r) {
         C* prev = V[r % 3];
         C* cur = V[(r + 1) % 3];
@@ -247,15 +290,15 @@ void CFBatch<R>::run(cudaStream_t s) {
         kb_update<R><<<gcol, BTPB, 0, s>>>(w, cur, prev, D, d_it, d_active, d_alpha, d_b2, kmax, d_part);
         kb_beta<<<ncols, BTPB, 0, s>>>(d_part, BGRID, d_it, d_active, d_b2, kmax, d_steps, tol);
         kb_scale<R><<<gcol, BTPB, 0, s>>>(w, D, d_it, d_active, d_b2, kmax);
-        kb_advance<<<1, 1, 0, s>>>(d_it);
+        kb_advance<<<1, 1, 0, s>>>(d_it, d_active, ncols);
         ESC_CUDA(cudaGetLastError());
     };
-    const int rounds = (kmax + 2) / 3;
+    const int rounds = (kmax - start_it + 2) / 3;
     if (use_graph) {
         cudaGraph_t g = nullptr;
         cudaGraphExec_t ge = nullptr;
         ESC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        for (int r = 0; r < 3; r++) iteration(r);
+        for (int r = 0; r < 3; r++) iteration(start_it + r);
         ESC_CUDA(cudaStreamEndCapture(s, &g));
         ESC_CUDA(cudaGraphInstantiate(&ge, g, 0));
         for (int q = 0; q < rounds; q++) ESC_CUDA(cudaGraphLaunch(ge, s));
@@ -264,7 +307,7 @@ void CFBatch<R>::run(cudaStream_t s) {
         cudaGraphDestroy(g);
     } else {
         for (int q = 0; q < rounds; q++)
-            for (int r = 0; r < 3; r++) iteration(r);
+            for (int r = 0; r < 3; r++) iteration(start_it + r);
         ESC_CUDA(cudaStreamSynchronize(s));
     }
 }

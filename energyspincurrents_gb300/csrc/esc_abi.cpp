@@ -10,6 +10,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <type_traits>
 
 #include "esc_internal.h"
 
@@ -363,27 +364,80 @@ int cf_batch_width(esc_handle* h, size_t es, int want) {
 
 // Start vectors must already be in column slots of set 1 of d_cfb.  Returns a (Re alpha),
 // b (b[0] = |phi|) and the number of steps per column.
+//
+// head > 0 (complex64 columns only): the first `head` iterations run on complex128 copies of the
+// columns; the last two vectors are then rounded to complex64 and the recurrence continues in
+// complex64 from iteration `head`.  The leading iterations fix the converged, low-lying poles of
+// the continued fraction, so their rounding in FP32 is what costs accuracy; the tail only adds
+// resolution.  The head needs 3 x ncols complex128 vectors for its duration; without that much
+// free device memory the run is all complex64.
 template <typename R>
 void cf_batch_run(esc_handle* h, int ncols, int kmax, const std::vector<int>& steps, const std::vector<esc::DevModel>& ms,
-                  double tol, bool graph, std::vector<std::vector<double>>& A, std::vector<std::vector<double>>& B) {
-    esc::CFBatch<R> cb;
-    cb.ncols = ncols; cb.kmax = kmax; cb.D = h->D; cb.tol = tol; cb.use_graph = graph;
-    cb.bufs = h->d_cfb;
+                  double tol, bool graph, std::vector<std::vector<double>>& A, std::vector<std::vector<double>>& B,
+                  int head = 0) {
     const size_t nd = (size_t)ncols * esc::CFB_GRID * 2 + (size_t)ncols * kmax * 2 + (size_t)ncols * (kmax + 1);
     ensure_t(h->d_cfs, h->cfs_bytes, nd * sizeof(double));
     ensure_t(h->d_cfi, h->cfi_bytes, (2 * (size_t)ncols + 2) * sizeof(int));
-    cb.d_part = h->d_cfs;
-    cb.d_alpha = cb.d_part + (size_t)ncols * esc::CFB_GRID * 2;
-    cb.d_b2 = cb.d_alpha + (size_t)ncols * kmax * 2;
-    cb.d_active = h->d_cfi;
-    cb.d_steps = h->d_cfi + ncols;
-    cb.d_it = h->d_cfi + 2 * ncols;
-    ESC_CUDA(cudaMemsetAsync(h->d_cfs, 0, nd * sizeof(double), h->stream));
-    ESC_CUDA(cudaMemcpyAsync(cb.d_steps, steps.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, h->stream));
-    const void* dg = diag_for(h, sizeof(R) == 4 ? ESC_C64 : ESC_C128);
-    cb.hv_column = [&](int c, const void* in, void* out, const int* active, cudaStream_t s) {
-        esc::launch_hv_tiled<R>(ms[c], h->passes, in, out, h->D, dg, s, active);
+    auto setup = [&](auto& cb, void* bufs, const void* dg) {
+        typedef typename std::remove_reference<decltype(cb)>::type CB;
+        cb.ncols = ncols; cb.kmax = kmax; cb.D = h->D; cb.tol = tol; cb.use_graph = graph;
+        cb.bufs = bufs;
+        cb.d_part = h->d_cfs;
+        cb.d_alpha = cb.d_part + (size_t)ncols * esc::CFB_GRID * 2;
+        cb.d_b2 = cb.d_alpha + (size_t)ncols * kmax * 2;
+        cb.d_active = h->d_cfi;
+        cb.d_steps = h->d_cfi + ncols;
+        cb.d_it = h->d_cfi + 2 * ncols;
+        typedef typename std::conditional<std::is_same<CB, esc::CFBatch<float>>::value, float, double>::type RR;
+        cb.hv_column = [h, &ms, dg](int c, const void* in, void* out, const int* active, cudaStream_t s) {
+            esc::launch_hv_tiled<RR>(ms[c], h->passes, in, out, h->D, dg, s, active);
+        };
     };
+    ESC_CUDA(cudaMemsetAsync(h->d_cfs, 0, nd * sizeof(double), h->stream));
+    esc::CFBatch<R> cb;
+    setup(cb, h->d_cfb, diag_for(h, sizeof(R) == 4 ? ESC_C64 : ESC_C128));
+    head = std::min(head, kmax);
+    void* dd = nullptr;
+    if (sizeof(R) == 4 && head > 0) {
+        const size_t vs = (size_t)ncols * h->D;   // states per set
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { (void)cudaGetLastError(); fr = 0; }
+        const size_t need = 3 * vs * 16 + (h->d_diag[0] ? 0 : (size_t)h->D * 8);
+        if (fr > need + ((size_t)1 << 30) && cudaMalloc(&dd, 3 * vs * 16) == cudaSuccess) {
+            char* d1 = (char*)dd + vs * 16;
+            esc::launch_convert_c64_to_c128((char*)h->d_cfb + vs * 8, d1, (int64_t)vs, h->stream);
+            std::vector<int> hs(ncols);
+            for (int c = 0; c < ncols; c++) hs[c] = std::min(steps[c], head);
+            ESC_CUDA(cudaMemcpyAsync(cb.d_steps, hs.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+            esc::CFBatch<double> c64;
+            setup(c64, dd, diag_for(h, ESC_C128));
+            c64.run(h->stream);   // synchronises
+            // columns that ran the whole head without stopping continue in complex64
+            std::vector<double> b2((size_t)ncols * (kmax + 1));
+            ESC_CUDA(cudaMemcpy(b2.data(), cb.d_b2, b2.size() * sizeof(double), cudaMemcpyDeviceToHost));
+            std::vector<int> act(ncols, 0);
+            for (int c = 0; c < ncols; c++) {
+                const double b0 = std::sqrt(b2[(size_t)c * (kmax + 1)]);
+                bool live = b0 > 0.0 && steps[c] > head;
+                for (int k = 1; live && k <= head; k++)
+                    if (!(std::sqrt(b2[(size_t)c * (kmax + 1) + k]) > tol * b0)) live = false;
+                act[c] = live ? 1 : 0;
+            }
+            for (int j = 0; j < 2; j++) {
+                const int set = (head + j) % 3;
+                esc::launch_convert_c128_to_c64((char*)dd + set * vs * 16, (char*)h->d_cfb + set * vs * 8, (int64_t)vs,
+                                                h->stream);
+            }
+            ESC_CUDA(cudaMemcpyAsync(cb.d_active, act.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+            sync(h);
+            cudaFree(dd);
+            cb.start_it = head;
+        } else {
+            (void)cudaGetLastError();
+            dd = nullptr;
+        }
+    }
+    ESC_CUDA(cudaMemcpyAsync(cb.d_steps, steps.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, h->stream));
     cb.run(h->stream);
     std::vector<double> al((size_t)ncols * kmax * 2), b2((size_t)ncols * (kmax + 1));
     ESC_CUDA(cudaMemcpyAsync(al.data(), cb.d_alpha, al.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -743,6 +797,7 @@ void spectrum_impl(esc_handle* h, const esc_dyn_cfg& cfg, std::vector<double>& o
 
     // CF resolvents G_A(omega) = <A gs|(z-H)^-1|A gs>, z = omega + E0 - i eta, for a list of
     // operators, run as columns of the batched CF Lanczos (batched.cu)
+    const int head = cfg.fp64_head == 0 ? 48 : std::max(0, cfg.fp64_head);
     auto cf_runs = [&](const std::vector<std::vector<esc::OpTerm>>& ts) {
         std::vector<std::vector<cplx>> G(ts.size());
         const int width = cf_batch_width(h, Pipe<R>::ES, (int)ts.size());
@@ -755,7 +810,7 @@ void spectrum_impl(esc_handle* h, const esc_dyn_cfg& cfg, std::vector<double>& o
             std::vector<int> steps(nc, K);
             std::vector<esc::DevModel> ms(nc, h->dm);
             std::vector<std::vector<double>> A, B;
-            cf_batch_run<R>(h, nc, K, steps, ms, 1e-10, true, A, B);
+            cf_batch_run<R>(h, nc, K, steps, ms, 1e-10, true, A, B, head);
             for (int c = 0; c < nc; c++) {
                 std::vector<cplx> g(nw);
                 for (int k = 0; k < nw; k++)
@@ -807,16 +862,21 @@ void spectrum_impl(esc_handle* h, const esc_dyn_cfg& cfg, std::vector<double>& o
                 el[c] = S.expect(ch[c], 0, d_tmp);
                 runs.push_back(ch[c]);
             }
+            // per pair: the a+b and a+ib resolvents; for JeJe a+b is the total channel t = x+y itself
+            std::vector<std::pair<int, int>> at;
             for (auto pr : pairs) {
-                runs.push_back(combine(ch[pr.first], ch[pr.second], 1.0));
+                int ip = -1;
+                if (je) ip = nc - 1;
+                else { ip = (int)runs.size(); runs.push_back(combine(ch[pr.first], ch[pr.second], 1.0)); }
+                at.push_back({ip, (int)runs.size()});
                 runs.push_back(combine(ch[pr.first], ch[pr.second], cplx(0, 1)));
             }
             auto G = cf_runs(runs);
             for (int c = 0; c < nc; c++) Sab[c][c] = G[c];
             for (size_t q = 0; q < pairs.size(); q++) {
                 const int a = pairs[q].first, b = pairs[q].second;
-                const auto& Sp = G[nc + 2 * q];
-                const auto& Sq = G[nc + 2 * q + 1];
+                const auto& Sp = G[at[q].first];
+                const auto& Sq = G[at[q].second];
                 for (int k = 0; k < nw; k++) {
                     const cplx X = Sp[k] - Sab[a][a][k] - Sab[b][b][k];
                     const cplx Y = Sq[k] - Sab[a][a][k] - Sab[b][b][k];
@@ -1183,11 +1243,32 @@ esc_status esc_spectrum(esc_handle* h, const esc_dyn_cfg* cfg, double* out, int*
     return guarded(h, [&]() {
         std::vector<double> s;
         int nc = 0;
-        // The ground state and the Krylov basis share one precision; CF runs use cfg->dtype only
-        // when there is no basis to match (the GS vector is converted as needed).
+        // Ritz mode runs in the precision of the ground state and its Krylov basis.  CF mode runs
+        // in complex64 when either the ground state or cfg->dtype is complex64; a complex128
+        // ground state is then rounded once to complex64 for the duration of the call.
         const esc_dtype dt = h->basis_dt;
-        if (dt == ESC_C64) spectrum_impl<float>(h, *cfg, s, nc);
-        else spectrum_impl<double>(h, *cfg, s, nc);
+        if (dt == ESC_C64) {
+            spectrum_impl<float>(h, *cfg, s, nc);
+        } else if (cfg->mode == ESC_DYNMODE_CF && cfg->dtype == ESC_C64) {
+            void* g32 = nullptr;
+            ESC_CUDA(cudaMalloc(&g32, (size_t)h->D * 8));
+            esc::launch_convert_c128_to_c64(h->d_gs, g32, h->D, h->stream);
+            void* g64 = h->d_gs;
+            h->d_gs = g32;
+            try {
+                spectrum_impl<float>(h, *cfg, s, nc);
+            } catch (...) {
+                h->d_gs = g64;
+                (void)cudaStreamSynchronize(h->stream);
+                cudaFree(g32);
+                throw;
+            }
+            h->d_gs = g64;
+            sync(h);
+            cudaFree(g32);
+        } else {
+            spectrum_impl<double>(h, *cfg, s, nc);
+        }
         if (nrows) *nrows = cfg->omega_steps + 1;
         if (ncols) *ncols = nc;
         if (out) std::copy(s.begin(), s.end(), out);

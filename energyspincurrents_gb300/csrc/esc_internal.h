@@ -209,10 +209,13 @@ struct CFBatch {
     int* d_active = nullptr;     // ncols
     int* d_it = nullptr;         // 1
     int* d_steps = nullptr;      // ncols (per-column step limit <= kmax)
+    // start_it > 0 continues a recurrence at iteration start_it: prev = set start_it % 3, cur =
+    // set (start_it + 1) % 3, alpha / b2 filled below start_it, active flags set by the caller
+    int start_it = 0;
     std::function<void(int, const void*, void*, const int*, cudaStream_t)> hv_column;
     void run(cudaStream_t s);
 };
-constexpr int CFB_GRID = 304;
+constexpr int CFB_GRID = 1216;   // blocks per column of the batched CF kernels (8 x 152 SMs)
 
 // ---------------------------------------------------------------------------------------------
 // Host numerics

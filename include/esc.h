@@ -115,6 +115,8 @@ typedef struct {
     double domega, eta;
     int cf_steps;               /* continued-fraction Lanczos steps (CF mode)                  */
     esc_dtype dtype;            /* CF mode: precision of the CF Lanczos vectors                */
+    int fp64_head;              /* CF mode, ESC_C64 only: leading CF steps run on complex128   *
+                                 * vectors before the complex64 tail (0: 48, < 0: none)         */
 } esc_dyn_cfg;
 
 /* Batched continued-fraction Lanczos: ncols independent three-term recurrences (no
