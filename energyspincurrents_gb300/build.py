@@ -23,7 +23,7 @@ LIB = os.path.join(OUT, "libesc.so")
 EXE = os.path.join(OUT, "LanczosCond")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kernels.cu", "hv_tiled.cu", "batched.cu"]
+CU_SOURCES = ["kernels.cu", "hv_tiled.cu", "batched.cu", "hv_jit.cu"]
 CPP_SOURCES = ["esc_abi.cpp", "params.cpp", "model.cpp", "numerics.cpp", "planner.cpp"]
 
 
@@ -50,11 +50,27 @@ def _headers():
     return hs + [os.path.join(REPO, "include", "esc.h")]
 
 
+def _embed_device_source():
+    """_build/hv_pass_device.inc: hv_pass_device.cuh as a C++ raw string (the source that the
+    run-time specialisation hands to NVRTC)."""
+    src = os.path.join(CSRC, "hv_pass_device.cuh")
+    dst = os.path.join(OUT, "hv_pass_device.inc")
+    with open(src) as f:
+        body = f.read()
+    if ')ESCSRC"' in body:
+        raise RuntimeError("hv_pass_device.cuh contains the raw-string delimiter")
+    text = 'R"ESCSRC(' + body + ')ESCSRC"\n'
+    if not os.path.exists(dst) or open(dst).read() != text:
+        with open(dst, "w") as f:
+            f.write(text)
+
+
 def build(force=False, verbose=False):
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
     cuda = _cuda_home(nvcc)
-    inc = ["-I", CSRC, "-I", os.path.join(REPO, "include"), "-I", os.path.join(cuda, "include")]
+    _embed_device_source()
+    inc = ["-I", CSRC, "-I", OUT, "-I", os.path.join(REPO, "include"), "-I", os.path.join(cuda, "include")]
     hdrs = _headers()
     jobs = []
     objs = []
@@ -84,7 +100,8 @@ def build(force=False, verbose=False):
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
         list(ex.map(run, jobs))
     if force or jobs or not os.path.exists(LIB):
-        run([nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-Xcompiler", "-fopenmp", "-lgomp"])
+        run([nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-Xcompiler", "-fopenmp", "-lgomp",
+             "-L", os.path.join(cuda, "lib64"), "-lnvrtc", "-Xlinker", "-rpath", "-Xlinker", os.path.join(cuda, "lib64")])
         os.replace(LIB + ".tmp", LIB)
     exe_src = os.path.join(CSRC, "LanczosCond.cpp")
     if os.path.exists(exe_src) and (force or _newer(EXE, [exe_src, LIB] + hdrs)):

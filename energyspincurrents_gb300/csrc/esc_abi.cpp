@@ -607,6 +607,15 @@ esc_status esc_create(const esc_params* p, esc_handle** out) {
         ESC_CUDA(cudaGetDevice(&h->device));
         ESC_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
         ensure_partials(h.get(), 4);
+        // Run-time specialised complex64 passes (hv_jit.cu): ESC_JIT=0 off, =1 on, =require on and
+        // an error if it fails; default on from 2^22 states, where the compile time is repaid.
+        const char* je = std::getenv("ESC_JIT");
+        const bool jit = je ? std::strcmp(je, "0") != 0 : h->D >= (int64_t(1) << 22);
+        if (jit) {
+            std::string err;
+            if (!esc::jit_compile(h->passes, err) && je && std::strcmp(je, "require") == 0)
+                throw Fail(ESC_ERR_CUDA, "run-time specialisation of the H.v passes failed: " + err);
+        }
     });
     if (st != ESC_OK) {
         g_err = h->err;
@@ -1240,6 +1249,13 @@ esc_status esc_spectrum(esc_handle* h, const esc_dyn_cfg* cfg, double* out, int*
     if (cfg->mode == ESC_DYNMODE_RITZ && !h->have_basis)
         return finish(h, ESC_ERR_STATE, "You need to set LancType=All for Dynamical calculations --- you dummy!");
     if (cfg->omega_steps < 0) return finish(h, ESC_ERR_PARAM, "omega_steps must be >= 0");
+    if (!out) {   // size query: nothing is computed
+        const int nc = cfg->kind == ESC_DYN_JEJE ? 6 : cfg->kind == ESC_DYN_JSJS ? 15 : cfg->kind == ESC_DYN_LOCALSZSZ ? 9 : 0;
+        if (!nc) return finish(h, ESC_ERR_PARAM, "Unknown dynstr parameter");
+        if (nrows) *nrows = cfg->omega_steps + 1;
+        if (ncols) *ncols = nc;
+        return finish(h, ESC_OK, "");
+    }
     return guarded(h, [&]() {
         std::vector<double> s;
         int nc = 0;

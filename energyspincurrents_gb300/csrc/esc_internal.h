@@ -119,9 +119,32 @@ struct DevPass {
     // (512 j) under each term mask, bit j
     unsigned int bjpar[MAX_PTERMS];
     unsigned int fjbit[MAX_SITES];
+    // Register-grouped form (complex64 kernel): the terms ordered by their thread-bit mask
+    // (tile-local bits 0..8).  A thread loads the partners of a group once -- its E register
+    // states, with the group's thread bits flipped -- and applies every term of the group from
+    // registers; the term's register-bit mask (local bits 9..) selects the register.
+    int ngroup, nterm;
+    unsigned short glo[MAX_PTERMS + MAX_SITES];   // thread-bit mask of group g
+    unsigned char gnt[MAX_PTERMS + MAX_SITES];    // terms in group g
+    unsigned char gk[MAX_PTERMS + MAX_SITES];     // term code: bond = register mask (0..15); field = 33 + register bit, 32 = thread-bit field
+    float ga[MAX_PTERMS + MAX_SITES], gb[MAX_PTERMS + MAX_SITES];   // bond: ceq, cdiff
+    int jit;   // kernel specialised for this pass at run time (hv_jit.cu), -1: none
 };
 // Builds one DevPass per plan pass from the relabelled model; throws if a term fits no tile.
 std::vector<DevPass> make_passes(const Plan& P, const DevModel& m);
+}  // namespace esc
+namespace escdev { struct PassTab; }
+namespace esc {
+// Run-time specialisation of the complex64 passes (hv_jit.cu): compiles one kernel per eligible
+// pass with its term groups written out, for the current device, and sets DevPass::jit.  Returns
+// false (passes unchanged) with a message if NVRTC or the module load fails.
+bool jit_compile(std::vector<DevPass>& passes, std::string& err);
+// The CUDA source jit_compile hands to NVRTC; which (optional) receives the pass index of each
+// kernel esc_jit_pass<k>.
+std::string jit_source(const std::vector<DevPass>& passes, std::vector<int>* which);
+void jit_launch(const DevPass& p, const escdev::PassTab& pt, const void* diag, const void* in, void* out, int64_t D,
+                int sms, cudaStream_t s, const int* active);
+escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m);
 // diag: precomputed diagonal of the bond terms (no field), R per state (launch_diag); may be NULL,
 // then the diagonal is computed in the kernel.
 // active (optional, device int): the launches do nothing when *active == 0 (batched recurrences).

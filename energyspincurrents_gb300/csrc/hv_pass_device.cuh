@@ -1,0 +1,142 @@
+// hv_pass_device.cuh -- device code of the register-grouped complex64 H.v pass.
+//
+// Shared by the ahead-of-time kernel in hv_tiled.cu (terms read from the pass table at run time)
+// and by the kernels specialised per Hamiltonian at run time in hv_jit.cu (terms compiled in as
+// straight-line code).  It includes nothing, because it is also handed verbatim to NVRTC.
+//
+// A CTA of 512 threads owns one tile of 512 E basis states at a time: thread t holds the states
+// t + 512 j (j < E), i.e. tile-local bits 0..8 are thread bits and bits 9.. are register bits.
+// Tiles are copied global -> shared with cp.async (16 B per copy, runs of 8 consecutive states),
+// double buffered: tile n+1 is in flight while tile n is computed.  Terms come in groups of equal
+// thread-bit mask: a thread loads the E partner states of a group from shared memory once and
+// applies every term of the group from registers.
+#pragma once
+
+namespace escdev {
+
+constexpr int TPB = 512;
+
+// Per-pass tables (kernel parameter).  tabLo / tabHi map the tile-local bits c.. (6 at a time)
+// to global index offsets; rest lists the global bits of the tile number.
+struct PassTab {
+    unsigned long long tabLo[64];
+    unsigned long long tabHi[16];
+    unsigned char rest[40];
+    int nrest, diag, accumulate, N;
+    float fx, fy, fz, pad;   // Bx/2, By/2, Bz/2
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int NPEND>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(NPEND) : "memory"); }
+
+__device__ __forceinline__ unsigned long long tile_bits(const PassTab& p, long long t) {
+    unsigned long long b = 0;
+    for (int q = 0; q < p.nrest; q++) b |= (((unsigned long long)t >> q) & 1ull) << p.rest[q];
+    return b;
+}
+
+// Partners of a group: P[j] = state (t ^ lo) + 512 j of the tile.
+template <int E>
+__device__ __forceinline__ void load_group(const float2* tile, int tid, unsigned lo, float2 (&P)[E]) {
+    const float2* src = tile + (tid ^ (int)lo);
+#pragma unroll
+    for (int j = 0; j < E; j++) P[j] = src[TPB * j];
+}
+
+// parity of the low 4 bits of x
+__host__ __device__ constexpr int par4(int x) { return (x ^ (x >> 1) ^ (x >> 2) ^ (x >> 3)) & 1; }
+
+// Bond term with register mask LMH: acc[j] += c * P[j ^ LMH], c = vA or vB by the parity of the
+// register bits under the mask (vA / vB already swapped for the thread-bit parity).
+template <int E, int LMH>
+__device__ __forceinline__ void gbond(const float2 (&P)[E], float2 vA, float2 vB, float2 (&acc)[E]) {
+#pragma unroll
+    for (int j = 0; j < E; j++) acc[j] = __ffma2_rn(par4(j & LMH) ? vB : vA, P[j ^ LMH], acc[j]);
+}
+
+// Field term on register bit FB (FB < 0: on a thread bit, sign sf = bit ? By/2 : -By/2 of the
+// thread): acc[j] += (Bx/2 + i s) w, s = bit ? By/2 : -By/2.
+template <int E, int FB>
+__device__ __forceinline__ void gfield(const float2 (&P)[E], float2 vfx, float fy, float sf, float2 (&acc)[E]) {
+#pragma unroll
+    for (int j = 0; j < E; j++) {
+        const float2 w = P[FB < 0 ? j : (j ^ (1 << FB))];
+        const float sg = FB < 0 ? sf : (((j >> FB) & 1) ? fy : -fy);
+        acc[j] = __ffma2_rn(vfx, w, acc[j]);
+        acc[j] = __ffma2_rn(make_float2(-sg, sg), make_float2(w.y, w.x), acc[j]);
+    }
+}
+
+// One pass over all tiles.  Terms: functor terms(tile, tid, vfx, fy, acc) adding the off-diagonal
+// terms of the pass for the thread's E states.  diag (pass 1): bond part of the diagonal per state.
+template <int E, class Terms>
+__device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, const float* __restrict__ diag,
+                                          const float2* __restrict__ in, float2* __restrict__ out, long long ntiles,
+                                          const int* __restrict__ active) {
+    if (active && *active == 0) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* bufs = reinterpret_cast<float2*>(smem_raw);   // 2 x (512 E) states
+    __shared__ unsigned long long hi_off[E];
+    const int tid = threadIdx.x;
+    if (tid < E) hi_off[tid] = p.tabHi[tid];
+    const unsigned long long lo = p.tabLo[tid >> 3] | (unsigned long long)(tid & 7);
+    // 16-byte copies: thread t moves states 2t' and 2t'+1, t' = t + 512 i (runs of 8 never split)
+    const unsigned long long lo2 = p.tabLo[(tid >> 2) & 63] | (unsigned long long)((2 * tid) & 7);
+    const int hi2 = tid >> 8;
+    const float2 vfx = make_float2(p.fx, p.fx);
+    const float fy = p.fy, fz = p.fz;
+    __syncthreads();
+    long long t = blockIdx.x;
+    int cur = 0;
+    auto issue = [&](long long tt, float2* dst) {
+        const unsigned long long b2 = tile_bits(p, tt) | lo2;
+#pragma unroll
+        for (int i = 0; i < E / 2; i++) cp_async16(dst + 2 * (tid + TPB * i), in + (b2 | hi_off[hi2 + 2 * i]));
+        cp_async_commit();
+    };
+    if (t < ntiles) issue(t, bufs);
+    for (; t < ntiles; t += gridDim.x, cur ^= 1) {
+        float2* tile = bufs + cur * (TPB * E);
+        const long long tn = t + gridDim.x;
+        if (tn < ntiles) {
+            issue(tn, bufs + (cur ^ 1) * (TPB * E));
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const unsigned long long base = tile_bits(p, t) | lo;
+        float2 acc[E], pre[E];
+        float dpre[E];
+#pragma unroll
+        for (int j = 0; j < E; j++) {
+            acc[j] = make_float2(0.f, 0.f);
+            if (p.diag) dpre[j] = diag[base | hi_off[j]];
+            else if (p.accumulate) pre[j] = out[base | hi_off[j]];
+        }
+        terms(tile, tid, vfx, fy, acc);
+#pragma unroll
+        for (int j = 0; j < E; j++) {
+            const unsigned long long k = base | hi_off[j];
+            float2 o = acc[j];
+            if (p.diag) {
+                const float dg = fmaf(fz, (float)(p.N - 2 * __popcll(k)), dpre[j]);
+                const float2 v = tile[tid + TPB * j];
+                o.x = fmaf(dg, v.x, o.x);
+                o.y = fmaf(dg, v.y, o.y);
+            } else if (p.accumulate) {
+                o.x += pre[j].x;
+                o.y += pre[j].y;
+            }
+            out[k] = o;
+        }
+        __syncthreads();   // buffer `cur` is refilled by the next iteration's prefetch
+    }
+}
+
+}  // namespace escdev

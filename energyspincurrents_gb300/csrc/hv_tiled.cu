@@ -9,10 +9,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
 #include "esc_internal.h"
+#include "hv_pass_device.cuh"
 
 namespace esc {
 
@@ -370,6 +372,86 @@ __global__ void __launch_bounds__(TILE_THREADS, 2) k_hv_pass_f32(const __grid_co
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Register-grouped complex64 pass (device code in hv_pass_device.cuh).  This ahead-of-time
+// instance reads the term groups from the pass table; hv_jit.cu compiles the same pass body
+// with the groups of one Hamiltonian written out as straight-line code.
+// ---------------------------------------------------------------------------------------------
+template <int E>
+__device__ __forceinline__ void gbond_switch(int lmh, const float2 (&P)[E], float2 vA, float2 vB, float2 (&acc)[E]) {
+#define ESC_GB(k)                                                    \
+    case k:                                                          \
+        if constexpr ((k) < E) escdev::gbond<E, (k)>(P, vA, vB, acc); \
+        break;
+    switch (lmh) {
+        ESC_GB(0) ESC_GB(1) ESC_GB(2) ESC_GB(3) ESC_GB(4) ESC_GB(5) ESC_GB(6) ESC_GB(7)
+        ESC_GB(8) ESC_GB(9) ESC_GB(10) ESC_GB(11) ESC_GB(12) ESC_GB(13) ESC_GB(14) ESC_GB(15)
+        default: break;
+    }
+#undef ESC_GB
+}
+template <int E, int FB = -1>
+__device__ __forceinline__ void gfield_dispatch(int fb, const float2 (&P)[E], float2 vfx, float fy, float sf,
+                                                float2 (&acc)[E]) {
+    if constexpr ((1 << (FB + 1)) <= E) {
+        if (fb == FB) escdev::gfield<E, FB>(P, vfx, fy, sf, acc);
+        else gfield_dispatch<E, FB + 1>(fb, P, vfx, fy, sf, acc);
+    }
+}
+
+template <int E>
+struct RuntimeTerms {
+    const DevPass& p;
+    __device__ __forceinline__ void operator()(const float2* tile, int tid, float2 vfx, float fy, float2 (&acc)[E]) const {
+        int q = 0;
+        for (int g = 0; g < p.ngroup; g++) {
+            const unsigned int glo = p.glo[g];
+            float2 P[E];
+            escdev::load_group<E>(tile, tid, glo, P);
+            const bool par = __popc((unsigned)tid & glo) & 1;
+            const float sf = ((unsigned)tid & glo) ? fy : -fy;
+            const int qe = q + p.gnt[g];
+            for (; q < qe; q++) {
+                const int code = p.gk[q];
+                if (code < 32) {
+                    const float a = p.ga[q], b = p.gb[q];
+                    const float2 vA = par ? make_float2(b, b) : make_float2(a, a);
+                    const float2 vB = par ? make_float2(a, a) : make_float2(b, b);
+                    gbond_switch<E>(code, P, vA, vB, acc);
+                } else {
+                    gfield_dispatch<E>(code - 33, P, vfx, fy, sf, acc);
+                }
+            }
+        }
+    }
+};
+
+template <int E>
+__global__ void __launch_bounds__(TILE_THREADS, 2) k_hv_pass_f32g(const __grid_constant__ escdev::PassTab pt,
+                                                                const __grid_constant__ DevPass p,
+                                                                const float* __restrict__ diag,
+                                                                const float2* __restrict__ in,
+                                                                float2* __restrict__ out, long long ntiles,
+                                                                const int* __restrict__ active) {
+    escdev::pass_body<E>(pt, RuntimeTerms<E>{p}, diag, in, out, ntiles, active);
+}
+
+escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m) {
+    escdev::PassTab t;
+    std::memset(&t, 0, sizeof(t));
+    std::memcpy(t.tabLo, p.tabLo, sizeof(t.tabLo));
+    std::memcpy(t.tabHi, p.tabHi, sizeof(t.tabHi));
+    std::memcpy(t.rest, p.rest, sizeof(t.rest));
+    t.nrest = p.nrest;
+    t.diag = p.diag;
+    t.accumulate = p.accumulate;
+    t.N = m.N;
+    t.fx = m.fxf;
+    t.fy = m.fyf;
+    t.fz = m.fzf;
+    return t;
+}
+
 // FP64 energy sweep: sum over one pass of conj(v[k]) (H_pass v)[k], computed in FP64 from a
 // complex64 or complex128 vector, without writing H v.  The passes of a plan add up to
 // <v|H|v>.  One (re, im) partial per CTA (fixed grid: deterministic).
@@ -470,26 +552,69 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
     const int np = (int)P.tiles.size();
     std::vector<DevPass> out(np);
     std::vector<char> bdone(m.nb, 0), fdone(P.N, 0);
+    const bool field = m.fx != 0.0 || m.fy != 0.0;
     for (int pi = 0; pi < np; pi++) {
         DevPass& d = out[pi];
         std::memset(&d, 0, sizeof(d));
-        const std::vector<int>& B = P.tiles[pi];
+        d.jit = -1;
+        std::vector<int> B = P.tiles[pi];
         d.Tp = (int)B.size();
         d.c = std::min(P.c, d.Tp);
         if (d.Tp - d.c > 12) throw std::invalid_argument("tile too large for the run-offset tables");
         unsigned long long tmask = 0;
-        int local_of[64];
-        for (int q = 0; q < 64; q++) local_of[q] = -1;
-        for (int q = 0; q < d.Tp; q++) { tmask |= 1ull << B[q]; local_of[B[q]] = q; }
+        for (int q = 0; q < d.Tp; q++) tmask |= 1ull << B[q];
         for (int q = 0; q < d.c; q++)
             if (B[q] != q) throw std::invalid_argument("tile must contain the lowest c bits");
-        for (int r = 0; r < 64; r++) {
+        // terms of this pass: every bond and field site not taken by an earlier pass
+        std::vector<int> pb, pf;
+        for (int b = 0; b < m.nb; b++)
+            if (!bdone[b] && !(m.b[b].mask & ~tmask)) { pb.push_back(b); bdone[b] = 1; }
+        if (field)
+            for (int s = 0; s < P.N; s++)
+                if (!fdone[s] && ((tmask >> s) & 1ull)) { pf.push_back(s); fdone[s] = 1; }
+        if ((int)pb.size() > MAX_PTERMS) throw std::invalid_argument("too many bonds in one pass");
+        // Register sites: the tile has 2^Tp states over 512 threads, so the top r = Tp - 9 local
+        // bits index a thread's registers.  Pick the r non-shared sites that leave the fewest
+        // distinct thread-bit masks (each costs one shared-memory load per state) and put them last.
+        const int r = std::max(0, d.Tp - 9);
+        if (r > 0 && d.Tp - d.c >= r) {
+            const int nf = d.Tp - d.c;   // free positions c..Tp-1
+            std::vector<int> freeb(B.begin() + d.c, B.end());
+            std::vector<unsigned long long> gm;
+            for (int b : pb) gm.push_back(m.b[b].mask);
+            for (int s : pf) gm.push_back(1ull << s);
+            int best = 1 << 30;
+            unsigned bestsel = 0;
+            for (unsigned sel = 0; sel < (1u << nf); sel++) {
+                if (__builtin_popcount(sel) != r) continue;
+                // local numbering: register sites -> bits Tp-r.., others keep their order
+                unsigned long long regm = 0;
+                for (int q = 0; q < nf; q++)
+                    if ((sel >> q) & 1u) regm |= 1ull << freeb[q];
+                // distinct masks of the non-register part (global masks suffice)
+                std::vector<unsigned long long> g{0ull};
+                for (unsigned long long x : gm) {
+                    const unsigned long long lo = x & ~regm;
+                    if (std::find(g.begin(), g.end(), lo) == g.end()) g.push_back(lo);
+                }
+                if ((int)g.size() < best) { best = (int)g.size(); bestsel = sel; }
+            }
+            std::vector<int> lane, reg;
+            for (int q = 0; q < nf; q++) (((bestsel >> q) & 1u) ? reg : lane).push_back(freeb[q]);
+            B.resize(d.c);
+            B.insert(B.end(), lane.begin(), lane.end());
+            B.insert(B.end(), reg.begin(), reg.end());
+        }
+        int local_of[64];
+        for (int q = 0; q < 64; q++) local_of[q] = -1;
+        for (int q = 0; q < d.Tp; q++) local_of[B[q]] = q;
+        for (int rr = 0; rr < 64; rr++) {
             unsigned long long lo = 0, hi = 0;
             for (int q = 0; q < 6; q++) {
-                if (d.c + q < d.Tp && ((r >> q) & 1)) lo |= 1ull << B[d.c + q];
-                if (d.c + 6 + q < d.Tp && ((r >> q) & 1)) hi |= 1ull << B[d.c + 6 + q];
+                if (d.c + q < d.Tp && ((rr >> q) & 1)) lo |= 1ull << B[d.c + q];
+                if (d.c + 6 + q < d.Tp && ((rr >> q) & 1)) hi |= 1ull << B[d.c + 6 + q];
             }
-            d.tabLo[r] = lo; d.tabHi[r] = hi;
+            d.tabLo[rr] = lo; d.tabHi[rr] = hi;
         }
         d.nrest = 0;
         for (int q = 0; q < P.N; q++) if (!((tmask >> q) & 1ull)) d.rest[d.nrest++] = (unsigned char)q;
@@ -500,9 +625,7 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
         };
         d.diag = (pi == 0);
         d.accumulate = (pi > 0);
-        for (int b = 0; b < m.nb; b++) {
-            if (bdone[b] || (m.b[b].mask & ~tmask)) continue;
-            if (d.nbond >= MAX_PTERMS) throw std::invalid_argument("too many bonds in one pass");
+        for (int b : pb) {
             d.blm[d.nbond] = local(m.b[b].mask);
             d.ceq[d.nbond] = m.b[b].ceq;
             d.cdiff[d.nbond] = m.b[b].cdiff;
@@ -511,17 +634,42 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
             for (int j = 0; j < 32; j++)
                 d.bjpar[d.nbond] |= (unsigned)(__builtin_popcount(((unsigned)j << 9) & d.blm[d.nbond]) & 1) << j;
             d.nbond++;
-            bdone[b] = 1;
         }
-        if (m.fx != 0.0 || m.fy != 0.0)
-            for (int s = 0; s < P.N; s++) {
-                if (fdone[s] || !((tmask >> s) & 1ull)) continue;
-                d.flm[d.nfield] = local(1ull << s);
-                for (int j = 0; j < 32; j++)
-                    d.fjbit[d.nfield] |= (unsigned)((((unsigned)j << 9) & d.flm[d.nfield]) != 0u) << j;
-                d.nfield++;
-                fdone[s] = 1;
-            }
+        for (int s : pf) {
+            d.flm[d.nfield] = local(1ull << s);
+            for (int j = 0; j < 32; j++)
+                d.fjbit[d.nfield] |= (unsigned)((((unsigned)j << 9) & d.flm[d.nfield]) != 0u) << j;
+            d.nfield++;
+        }
+        // register groups: thread-bit mask = local bits 0..8
+        const unsigned lanes = (1u << std::min(d.Tp, 9)) - 1u;
+        std::vector<unsigned> keys;
+        for (int b = 0; b < d.nbond; b++) keys.push_back(d.blm[b] & lanes);
+        for (int f = 0; f < d.nfield; f++) keys.push_back(d.flm[f] & lanes);
+        std::vector<unsigned> order;
+        for (unsigned k : keys)
+            if (std::find(order.begin(), order.end(), k) == order.end()) order.push_back(k);
+        d.ngroup = 0;
+        d.nterm = 0;
+        for (unsigned g : order) {
+            int n = 0;
+            for (int b = 0; b < d.nbond; b++)
+                if ((d.blm[b] & lanes) == g) {
+                    d.gk[d.nterm] = (unsigned char)(d.blm[b] >> 9);
+                    d.ga[d.nterm] = d.ceqf[b];
+                    d.gb[d.nterm] = d.cdifff[b];
+                    d.nterm++; n++;
+                }
+            for (int f = 0; f < d.nfield; f++)
+                if ((d.flm[f] & lanes) == g) {
+                    const unsigned hi = d.flm[f] >> 9;
+                    d.gk[d.nterm] = (unsigned char)(hi ? 33 + (31 - __builtin_clz(hi)) : 32);
+                    d.nterm++; n++;
+                }
+            d.glo[d.ngroup] = (unsigned short)g;
+            d.gnt[d.ngroup] = (unsigned char)n;
+            d.ngroup++;
+        }
     }
     for (int b = 0; b < m.nb; b++)
         if (!bdone[b]) throw std::invalid_argument("plan leaves a bond outside every tile");
@@ -567,6 +715,29 @@ static void run_f32(const DevModel& m, const DevPass& p, const void* diag, const
     ESC_CUDA(cudaGetLastError());
 }
 
+template <int E>
+static void run_f32g(const DevModel& m, const DevPass& p, const void* diag, const void* in, void* out, int64_t D, int sms,
+                     cudaStream_t s, const int* active) {
+    const size_t smem = 2 * (size_t)TILE_THREADS * E * sizeof(float2);   // double buffer
+    if (smem > 48 * 1024)
+        ESC_CUDA(cudaFuncSetAttribute(k_hv_pass_f32g<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass_f32g<E>, TILE_THREADS, smem));
+    const long long ntiles = (long long)(D >> p.Tp);
+    const long long g = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
+    k_hv_pass_f32g<E><<<(unsigned)g, TILE_THREADS, smem, s>>>(make_pass_tab(p, m), p, (const float*)diag,
+                                                              (const float2*)in, (float2*)out, ntiles, active);
+    ESC_CUDA(cudaGetLastError());
+}
+
+static int kernel_variant() {
+    static int v = [] {
+        const char* e = std::getenv("ESC_HV_KERNEL");
+        return e ? std::atoi(e) : 0;
+    }();
+    return v;
+}
+
 template <typename R>
 void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in, void* out, int64_t D,
                      const void* diag, cudaStream_t s, const int* active) {
@@ -576,6 +747,15 @@ void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, cons
     ESC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     for (const DevPass& p : passes) {
         if constexpr (sizeof(R) == 4) {
+            if (diag && p.jit >= 0 && kernel_variant() == 0) {
+                jit_launch(p, make_pass_tab(p, m), diag, in, out, D, sms, s, active);
+                continue;
+            }
+            if (diag && p.c == 3 && (p.Tp == 11 || p.Tp == 12) && kernel_variant() != 1) {
+                if (p.Tp == 11) run_f32g<4>(m, p, diag, in, out, D, sms, s, active);
+                else run_f32g<8>(m, p, diag, in, out, D, sms, s, active);
+                continue;
+            }
             if (diag && p.c == 3 && p.Tp >= 11 && p.Tp <= 13) {
                 switch (p.Tp) {
                     case 11: run_f32<4>(m, p, diag, in, out, D, sms, s, active); break;

@@ -361,3 +361,22 @@ def test_grad_spectrum_vs_central_differences(kind):
     fd = np.stack(fd, 1)
     scale = max(1.0, np.abs(fd).max())
     assert np.abs(dS - fd).max() <= 1e-5 * scale, (np.abs(dS - fd).max(), scale)
+
+
+@pytest.mark.parametrize("shape,tile_bits", [((3, 6), 12), ((4, 4), 11), ((3, 8), 12)])
+def test_runtime_specialised_passes_bitwise_equal(shape, tile_bits, monkeypatch):
+    """The complex64 passes compiled at run time with the Hamiltonian's terms written out (NVRTC)
+    give bit-identical H.v to the ahead-of-time register-grouped kernel, and agree with the oracle."""
+    monkeypatch.setenv("ESC_TILE_BITS", str(tile_bits))
+    Lx, Ly = shape
+    p = kitaev(Lx=Lx, Ly=Ly, J=0.1)
+    monkeypatch.setenv("ESC_JIT", "require")
+    hj = esc.Handle(p)
+    monkeypatch.setenv("ESC_JIT", "0")
+    ha = esc.Handle(p)
+    x = O.random_start(5, ha.D, normalize=False).astype(np.complex64)
+    yj, ya = hj.hv(x), ha.hv(x)
+    assert np.array_equal(yj, ya)
+    if ha.N <= 18:
+        m = O.Model("Kitaev", Lx, Ly, 1, 1, -1.0, -1.0, -1.0, p["Bxx"], p["Byy"], p["Bzz"], 0.1, 4, False)
+        assert relerr(yj.astype(np.complex128), m.hv(x.astype(np.complex128))) < 2e-6
