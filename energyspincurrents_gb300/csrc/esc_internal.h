@@ -145,6 +145,8 @@ std::string jit_source(const std::vector<DevPass>& passes, std::vector<int>* whi
 void jit_launch(const DevPass& p, const escdev::PassTab& pt, const void* diag, const void* in, void* out, int64_t D,
                 int sms, cudaStream_t s, const int* active);
 escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m);
+// Tile buffers per CTA of the complex64 passes (2; ESC_STAGES=3 for three).
+int pass_stages();
 // diag: precomputed diagonal of the bond terms (no field), R per state (launch_diag); may be NULL,
 // then the diagonal is computed in the kernel.
 // active (optional, device int): the launches do nothing when *active == 0 (batched recurrences).

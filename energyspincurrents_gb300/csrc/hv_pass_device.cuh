@@ -74,13 +74,16 @@ __device__ __forceinline__ void gfield(const float2 (&P)[E], float2 vfx, float f
 
 // One pass over all tiles.  Terms: functor terms(tile, tid, vfx, fy, acc) adding the off-diagonal
 // terms of the pass for the thread's E states.  diag (pass 1): bond part of the diagonal per state.
-template <int E, class Terms>
+// NS-stage ring of tile buffers: tiles t + g, ..., t + (NS-1) g are in flight while tile t is
+// computed (g = grid size); every iteration commits exactly one cp.async group (possibly empty),
+// so wait_group<NS-1> always means "tile t has landed".
+template <int E, int NS, class Terms>
 __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, const float* __restrict__ diag,
                                           const float2* __restrict__ in, float2* __restrict__ out, long long ntiles,
                                           const int* __restrict__ active) {
     if (active && *active == 0) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2* bufs = reinterpret_cast<float2*>(smem_raw);   // 2 x (512 E) states
+    float2* bufs = reinterpret_cast<float2*>(smem_raw);   // NS x (512 E) states
     __shared__ unsigned long long hi_off[E];
     const int tid = threadIdx.x;
     if (tid < E) hi_off[tid] = p.tabHi[tid];
@@ -91,25 +94,24 @@ __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, 
     const float2 vfx = make_float2(p.fx, p.fx);
     const float fy = p.fy, fz = p.fz;
     __syncthreads();
-    long long t = blockIdx.x;
-    int cur = 0;
-    auto issue = [&](long long tt, float2* dst) {
-        const unsigned long long b2 = tile_bits(p, tt) | lo2;
+    const long long g = gridDim.x;
+    auto issue = [&](long long tt, int slot) {
+        if (tt < ntiles) {
+            float2* dst = bufs + slot * (TPB * E);
+            const unsigned long long b2 = tile_bits(p, tt) | lo2;
 #pragma unroll
-        for (int i = 0; i < E / 2; i++) cp_async16(dst + 2 * (tid + TPB * i), in + (b2 | hi_off[hi2 + 2 * i]));
+            for (int i = 0; i < E / 2; i++) cp_async16(dst + 2 * (tid + TPB * i), in + (b2 | hi_off[hi2 + 2 * i]));
+        }
         cp_async_commit();
     };
-    if (t < ntiles) issue(t, bufs);
-    for (; t < ntiles; t += gridDim.x, cur ^= 1) {
-        float2* tile = bufs + cur * (TPB * E);
-        const long long tn = t + gridDim.x;
-        if (tn < ntiles) {
-            issue(tn, bufs + (cur ^ 1) * (TPB * E));
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
+    long long t = blockIdx.x;
+#pragma unroll
+    for (int s = 0; s < NS - 1; s++) issue(t + s * g, s);
+    for (int cur = 0; t < ntiles; t += g, cur = (cur + 1 == NS ? 0 : cur + 1)) {
+        issue(t + (NS - 1) * g, cur == 0 ? NS - 1 : cur - 1);
+        cp_async_wait<NS - 1>();
         __syncthreads();
+        float2* tile = bufs + cur * (TPB * E);
         const unsigned long long base = tile_bits(p, t) | lo;
         float2 acc[E], pre[E];
         float dpre[E];
@@ -135,8 +137,9 @@ __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, 
             }
             out[k] = o;
         }
-        __syncthreads();   // buffer `cur` is refilled by the next iteration's prefetch
+        __syncthreads();   // buffer `cur` is refilled by a later iteration's prefetch
     }
+    cp_async_wait<0>();
 }
 
 }  // namespace escdev

@@ -426,14 +426,14 @@ struct RuntimeTerms {
     }
 };
 
-template <int E>
+template <int E, int NS>
 __global__ void __launch_bounds__(TILE_THREADS, 2) k_hv_pass_f32g(const __grid_constant__ escdev::PassTab pt,
                                                                 const __grid_constant__ DevPass p,
                                                                 const float* __restrict__ diag,
                                                                 const float2* __restrict__ in,
                                                                 float2* __restrict__ out, long long ntiles,
                                                                 const int* __restrict__ active) {
-    escdev::pass_body<E>(pt, RuntimeTerms<E>{p}, diag, in, out, ntiles, active);
+    escdev::pass_body<E, NS>(pt, RuntimeTerms<E>{p}, diag, in, out, ntiles, active);
 }
 
 escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m) {
@@ -551,8 +551,50 @@ template void launch_energy<double>(const DevModel&, const std::vector<DevPass>&
 std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
     const int np = (int)P.tiles.size();
     std::vector<DevPass> out(np);
-    std::vector<char> bdone(m.nb, 0), fdone(P.N, 0);
     const bool field = m.fx != 0.0 || m.fy != 0.0;
+    // Term -> pass assignment.  Default: a bond or field goes to the first pass whose tile holds
+    // it.  ESC_PASS_BALANCE=1: most constrained term first, each to the eligible pass with the
+    // fewest terms so far.
+    std::vector<unsigned long long> tm(np, 0);
+    for (int pi = 0; pi < np; pi++)
+        for (int b : P.tiles[pi]) tm[pi] |= 1ull << b;
+    std::vector<std::vector<int>> passb(np), passf(np);
+    {
+        struct Term { unsigned long long mask; int id; bool bond; };
+        std::vector<Term> terms;
+        for (int b = 0; b < m.nb; b++) terms.push_back({m.b[b].mask, b, true});
+        if (field)
+            for (int s = 0; s < P.N; s++) terms.push_back({1ull << s, s, false});
+        auto elig = [&](unsigned long long mk) {
+            std::vector<int> e;
+            for (int pi = 0; pi < np; pi++) if (!(mk & ~tm[pi])) e.push_back(pi);
+            return e;
+        };
+        const char* be = std::getenv("ESC_PASS_BALANCE");
+        const bool balance = be && std::atoi(be) == 1;
+        std::vector<int> order(terms.size()), load(np, 0);
+        for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
+        if (balance)
+            std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+                return elig(terms[a].mask).size() < elig(terms[b].mask).size();
+            });
+        for (int i : order) {
+            const std::vector<int> e = elig(terms[i].mask);
+            if (e.empty()) {
+                if (terms[i].bond) throw std::invalid_argument("plan leaves a bond outside every tile");
+                continue;
+            }
+            int pick = e[0];
+            if (balance)
+                for (int pi : e) if (load[pi] < load[pick]) pick = pi;
+            load[pick]++;
+            (terms[i].bond ? passb : passf)[pick].push_back(terms[i].id);
+        }
+        for (int pi = 0; pi < np; pi++) {
+            std::sort(passb[pi].begin(), passb[pi].end());
+            std::sort(passf[pi].begin(), passf[pi].end());
+        }
+    }
     for (int pi = 0; pi < np; pi++) {
         DevPass& d = out[pi];
         std::memset(&d, 0, sizeof(d));
@@ -565,13 +607,8 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
         for (int q = 0; q < d.Tp; q++) tmask |= 1ull << B[q];
         for (int q = 0; q < d.c; q++)
             if (B[q] != q) throw std::invalid_argument("tile must contain the lowest c bits");
-        // terms of this pass: every bond and field site not taken by an earlier pass
-        std::vector<int> pb, pf;
-        for (int b = 0; b < m.nb; b++)
-            if (!bdone[b] && !(m.b[b].mask & ~tmask)) { pb.push_back(b); bdone[b] = 1; }
-        if (field)
-            for (int s = 0; s < P.N; s++)
-                if (!fdone[s] && ((tmask >> s) & 1ull)) { pf.push_back(s); fdone[s] = 1; }
+        const std::vector<int>& pb = passb[pi];
+        const std::vector<int>& pf = passf[pi];
         if ((int)pb.size() > MAX_PTERMS) throw std::invalid_argument("too many bonds in one pass");
         // Register sites: the tile has 2^Tp states over 512 threads, so the top r = Tp - 9 local
         // bits index a thread's registers.  Pick the r non-shared sites that leave the fewest
@@ -671,8 +708,6 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
             d.ngroup++;
         }
     }
-    for (int b = 0; b < m.nb; b++)
-        if (!bdone[b]) throw std::invalid_argument("plan leaves a bond outside every tile");
     return out;
 }
 
@@ -715,19 +750,27 @@ static void run_f32(const DevModel& m, const DevPass& p, const void* diag, const
     ESC_CUDA(cudaGetLastError());
 }
 
-template <int E>
+template <int E, int NS>
 static void run_f32g(const DevModel& m, const DevPass& p, const void* diag, const void* in, void* out, int64_t D, int sms,
                      cudaStream_t s, const int* active) {
-    const size_t smem = 2 * (size_t)TILE_THREADS * E * sizeof(float2);   // double buffer
-    if (smem > 48 * 1024)
-        ESC_CUDA(cudaFuncSetAttribute(k_hv_pass_f32g<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem = (size_t)NS * TILE_THREADS * E * sizeof(float2);   // NS-stage ring of tiles
+    // always raised: dynamic + static shared memory may pass 48 KB even when the ring alone does not
+    ESC_CUDA(cudaFuncSetAttribute(k_hv_pass_f32g<E, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass_f32g<E>, TILE_THREADS, smem));
+    ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass_f32g<E, NS>, TILE_THREADS, smem));
     const long long ntiles = (long long)(D >> p.Tp);
     const long long g = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
-    k_hv_pass_f32g<E><<<(unsigned)g, TILE_THREADS, smem, s>>>(make_pass_tab(p, m), p, (const float*)diag,
-                                                              (const float2*)in, (float2*)out, ntiles, active);
+    k_hv_pass_f32g<E, NS><<<(unsigned)g, TILE_THREADS, smem, s>>>(make_pass_tab(p, m), p, (const float*)diag,
+                                                                  (const float2*)in, (float2*)out, ntiles, active);
     ESC_CUDA(cudaGetLastError());
+}
+
+int pass_stages() {
+    static int v = [] {
+        const char* e = std::getenv("ESC_STAGES");
+        return e && std::atoi(e) == 3 ? 3 : 2;
+    }();
+    return v;
 }
 
 static int kernel_variant() {
@@ -752,8 +795,11 @@ void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, cons
                 continue;
             }
             if (diag && p.c == 3 && (p.Tp == 11 || p.Tp == 12) && kernel_variant() != 1) {
-                if (p.Tp == 11) run_f32g<4>(m, p, diag, in, out, D, sms, s, active);
-                else run_f32g<8>(m, p, diag, in, out, D, sms, s, active);
+                const bool two = pass_stages() == 2;   // measured: 2 stages keep 2 CTAs per SM and win
+                if (p.Tp == 11) two ? run_f32g<4, 2>(m, p, diag, in, out, D, sms, s, active)
+                                : run_f32g<4, 3>(m, p, diag, in, out, D, sms, s, active);
+                else two ? run_f32g<8, 2>(m, p, diag, in, out, D, sms, s, active)
+                         : run_f32g<8, 3>(m, p, diag, in, out, D, sms, s, active);
                 continue;
             }
             if (diag && p.c == 3 && p.Tp >= 11 && p.Tp <= 13) {
