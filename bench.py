@@ -254,15 +254,20 @@ def main():
     gbs_total = world * algo_bytes / (ms * 1e-3) / 1e9
     kernel_gbs = algo_bytes / (ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
-    prof = traffic_from_profile()
-    traffic = None
-    if prof and prof.get("bytes_per_state"):
-        traffic = int(prof["bytes_per_state"] * D)
+    prof = traffic_from_profile() or {}
+    traffic, tsrc = None, None
+    meas = prof.get("measured_bytes_per_hv", {})
+    if str(args.sites) in meas:
+        traffic, tsrc = int(meas[str(args.sites)]), prof.get("source")
+    elif prof.get("first_pass_bytes_per_state"):
+        # per-pass DRAM bytes per state measured on a smaller cluster, scaled by the states and
+        # passes of this one (pass 1 reads v and the bond diagonal, later passes v and the partial)
+        traffic = int(D * (prof["first_pass_bytes_per_state"] + (npasses - 1) * prof["later_pass_bytes_per_state"]))
+        tsrc = prof.get("source") + f", scaled to 2^{args.sites} states and {npasses} passes"
     roof = {"bound": "hbm", "achieved": round(kernel_gbs, 1), "peak": peak, "unit": "GB/s",
             "frac": round(kernel_gbs / peak, 4), "peak_source": peak_kind, "traffic": traffic,
-            "kernel": "k_hv_pass_f32 (all passes of one H.v)", "passes": npasses,
-            "algorithmic_bytes_per_launch": algo_bytes,
-            "traffic_source": (prof or {}).get("source")}
+            "kernel": "esc_jit_pass* (run-time specialised complex64 passes of one H.v)", "passes": npasses,
+            "algorithmic_bytes_per_launch": algo_bytes, "traffic_source": tsrc}
     del v, out
     torch.cuda.empty_cache()
 
