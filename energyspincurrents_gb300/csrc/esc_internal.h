@@ -163,6 +163,8 @@ template <typename R> void launch_axpy_dev(const void* x, void* y, const double*
 // Basis permutation: out[j] = in[src(j)], src assembled bitwise from five 8-bit tables.
 struct DevPerm {
     unsigned long long tab[5][256];
+    int N;
+    signed char sb[MAX_SITES];   // src bit of each dst bit
 };
 DevPerm make_perm_table(const std::vector<int>& bit_of_src_bit);   // tab maps dst index bits -> src index
 template <typename R> void launch_permute(const DevPerm& p, const void* in, void* out, int64_t D, cudaStream_t s);
