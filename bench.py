@@ -197,6 +197,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-spectrum", action="store_true")
+    ap.add_argument("--autotune-report", action="store_true",
+                    help="print the self-tuner's timing of every H.v variant for --sites and exit (no JSON line)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -211,6 +213,9 @@ def main():
     build.build()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    if args.autotune_report:
+        print(esc.Handle(workload(args.sites)).autotune(), end="")
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist

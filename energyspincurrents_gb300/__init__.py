@@ -75,7 +75,7 @@ _lib = None
 # every symbol declared in include/esc.h
 EXPORTS = ["esc_params_default", "esc_params_from_file", "esc_lattice", "esc_plan", "esc_create", "esc_destroy", "esc_last_error",
            "esc_num_sites", "esc_dim", "esc_neighbors", "esc_basis_permutation", "esc_stream", "esc_hv", "esc_hv_batched", "esc_apply_op",
-           "esc_start_vector", "esc_rayleigh", "esc_rayleigh_noalloc", "esc_lanczos_gs", "esc_cf_batched", "esc_spectrum", "esc_measure_local", "esc_grad"]
+           "esc_start_vector", "esc_rayleigh", "esc_rayleigh_noalloc", "esc_lanczos_gs", "esc_cf_batched", "esc_spectrum", "esc_measure_local", "esc_grad", "esc_autotune"]
 
 
 def lib_path():
@@ -117,6 +117,7 @@ def lib():
     L.esc_cf_batched.argtypes = [vp, P(CFBatchCfg), vp, i64, ci, vp, vp, vp]
     L.esc_measure_local.argtypes = [vp, vp, vp]
     L.esc_grad.argtypes = [vp, P(DynCfg), vp, vp]
+    L.esc_autotune.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     _lib = L
     return L
 
@@ -314,6 +315,13 @@ class Handle:
         _check(self.h, lib().esc_cf_batched(self.h, ctypes.byref(cfg), _ptr(V), V.shape[1], flags, _ptr(a), _ptr(b),
                                             _ptr(lens)))
         return [(a[c, : lens[c]], b[c, : lens[c] + 1]) for c in range(nc)]
+
+    def autotune(self):
+        """Times the complex64 H.v variants for this Hamiltonian and keeps the fastest; returns the
+        report (one line per candidate, then the choice)."""
+        buf = ctypes.create_string_buffer(8192)
+        _check(self.h, lib().esc_autotune(self.h, buf, len(buf)))
+        return buf.value.decode()
 
     def spectrum(self, kind, mode="Ritz", omega_steps=None, domega=None, eta=None, cf_steps=0, dtype=None,
                  fp64_head=0):

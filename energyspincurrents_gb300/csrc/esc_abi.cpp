@@ -9,6 +9,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <sstream>
 #include <string>
 #include <type_traits>
 
@@ -566,6 +567,125 @@ struct CFSet {
 // =============================================================================================
 // C ABI
 // =============================================================================================
+namespace {
+
+std::vector<std::pair<int, int>> bond_pairs(const esc_handle* h) {
+    std::vector<std::pair<int, int>> pairs;
+    for (const auto& b : h->bonds)
+        if (b.kx - b.ky != 0.0 || b.kx + b.ky != 0.0) pairs.push_back({b.i, b.j});
+    return pairs;
+}
+
+// Installs a site relabelling + pass plan: relabelled model, passes, basis permutations.  The
+// bond diagonal depends on the relabelling, so cached diagonal vectors are dropped.
+void install_plan(esc_handle* h, const esc::Plan& plan, int balance, int stages) {
+    h->plan = plan;
+    std::vector<esc::Bond> rb(h->bonds);
+    for (auto& b : rb) { b.i = h->plan.perm[b.i]; b.j = h->plan.perm[b.j]; }
+    h->dm = esc::make_dev_model(h->p, h->L, rb, h->p.Bxx, h->p.Byy, h->p.Bzz);
+    h->passes = esc::make_passes(h->plan, h->dm, balance, stages);
+    std::vector<int> inv(h->N), fwd(h->N);
+    for (int s = 0; s < h->N; s++) { inv[h->plan.perm[s]] = s; fwd[s] = h->plan.perm[s]; }
+    h->to_int = esc::make_perm_table(inv);    // internal bit b reads reference bit inv[b]
+    h->to_ref = esc::make_perm_table(fwd);    // reference bit s reads internal bit perm[s]
+    for (int i = 0; i < 2; i++)
+        if (h->d_diag[i]) {
+            cudaFree(h->d_diag[i]);
+            h->d_diag[i] = nullptr;
+            h->diag_bytes[i] = 0;
+        }
+}
+
+// Run-time specialised complex64 passes (hv_jit.cu): ESC_JIT=0 off, =1 on, =require on and an
+// error if it fails; by default on from 2^22 states, where the compile time is repaid.
+void specialise(esc_handle* h, std::vector<esc::DevPass>& passes, int force = -1) {
+    const char* je = std::getenv("ESC_JIT");
+    bool jit = je ? std::strcmp(je, "0") != 0 : h->D >= (int64_t(1) << 22);
+    if (force >= 0) jit = force == 1;
+    if (!jit) return;
+    std::string err;
+    if (!esc::jit_compile(passes, err) && je && std::strcmp(je, "require") == 0)
+        throw Fail(ESC_ERR_CUDA, "run-time specialisation of the H.v passes failed: " + err);
+}
+
+// Self-tuning of the complex64 H.v: times one H.v (after one warm-up, median of 3, CUDA events
+// on the handle's stream) for each candidate -- tile bits T in {11, 12, 13}, ahead-of-time vs
+// run-time specialised passes, 2 vs 3 tile buffers, first-fit vs balanced term assignment -- and
+// installs the fastest.  Plans are built once per T.  The candidates compute the same H.v (the
+// tests hold every variant to the oracle); only their speed differs.  Needs two complex64
+// vectors of scratch; refuses once a ground state exists (its basis order would change).
+std::string autotune(esc_handle* h, std::vector<double>* times) {
+    if (h->have_gs) throw Fail(ESC_ERR_STATE, "autotune before the first Lanczos run (it may relabel the basis)");
+    const int64_t D = h->D;
+    void* buf = nullptr;
+    ESC_CUDA(cudaMalloc(&buf, (size_t)D * 16));
+    void* v = buf;
+    void* w = (char*)buf + (size_t)D * 8;
+    esc::launch_start_normal<float>(12345, v, D, h->stream);
+    cudaEvent_t e0, e1;
+    ESC_CUDA(cudaEventCreate(&e0));
+    ESC_CUDA(cudaEventCreate(&e1));
+    struct Cand { int T, jit, stages, balance; double ms; };
+    std::vector<Cand> cands;
+    std::ostringstream rep;
+    const esc::Plan keep = h->plan;
+    const std::vector<esc::DevPass> keep_passes = h->passes;
+    double best = 1e300;
+    Cand bc{};
+    esc::Plan bplan;
+    try {
+        for (int T : {11, 12, 13}) {
+            if (T > h->N) continue;
+            const esc::Plan plan = esc::make_plan(h->N, bond_pairs(h), T, 3, 200);
+            for (int balance : {0, 1})
+                for (int stages : {2, 3})
+                    for (int jit : {0, 1}) {
+                        if (jit && T == 13) continue;   // no specialised kernel for 8192-state tiles
+                        install_plan(h, plan, balance, stages);
+                        if (jit) specialise(h, h->passes, 1);
+                        bool spec = false;
+                        for (const auto& ps : h->passes) spec = spec || ps.jit >= 0;
+                        if (jit && !spec) continue;
+                        const void* dg = diag_for(h, ESC_C64);
+                        esc::launch_hv_tiled<float>(h->dm, h->passes, v, w, D, dg, h->stream);
+                        std::vector<float> ms(3);
+                        for (float& x : ms) {
+                            ESC_CUDA(cudaEventRecord(e0, h->stream));
+                            esc::launch_hv_tiled<float>(h->dm, h->passes, v, w, D, dg, h->stream);
+                            ESC_CUDA(cudaEventRecord(e1, h->stream));
+                            ESC_CUDA(cudaEventSynchronize(e1));
+                            ESC_CUDA(cudaEventElapsedTime(&x, e0, e1));
+                        }
+                        std::sort(ms.begin(), ms.end());
+                        const Cand c{T, jit, stages, balance, ms[1]};
+                        cands.push_back(c);
+                        rep << "T=" << T << " passes=" << plan.tiles.size() << " jit=" << jit << " stages=" << stages
+                            << " balance=" << balance << ": " << ms[1] << " ms\n";
+                        if (c.ms < best) { best = c.ms; bc = c; bplan = plan; }
+                    }
+        }
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(buf);
+        install_plan(h, keep, -1, 0);
+        h->passes = keep_passes;
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    install_plan(h, bplan, bc.balance, bc.stages);
+    if (bc.jit) specialise(h, h->passes, 1);
+    rep << "chosen: T=" << bc.T << " jit=" << bc.jit << " stages=" << bc.stages << " balance=" << bc.balance << " ("
+        << bc.ms << " ms)\n";
+    if (times)
+        for (const auto& c : cands) times->push_back(c.ms);
+    return rep.str();
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* esc_last_error(const esc_handle* h) { return h ? h->err.c_str() : g_err.c_str(); }
@@ -582,22 +702,10 @@ esc_status esc_create(const esc_params* p, esc_handle** out) {
         esc::build_bonds(*p, h->L, h->bonds);
         h->N = h->L.N;
         h->D = int64_t(1) << h->N;
-        // site relabelling and pass plan of the tiled H.v (planner.cpp)
-        std::vector<std::pair<int, int>> pairs;
-        for (const auto& b : h->bonds)
-            if (b.kx - b.ky != 0.0 || b.kx + b.ky != 0.0) pairs.push_back({b.i, b.j});
         int T = 12, c = 3;
         if (const char* e = std::getenv("ESC_TILE_BITS")) T = std::atoi(e);
         if (const char* e = std::getenv("ESC_TILE_LOW")) c = std::atoi(e);
-        h->plan = esc::make_plan(h->N, pairs, T, c, 200);
-        std::vector<esc::Bond> rb(h->bonds);
-        for (auto& b : rb) { b.i = h->plan.perm[b.i]; b.j = h->plan.perm[b.j]; }
-        h->dm = esc::make_dev_model(*p, h->L, rb, p->Bxx, p->Byy, p->Bzz);
-        h->passes = esc::make_passes(h->plan, h->dm);
-        std::vector<int> inv(h->N), fwd(h->N);
-        for (int s = 0; s < h->N; s++) { inv[h->plan.perm[s]] = s; fwd[s] = h->plan.perm[s]; }
-        h->to_int = esc::make_perm_table(inv);    // internal bit b reads reference bit inv[b]
-        h->to_ref = esc::make_perm_table(fwd);    // reference bit s reads internal bit perm[s]
+        install_plan(h.get(), esc::make_plan(h->N, bond_pairs(h.get()), T, c, 200), -1, 0);
         int ndev = 0;
         cudaError_t e = cudaGetDeviceCount(&ndev);
         if (e != cudaSuccess || ndev == 0) {
@@ -607,15 +715,9 @@ esc_status esc_create(const esc_params* p, esc_handle** out) {
         ESC_CUDA(cudaGetDevice(&h->device));
         ESC_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
         ensure_partials(h.get(), 4);
-        // Run-time specialised complex64 passes (hv_jit.cu): ESC_JIT=0 off, =1 on, =require on and
-        // an error if it fails; default on from 2^22 states, where the compile time is repaid.
-        const char* je = std::getenv("ESC_JIT");
-        const bool jit = je ? std::strcmp(je, "0") != 0 : h->D >= (int64_t(1) << 22);
-        if (jit) {
-            std::string err;
-            if (!esc::jit_compile(h->passes, err) && je && std::strcmp(je, "require") == 0)
-                throw Fail(ESC_ERR_CUDA, "run-time specialisation of the H.v passes failed: " + err);
-        }
+        specialise(h.get(), h->passes);
+        if (const char* e = std::getenv("ESC_AUTOTUNE"))
+            if (std::atoi(e) == 1) autotune(h.get(), nullptr);
     });
     if (st != ESC_OK) {
         g_err = h->err;
@@ -624,6 +726,18 @@ esc_status esc_create(const esc_params* p, esc_handle** out) {
     }
     *out = h.release();
     return ESC_OK;
+}
+
+esc_status esc_autotune(esc_handle* h, char* report, size_t report_len) {
+    if (!h) return finish(h, ESC_ERR_PARAM, "null argument");
+    return guarded(h, [&]() {
+        const std::string r = autotune(h, nullptr);
+        if (report && report_len) {
+            const size_t n = std::min(report_len - 1, r.size());
+            std::memcpy(report, r.data(), n);
+            report[n] = 0;
+        }
+    });
 }
 
 esc_status esc_destroy(esc_handle* h) {

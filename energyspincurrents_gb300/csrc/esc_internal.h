@@ -128,10 +128,13 @@ struct DevPass {
     unsigned char gnt[MAX_PTERMS + MAX_SITES];    // terms in group g
     unsigned char gk[MAX_PTERMS + MAX_SITES];     // term code: bond = register mask (0..15); field = 33 + register bit, 32 = thread-bit field
     float ga[MAX_PTERMS + MAX_SITES], gb[MAX_PTERMS + MAX_SITES];   // bond: ceq, cdiff
-    int jit;   // kernel specialised for this pass at run time (hv_jit.cu), -1: none
+    int jit;      // kernel specialised for this pass at run time (hv_jit.cu), -1: none
+    int stages;   // tile buffers per CTA of the complex64 pass (2 or 3)
 };
 // Builds one DevPass per plan pass from the relabelled model; throws if a term fits no tile.
-std::vector<DevPass> make_passes(const Plan& P, const DevModel& m);
+// balance: term -> pass assignment (0 first eligible pass, 1 balanced, -1 from ESC_PASS_BALANCE);
+// stages: tile buffers of the complex64 passes (0: from ESC_STAGES, default 2).
+std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance = -1, int stages = 0);
 }  // namespace esc
 namespace escdev { struct PassTab; }
 namespace esc {
@@ -145,7 +148,7 @@ std::string jit_source(const std::vector<DevPass>& passes, std::vector<int>* whi
 void jit_launch(const DevPass& p, const escdev::PassTab& pt, const void* diag, const void* in, void* out, int64_t D,
                 int sms, cudaStream_t s, const int* active);
 escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m);
-// Tile buffers per CTA of the complex64 passes (2; ESC_STAGES=3 for three).
+// Default tile buffers per CTA of the complex64 passes (2; ESC_STAGES=3 for three).
 int pass_stages();
 // diag: precomputed diagonal of the bond terms (no field), R per state (launch_diag); may be NULL,
 // then the diagonal is computed in the kernel.

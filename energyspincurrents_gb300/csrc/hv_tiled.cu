@@ -548,7 +548,7 @@ template void launch_energy<float>(const DevModel&, const std::vector<DevPass>&,
 template void launch_energy<double>(const DevModel&, const std::vector<DevPass>&, const void*, int64_t, double*, int,
                                     std::vector<double>&, cudaStream_t);
 
-std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
+std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_opt, int stages) {
     const int np = (int)P.tiles.size();
     std::vector<DevPass> out(np);
     const bool field = m.fx != 0.0 || m.fy != 0.0;
@@ -571,7 +571,7 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
             return e;
         };
         const char* be = std::getenv("ESC_PASS_BALANCE");
-        const bool balance = be && std::atoi(be) == 1;
+        const bool balance = balance_opt >= 0 ? balance_opt == 1 : (be && std::atoi(be) == 1);
         std::vector<int> order(terms.size()), load(np, 0);
         for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
         if (balance)
@@ -599,6 +599,7 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m) {
         DevPass& d = out[pi];
         std::memset(&d, 0, sizeof(d));
         d.jit = -1;
+        d.stages = stages == 2 || stages == 3 ? stages : pass_stages();
         std::vector<int> B = P.tiles[pi];
         d.Tp = (int)B.size();
         d.c = std::min(P.c, d.Tp);
@@ -795,7 +796,7 @@ void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, cons
                 continue;
             }
             if (diag && p.c == 3 && (p.Tp == 11 || p.Tp == 12) && kernel_variant() != 1) {
-                const bool two = pass_stages() == 2;   // measured: 2 stages keep 2 CTAs per SM and win
+                const bool two = p.stages != 3;
                 if (p.Tp == 11) two ? run_f32g<4, 2>(m, p, diag, in, out, D, sms, s, active)
                                 : run_f32g<4, 3>(m, p, diag, in, out, D, sms, s, active);
                 else two ? run_f32g<8, 2>(m, p, diag, in, out, D, sms, s, active)

@@ -238,13 +238,23 @@ esc_status esc_cf_batched(esc_handle* h, const esc_cf_batch_cfg* cfg, const void
 
 /* Dynamical correlations of the last ground state.  Replaces DynJeJe / DynJsJs / LocalDynSzSz
  * (src/dynamics.h:345-460, :222-341, :64-217).  `out` receives (omega_steps+1) x ncols doubles in
- * the column order of the reference's JeJe_ (6) / JsJs_ (15) / 2SSLocal_ (9) files. */
+ * the column order of the reference's JeJe_ (6) / JsJs_ (15) / 2SSLocal_ (9) files.  With
+ * out == NULL only nrows / ncols are filled (nothing is computed). */
 esc_status esc_spectrum(esc_handle* h, const esc_dyn_cfg* cfg, double* out, int* nrows, int* ncols);
 
 /* Ground-state expectation values printed by Observables::measureLocalS / measureLocalJe
  * (src/Observables.h:107-128, :88-104): s_out N x 3 complex (<Sx>,<Sy>,<Sz>), je_out N x 2
  * complex (<Jex_i>,<Jey_i>).  Either may be NULL. */
 esc_status esc_measure_local(esc_handle* h, double* s_out, double* je_out);
+
+/* Self-tuning (extension, no reference counterpart): times the complex64 H.v variants of this
+ * Hamiltonian on this device -- tile bits 11/12/13, ahead-of-time vs run-time specialised passes,
+ * 2 vs 3 tile buffers, first-fit vs balanced term-to-pass assignment -- and keeps the fastest.
+ * All variants compute the same H.v.  Call before esc_lanczos_gs (it may change the internal
+ * basis order; ESC_ERR_STATE otherwise).  Uses two complex64 vectors of scratch.  report (may be
+ * NULL) receives one line per candidate and the choice.  ESC_AUTOTUNE=1 in the environment runs
+ * it inside esc_create. */
+esc_status esc_autotune(esc_handle* h, char* report, size_t report_len);
 
 /* Gradients (extension, no reference counterpart).  dE0[3] = dE0/d{K, J, h} by
  * Hellmann-Feynman on the last ground state, with K the common Kitaev coupling

@@ -398,3 +398,21 @@ def test_mixed_cf_spectrum_matches_fp64(shape, kind):
     # without the complex128 head the complex64 recurrence alone is visibly less accurate
     s32n = h.spectrum(kind, "CF", cf_steps=1000, dtype=np.complex64, fp64_head=-1)
     assert np.abs(s32n[:, 1:] - s64[:, 1:]).max() > np.abs(s32[:, 1:] - s64[:, 1:]).max()
+
+
+def test_autotune_keeps_hv_and_reports_candidates():
+    """The autotuner times the complex64 H.v variants and installs the fastest; the installed
+    variant computes the same H.v (to complex64 rounding) and Lanczos still works afterwards."""
+    p = kitaev(Lx=3, Ly=6, J=0.1, seed=0, lanczos_steps=60)
+    h = esc.Handle(p)
+    x = O.random_start(3, h.D, normalize=False).astype(np.complex64)
+    before = h.hv(x).astype(np.complex128)
+    rep = h.autotune()
+    lines = [l for l in rep.splitlines() if l.startswith("T=")]
+    assert len(lines) >= 8 and "chosen:" in rep
+    assert relerr(h.hv(x).astype(np.complex128), before) < 2e-6
+    r = h.lanczos_gs(start=O.random_start(0, h.D), lanctype="GS", reortho=1)
+    ref = esc.Handle(p).lanczos_gs(start=O.random_start(0, h.D), lanctype="GS", reortho=1)
+    assert abs(r["E0"] - ref["E0"]) < 1e-10 * abs(ref["E0"])
+    with pytest.raises(esc.EscError):
+        h.autotune()            # refused once a ground state exists
