@@ -75,7 +75,7 @@ _lib = None
 # every symbol declared in include/esc.h
 EXPORTS = ["esc_params_default", "esc_params_from_file", "esc_lattice", "esc_plan", "esc_create", "esc_destroy", "esc_last_error",
            "esc_num_sites", "esc_dim", "esc_neighbors", "esc_basis_permutation", "esc_stream", "esc_hv", "esc_hv_batched", "esc_apply_op",
-           "esc_start_vector", "esc_rayleigh", "esc_rayleigh_noalloc", "esc_lanczos_gs", "esc_cf_batched", "esc_spectrum", "esc_measure_local", "esc_grad", "esc_autotune"]
+           "esc_start_vector", "esc_rayleigh", "esc_rayleigh_noalloc", "esc_lanczos_gs", "esc_cf_batched", "esc_spectrum", "esc_measure_local", "esc_grad", "esc_autotune", "esc_two_point"]
 
 
 def lib_path():
@@ -118,6 +118,7 @@ def lib():
     L.esc_measure_local.argtypes = [vp, vp, vp]
     L.esc_grad.argtypes = [vp, P(DynCfg), vp, vp]
     L.esc_autotune.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+    L.esc_two_point.argtypes = [vp, ci, ci, vp]
     _lib = L
     return L
 
@@ -316,6 +317,12 @@ class Handle:
                                             _ptr(lens)))
         return [(a[c, : lens[c]], b[c, : lens[c] + 1]) for c in range(nc)]
 
+    def two_point(self, opA, opB):
+        """Observables::TwoPointCorr: N x N matrix <gs| A_si B_sj |gs> (si >= sj, mirrored)."""
+        out = np.empty((self.N, self.N), dtype=np.complex128)
+        _check(self.h, lib().esc_two_point(self.h, OP_ID[opA], OP_ID[opB], _ptr(out)))
+        return out
+
     def autotune(self):
         """Times the complex64 H.v variants for this Hamiltonian and keeps the fastest; returns the
         report (one line per candidate, then the choice)."""
@@ -415,6 +422,12 @@ class Observables:
 
     def measureLocalJe(self, GS_):
         return self.handle.measure_local()[1]
+
+    def TwoPointCorr(self, OpA, OpB, GS_=None):
+        """src/Observables.h:131-158, on the handle's ground state."""
+        if OpA not in OP_ID or OpB not in OP_ID:
+            raise ValueError("Unknown Operator label")
+        return self.handle.two_point(OpA, OpB)
 
 
 def StartDynamics(dynstr, variables, lanczos, mode=None):

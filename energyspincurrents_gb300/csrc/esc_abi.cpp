@@ -1355,6 +1355,81 @@ void grad_impl(esc_handle* h, const esc_dyn_cfg* cfg, double* dE0, double* dS) {
 
 }  // namespace
 
+namespace {
+
+// Observables::TwoPointCorr (src/Observables.h:131-158): C(si, sj) = <gs| A_si B_sj |gs> for
+// si >= sj, and C(sj, si) = the same value (the reference mirrors it without conjugation).
+// GPU form: U_j = B_sj |gs> for all j; for a Hermitian A, Phi_i = A_si |gs> and one GEMV per
+// column gives <Phi_i|U_j> for all i (2N operator applications instead of N(N+1)/2); otherwise
+// A_si U_j is applied per pair and dotted with |gs>.  Falls back to the pairwise form when the
+// 2N vectors do not fit in device memory.
+bool hermitian_op(int op) {
+    switch (op) {
+        case ESC_OP_SP: case ESC_OP_SM: case ESC_OP_SPE3: case ESC_OP_SME3: return false;
+        default: return true;
+    }
+}
+
+template <typename R>
+void two_point_impl(esc_handle* h, int opA, int opB, std::vector<cplx>& C) {
+    Pipe<R> P(h);
+    const int N = h->N;
+    const int64_t D = h->D;
+    const size_t ES = Pipe<R>::ES;
+    auto T = [&](int op, int site) { return esc::make_dev_op(esc::operator_terms(op, site, h->p, h->L), &h->plan.perm); };
+    C.assign((size_t)N * N, cplx(0, 0));
+    ensure_t(h->d_sc, h->sc_bytes, std::max(h->sc_bytes, (size_t)(2 * N + 8) * sizeof(double)));
+    ensure_partials(h, N + 2);
+    double* d_r = h->d_sc;
+    std::vector<double> r(2 * (size_t)N);
+    void* U = nullptr;
+    void* Phi = nullptr;
+    const bool herm = hermitian_op(opA);
+    if (cudaMalloc(&U, (size_t)N * D * ES) != cudaSuccess || (herm && cudaMalloc(&Phi, (size_t)N * D * ES) != cudaSuccess)) {
+        (void)cudaGetLastError();
+        if (U) cudaFree(U);
+        U = Phi = nullptr;
+    }
+    try {
+        if (U && herm) {
+            for (int j = 0; j < N; j++) P.apply(T(opB, j), h->d_gs, (char*)U + (size_t)j * D * ES);
+            for (int i = 0; i < N; i++) P.apply(T(opA, i), h->d_gs, (char*)Phi + (size_t)i * D * ES);
+            for (int j = 0; j < N; j++) {
+                esc::launch_gemv_h<R>(Phi, D, N, (char*)U + (size_t)j * D * ES, D, h->d_part, part_cap_doubles(h), d_r,
+                                      h->stream);
+                ESC_CUDA(cudaMemcpyAsync(r.data(), d_r, r.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+                sync(h);
+                for (int i = j; i < N; i++) C[(size_t)i * N + j] = C[(size_t)j * N + i] = cplx(r[2 * i], r[2 * i + 1]);
+            }
+        } else {
+            ensure(h->d_work, h->work_bytes, std::max(h->work_bytes, 2 * (size_t)D * ES));
+            char* u = (char*)h->d_work;
+            char* w = u + (size_t)D * ES;
+            for (int j = 0; j < N; j++) {
+                P.apply(T(opB, j), h->d_gs, u);
+                for (int i = j; i < N; i++) {
+                    P.apply(T(opA, i), u, w);
+                    P.dot(h->d_gs, w, d_r);
+                    double c[2];
+                    ESC_CUDA(cudaMemcpyAsync(c, d_r, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+                    sync(h);
+                    C[(size_t)i * N + j] = C[(size_t)j * N + i] = cplx(c[0], c[1]);
+                }
+            }
+        }
+    } catch (...) {
+        (void)cudaStreamSynchronize(h->stream);
+        if (U) cudaFree(U);
+        if (Phi) cudaFree(Phi);
+        throw;
+    }
+    sync(h);
+    if (U) cudaFree(U);
+    if (Phi) cudaFree(Phi);
+}
+
+}  // namespace
+
 extern "C" {
 
 esc_status esc_spectrum(esc_handle* h, const esc_dyn_cfg* cfg, double* out, int* nrows, int* ncols) {
@@ -1402,6 +1477,19 @@ esc_status esc_spectrum(esc_handle* h, const esc_dyn_cfg* cfg, double* out, int*
         if (nrows) *nrows = cfg->omega_steps + 1;
         if (ncols) *ncols = nc;
         if (out) std::copy(s.begin(), s.end(), out);
+    });
+}
+
+esc_status esc_two_point(esc_handle* h, int opA, int opB, double* out) {
+    if (!h || !out) return finish(h, ESC_ERR_PARAM, "null argument");
+    if (!h->have_gs) return finish(h, ESC_ERR_STATE, "no ground state: call esc_lanczos_gs first");
+    for (int op : {opA, opB})
+        if (op < 0 || op > ESC_OP_JSXJSYJSZ) return finish(h, ESC_ERR_PARAM, "Unknown Operator label");
+    return guarded(h, [&]() {
+        std::vector<cplx> C;
+        if (h->basis_dt == ESC_C64) two_point_impl<float>(h, opA, opB, C);
+        else two_point_impl<double>(h, opA, opB, C);
+        std::memcpy(out, C.data(), C.size() * sizeof(cplx));
     });
 }
 

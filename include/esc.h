@@ -242,6 +242,11 @@ esc_status esc_cf_batched(esc_handle* h, const esc_cf_batch_cfg* cfg, const void
  * out == NULL only nrows / ncols are filled (nothing is computed). */
 esc_status esc_spectrum(esc_handle* h, const esc_dyn_cfg* cfg, double* out, int* nrows, int* ncols);
 
+/* Observables::TwoPointCorr (src/Observables.h:131-158): out (N x N complex, row-major) =
+ * <gs| A_si B_sj |gs> for si >= sj, mirrored to (sj, si) without conjugation as the reference does.
+ * opA / opB: single-site operators (ESC_OP_I .. ESC_OP_JSXJSYJSZ). */
+esc_status esc_two_point(esc_handle* h, int opA, int opB, double* out);
+
 /* Ground-state expectation values printed by Observables::measureLocalS / measureLocalJe
  * (src/Observables.h:107-128, :88-104): s_out N x 3 complex (<Sx>,<Sy>,<Sz>), je_out N x 2
  * complex (<Jex_i>,<Jey_i>).  Either may be NULL. */

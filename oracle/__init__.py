@@ -47,6 +47,7 @@ def lib():
         L.or_cf_lanczos.argtypes = [c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p, P(c_int)]
         L.or_cf_eval.argtypes = [c_void_p, c_void_p, c_int, c_double, c_int, c_void_p, c_double, c_void_p]
         L.or_dot.argtypes = [c_int64, c_void_p, c_void_p, c_void_p]
+        L.or_two_point.argtypes = [c_void_p, c_char_p, c_char_p, c_void_p, c_void_p]
         _lib = L
     return _lib
 
@@ -192,6 +193,14 @@ class Model:
         if lib().or_dynamics(self.h, which.encode(), omegasteps, domega, eta, _p(out)):
             raise ValueError(lib().or_last_error().decode())
         return out.reshape(omegasteps + 1, ncol)
+
+    def two_point(self, opA, opB, psi=None):
+        """Observables::TwoPointCorr: N x N matrix <gs| A_si B_sj |gs> (si >= sj, mirrored)."""
+        out = np.empty(self.N * self.N * 2)
+        p = None if psi is None else np.ascontiguousarray(psi, dtype=np.complex128)
+        if lib().or_two_point(self.h, opA.encode(), opB.encode(), None if p is None else _p(p), _p(out)):
+            raise ValueError(lib().or_last_error().decode())
+        return (out[0::2] + 1j * out[1::2]).reshape(self.N, self.N)
 
     def cf_lanczos(self, phi, steps, reortho=False):
         phi = np.ascontiguousarray(phi, dtype=np.complex128)

@@ -890,6 +890,29 @@ int or_cf_eval(const double* a, const double* b, int n, double E0, int nomega, c
     return 0;
 }
 
+// Observables::TwoPointCorr (src/Observables.h:131-158): for sj, out1 = B_sj |gs>; for si >= sj,
+// Corr(si,sj) = <gs| A_si out1> and Corr(sj,si) = the same value (not its conjugate).  psi NULL:
+// the model's ground state.  out: N x N complex, row-major.
+int or_two_point(void* h, const char* opA, const char* opB, const double* psi, double* out) {
+    OrModel* m = (OrModel*)h;
+    try {
+        const int N = m->N;
+        const VecC gs = psi ? VecC((const cplx*)psi, (const cplx*)psi + m->D) : m->Psi;
+        std::vector<cplx> C((size_t)N * N);
+        for (int sj = 0; sj < N; sj++) {
+            const VecC out1 = apply_named(*m, gs, opB, sj);
+            for (int si = sj; si < N; si++) {
+                const VecC out2 = apply_named(*m, out1, opA, si);
+                const cplx c = vdot(gs.data(), out2.data(), m->D);
+                C[(size_t)si * N + sj] = c;
+                C[(size_t)sj * N + si] = c;
+            }
+        }
+        std::memcpy(out, C.data(), C.size() * sizeof(cplx));
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
 int or_dot(int64_t D, const double* a, const double* b, double* out) {
     cplx r = vdot((const cplx*)a, (const cplx*)b, D);
     out[0] = r.real(); out[1] = r.imag();

@@ -40,9 +40,11 @@ def build(force=False):
         "LanczosCond": os.path.join(REF, "main.cpp"),
         "golden_driver": os.path.join(HERE, "golden_driver.cpp"),
     }
+    deps = glob.glob(os.path.join(HERE, "shim", "**", "*"), recursive=True) + [os.path.join(HERE, "lapack_bridge.cpp")]
     for name, src in targets.items():
         exe = os.path.join(OUT, name)
-        if os.path.exists(exe) and not force:
+        if os.path.exists(exe) and not force and all(
+                os.path.getmtime(exe) >= os.path.getmtime(d) for d in [src] + deps if os.path.isfile(d)):
             continue
         subprocess.run(common + ["-o", exe, src] + link, check=True)
     return OUT

@@ -115,6 +115,15 @@ int main(int argc, char** argv) {
         std::vector<std::complex<double>> loc;
         for (int s = 0; s < N; s++) { loc.push_back(Sxi[s]); loc.push_back(Syi[s]); loc.push_back(Szi[s]); }
         dump("localS.bin", loc.data(), loc.size() * 16);
+        // Observables::TwoPointCorr (src/Observables.h:131-158), its commented drivers in main.cpp:118-183
+        const char* pairs[][2] = {{"Sz", "Sz"}, {"Sx", "Sy"}, {"Sp", "Sm"}, {"Jsx", "Jsy"}, {"Jex", "Jey"}};
+        for (auto& pr : pairs) {
+            Eigen::MatrixXcd C = Obs.TwoPointCorr(pr[0], pr[1], Psi);
+            std::vector<std::complex<double>> c;
+            for (int i = 0; i < N; i++)
+                for (int j = 0; j < N; j++) c.push_back(C(i, j));
+            dump(std::string("corr_") + pr[0] + "_" + pr[1] + ".bin", c.data(), c.size() * 16);
+        }
         std::string a = "Energy Current", b = "Spin Current", c = "LocalSzSz";
         StartDynamics(a, P, Lat, Basis, H, Lan, Psi);
         StartDynamics(b, P, Lat, Basis, H, Lan, Psi);

@@ -193,6 +193,10 @@ def project(vecs, D):
     return out.reshape(vecs.shape[:-1] + (3,))
 
 
+# Observables::TwoPointCorr pairs dumped by golden_driver.cpp
+CORR_PAIRS = [("Sz", "Sz"), ("Sx", "Sy"), ("Sp", "Sm"), ("Jsx", "Jsy"), ("Jex", "Jey")]
+
+
 def run_case(name, text, full_ops, exe):
     p = parse_params(text)
     N = int(p["NumberofSitesLx"]) * int(p["NumberofSitesLy"])
@@ -241,6 +245,8 @@ def run_case(name, text, full_ops, exe):
                 res[f"full_{k}"] = v
             if p.get("LancType") == "All":
                 res["localS"] = rd("localS.bin", np.complex128).reshape(N, 3)
+                for a, b in CORR_PAIRS:
+                    res[f"corr_{a}_{b}"] = rd(f"corr_{a}_{b}.bin", np.complex128).reshape(N, N)
                 for fn, key in (("JeJe_outSpectrum.real", "JeJe"), ("JsJs_outSpectrum.real", "JsJs"),
                                 ("2SSLocal_outSpectrum.real", "SSLocal")):
                     res[key] = np.loadtxt(os.path.join(out, fn))

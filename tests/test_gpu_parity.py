@@ -416,3 +416,20 @@ def test_autotune_keeps_hv_and_reports_candidates():
     assert abs(r["E0"] - ref["E0"]) < 1e-10 * abs(ref["E0"])
     with pytest.raises(esc.EscError):
         h.autotune()            # refused once a ground state exists
+
+
+@pytest.mark.parametrize("pair", [("Sz", "Sz"), ("Sx", "Sy"), ("Sp", "Sm"), ("Jsx", "Jsy"), ("Jex", "Jey"), ("Sme3", "Spe3")])
+def test_two_point_corr_vs_oracle(pair, tmp_path):
+    """Observables::TwoPointCorr on the GPU (GEMV form for Hermitian A, pairwise otherwise) against
+    the oracle on the same ground state, and against the reference's own matrix."""
+    g, P, h = golden_handle("kitaev12", tmp_path)
+    p = parse_param_text(g["params"])
+    gs = h.lanczos_gs(start=O.random_start(int(p["RandomSeed"]), h.D), lanctype="All")["gs"]
+    m = O.Model(p["Model"], int(p["NumberofSitesLx"]), int(p["NumberofSitesLy"]), 1, 1,
+                *[float(p[k]) for k in ["Kxx", "Kyy", "Kzz", "Bxx", "Byy", "Bzz"]], 0.0, 4)
+    a, b = pair
+    c = h.two_point(a, b)
+    ref = m.two_point(a, b, gs)
+    np.testing.assert_allclose(c, ref, rtol=0, atol=1e-12)
+    if f"corr_{a}_{b}" in g.files:
+        np.testing.assert_allclose(c, g[f"corr_{a}_{b}"], rtol=0, atol=1e-9)

@@ -84,3 +84,15 @@ def test_operators(name):
         np.testing.assert_allclose(proj(o), g["proj_" + op], rtol=1e-13, atol=1e-12)
         if "full_" + op in g.files:
             assert np.array_equal(o, g["full_" + op])
+
+
+CORR_PAIRS = [("Sz", "Sz"), ("Sx", "Sy"), ("Sp", "Sm"), ("Jsx", "Jsy"), ("Jex", "Jey")]
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names() if "corr_Sz_Sz" in np.load(f"{GOLDEN}/{n}.npz").files])
+def test_two_point_corr(name):
+    """Observables::TwoPointCorr (src/Observables.h:131-158) on the reference's own ground state."""
+    g, p, m = load(name)
+    for a, b in CORR_PAIRS:
+        c = m.two_point(a, b, g["psi"])
+        np.testing.assert_allclose(c, g[f"corr_{a}_{b}"], rtol=0, atol=1e-13)
