@@ -154,7 +154,7 @@ def run_reference(args, rank):
 
 def time_to_spectrum(esc, sites=24, gs_steps=300, cf_steps=1000):
     """time-to-S(omega) on the JeJe channels (CF mode, 2000 omega in [0,6], eta=0.05), from one FP64
-    ground state: mixed batched (complex64 CF vectors after a complex128 head of 48 steps, the
+    ground state: mixed batched (complex64 CF vectors after the default complex128 head of 24 steps, the
     channels as columns of one batched CUDA-graph recurrence) against plain FP64 (complex128, same
     path).  1000 CF steps: the continued fraction is converged there (two FP64 runs that differ
     only in rounding agree to ~1e-11), so the mixed-vs-FP64 difference measures precision, not the
@@ -164,14 +164,14 @@ def time_to_spectrum(esc, sites=24, gs_steps=300, cf_steps=1000):
     params = workload(sites)
     P = esc.ConstVariables(**params, omega_steps=1999, domega=6.0 / 1999, eta=0.05)
     out = {"sites": sites, "kind": "JeJe, continued fraction", "gs_steps": gs_steps, "cf_steps": cf_steps,
-           "omega": "2000 points in [0,6]", "eta": 0.05, "fp64_head": 48}
+           "omega": "2000 points in [0,6]", "eta": 0.05, "fp64_head": 24}
     h = esc.Handle(P)
     h.lanczos_gs(steps=gs_steps, lanctype="GS", reortho=0, want_gs=False)
     res = {}
     for name, dt in (("mixed", np.complex64), ("fp64", np.complex128)):
         torch_sync()
         t0 = time.perf_counter()
-        S = h.spectrum("Energy Current", "CF", cf_steps=cf_steps, dtype=dt, fp64_head=48)
+        S = h.spectrum("Energy Current", "CF", cf_steps=cf_steps, dtype=dt)
         res[name] = (time.perf_counter() - t0, S)
     h.close()
     out["mixed_batched_s"] = round(res["mixed"][0], 3)

@@ -920,7 +920,9 @@ void spectrum_impl(esc_handle* h, const esc_dyn_cfg& cfg, std::vector<double>& o
 
     // CF resolvents G_A(omega) = <A gs|(z-H)^-1|A gs>, z = omega + E0 - i eta, for a list of
     // operators, run as columns of the batched CF Lanczos (batched.cu)
-    const int head = cfg.fp64_head == 0 ? 48 : std::max(0, cfg.fp64_head);
+    // default complex128 head: 24 steps for JeJe, 48 for the larger-amplitude JsJs and local
+    // spectra -- measured max |S_mixed - S_FP64| <= 3e-7 at N = 18, 24 (1000 CF steps, eta 0.05)
+    const int head = cfg.fp64_head == 0 ? (cfg.kind == ESC_DYN_JEJE ? 24 : 48) : std::max(0, cfg.fp64_head);
     auto cf_runs = [&](const std::vector<std::vector<esc::OpTerm>>& ts) {
         std::vector<std::vector<cplx>> G(ts.size());
         const int width = cf_batch_width(h, Pipe<R>::ES, (int)ts.size());

@@ -116,7 +116,8 @@ typedef struct {
     int cf_steps;               /* continued-fraction Lanczos steps (CF mode)                  */
     esc_dtype dtype;            /* CF mode: precision of the CF Lanczos vectors                */
     int fp64_head;              /* CF mode, ESC_C64 only: leading CF steps run on complex128   *
-                                 * vectors before the complex64 tail (0: 48, < 0: none)         */
+                                 * vectors before the complex64 tail (0: 24 for JeJe, 48 for    *
+                                 * the others; < 0: none)                                       */
 } esc_dyn_cfg;
 
 /* Batched continued-fraction Lanczos: ncols independent three-term recurrences (no
