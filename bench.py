@@ -197,6 +197,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-spectrum", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="skip the self-tuner (library default plan)")
     ap.add_argument("--autotune-report", action="store_true",
                     help="print the self-tuner's timing of every H.v variant for --sites and exit (no JSON line)")
     args = ap.parse_args()
@@ -223,6 +224,10 @@ def main():
     params = workload(args.sites)
     h = esc.Handle(params)
     D = h.D
+    tuning = None
+    if not args.no_autotune:
+        # the library's self-tuner: per-pass choice of kernel variant for this Hamiltonian (untimed)
+        tuning = h.autotune().strip().splitlines()[-1]
     stream = torch.cuda.ExternalStream(h.stream())
     v = torch.empty(D, dtype=torch.complex64, device="cuda")
     out = torch.empty_like(v)
@@ -232,6 +237,8 @@ def main():
     st = esc.lib().esc_start_vector(h.h, 1, 1, esc.ctypes.c_void_p(v.data_ptr()), esc.C64, flags)
     assert st == 0, esc.lib().esc_last_error(h.h)
     npasses = esc.plan(esc.ConstVariables(**params))[1]
+    if tuning:
+        npasses = len(tuning.split("passes:")[1].split("(")[0].split())
     torch.cuda.synchronize()
 
     def step():
@@ -271,7 +278,8 @@ def main():
         tsrc = prof.get("source") + f", scaled to 2^{args.sites} states and {npasses} passes"
     roof = {"bound": "hbm", "achieved": round(kernel_gbs, 1), "peak": peak, "unit": "GB/s",
             "frac": round(kernel_gbs / peak, 4), "peak_source": peak_kind, "traffic": traffic,
-            "kernel": "esc_jit_pass* (run-time specialised complex64 passes of one H.v)", "passes": npasses,
+            "kernel": "complex64 tiled H.v passes (esc_jit_pass*, k_hv_pass_f32g; per-pass choice of the self-tuner)",
+            "passes": npasses,
             "algorithmic_bytes_per_launch": algo_bytes, "traffic_source": tsrc}
     del v, out
     torch.cuda.empty_cache()
@@ -314,7 +322,8 @@ def main():
                 "config": {"workload": f"Kitaev-Heisenberg honeycomb N={args.sites} ({params['Lx']}x{params['Ly']//2} "
                                        f"unit cells, PBC), K=-1 J=0.05 h=0.02[111], one H.v per step (complex64)",
                            "states": D, "l2": "inputs larger than L2 (no flush needed)" if D * 8 > 129e6 else
-                           "inputs smaller than L2", "parallelism": "replicas" if world > 1 else "single GPU"},
+                           "inputs smaller than L2", "parallelism": "replicas" if world > 1 else "single GPU",
+                           "tuning": tuning},
                 "roofline": roof, "cpu_baseline": cb, "e2e": e2e, "time_to_S": tts, "clocks": clk.summary(),
                 "gpu_launches": args.steps * npasses}
         print(json.dumps(line), flush=True)

@@ -326,7 +326,7 @@ class Handle:
     def autotune(self):
         """Times the complex64 H.v variants for this Hamiltonian and keeps the fastest; returns the
         report (one line per candidate, then the choice)."""
-        buf = ctypes.create_string_buffer(8192)
+        buf = ctypes.create_string_buffer(32768)
         _check(self.h, lib().esc_autotune(self.h, buf, len(buf)))
         return buf.value.decode()
 

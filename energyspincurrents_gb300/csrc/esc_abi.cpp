@@ -608,12 +608,14 @@ void specialise(esc_handle* h, std::vector<esc::DevPass>& passes, int force = -1
         throw Fail(ESC_ERR_CUDA, "run-time specialisation of the H.v passes failed: " + err);
 }
 
-// Self-tuning of the complex64 H.v: times one H.v (after one warm-up, median of 3, CUDA events
-// on the handle's stream) for each candidate -- tile bits T in {11, 12, 13}, ahead-of-time vs
-// run-time specialised passes, 2 vs 3 tile buffers, first-fit vs balanced term assignment -- and
-// installs the fastest.  Plans are built once per T.  The candidates compute the same H.v (the
-// tests hold every variant to the oracle); only their speed differs.  Needs two complex64
-// vectors of scratch; refuses once a ground state exists (its basis order would change).
+// Self-tuning of the complex64 H.v.  For each plan -- tile bits T in {11, 12, 13} (the planner's
+// pass count follows) x first-fit / balanced term assignment -- each kernel variant (ahead-of-time
+// vs run-time specialised, 2 vs 3 tile buffers) is timed pass by pass (CUDA events on the
+// handle's stream, median of 3 after a warm-up); the plan's composite takes the fastest variant
+// of every pass (light passes and heavy passes may prefer different tile rings) and is timed as a
+// whole; the fastest composite is installed.  All variants compute the same H.v (the tests hold
+// each to the oracle); only their speed differs.  Needs two complex64 vectors of scratch; refuses
+// once a ground state exists (a new plan relabels the internal basis).
 std::string autotune(esc_handle* h, std::vector<double>* times) {
     if (h->have_gs) throw Fail(ESC_ERR_STATE, "autotune before the first Lanczos run (it may relabel the basis)");
     const int64_t D = h->D;
@@ -625,19 +627,34 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
     cudaEvent_t e0, e1;
     ESC_CUDA(cudaEventCreate(&e0));
     ESC_CUDA(cudaEventCreate(&e1));
-    struct Cand { int T, jit, stages, balance; double ms; };
-    std::vector<Cand> cands;
+    auto median_ms = [&](const std::vector<esc::DevPass>& ps) {
+        const void* dg = diag_for(h, ESC_C64);
+        esc::launch_hv_tiled<float>(h->dm, ps, v, w, D, dg, h->stream);
+        std::vector<float> ms(3);
+        for (float& x : ms) {
+            ESC_CUDA(cudaEventRecord(e0, h->stream));
+            esc::launch_hv_tiled<float>(h->dm, ps, v, w, D, dg, h->stream);
+            ESC_CUDA(cudaEventRecord(e1, h->stream));
+            ESC_CUDA(cudaEventSynchronize(e1));
+            ESC_CUDA(cudaEventElapsedTime(&x, e0, e1));
+        }
+        std::sort(ms.begin(), ms.end());
+        return (double)ms[1];
+    };
     std::ostringstream rep;
     const esc::Plan keep = h->plan;
     const std::vector<esc::DevPass> keep_passes = h->passes;
     double best = 1e300;
-    Cand bc{};
     esc::Plan bplan;
+    int bbal = 0, bT = 0;
+    std::vector<esc::DevPass> bpasses;
     try {
         for (int T : {11, 12, 13}) {
             if (T > h->N) continue;
             const esc::Plan plan = esc::make_plan(h->N, bond_pairs(h), T, 3, 200);
-            for (int balance : {0, 1})
+            for (int balance : {0, 1}) {
+                std::vector<std::vector<esc::DevPass>> vars;
+                std::vector<std::vector<double>> per;
                 for (int stages : {2, 3})
                     for (int jit : {0, 1}) {
                         if (jit && T == 13) continue;   // no specialised kernel for 8192-state tiles
@@ -646,23 +663,32 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
                         bool spec = false;
                         for (const auto& ps : h->passes) spec = spec || ps.jit >= 0;
                         if (jit && !spec) continue;
-                        const void* dg = diag_for(h, ESC_C64);
-                        esc::launch_hv_tiled<float>(h->dm, h->passes, v, w, D, dg, h->stream);
-                        std::vector<float> ms(3);
-                        for (float& x : ms) {
-                            ESC_CUDA(cudaEventRecord(e0, h->stream));
-                            esc::launch_hv_tiled<float>(h->dm, h->passes, v, w, D, dg, h->stream);
-                            ESC_CUDA(cudaEventRecord(e1, h->stream));
-                            ESC_CUDA(cudaEventSynchronize(e1));
-                            ESC_CUDA(cudaEventElapsedTime(&x, e0, e1));
-                        }
-                        std::sort(ms.begin(), ms.end());
-                        const Cand c{T, jit, stages, balance, ms[1]};
-                        cands.push_back(c);
-                        rep << "T=" << T << " passes=" << plan.tiles.size() << " jit=" << jit << " stages=" << stages
-                            << " balance=" << balance << ": " << ms[1] << " ms\n";
-                        if (c.ms < best) { best = c.ms; bc = c; bplan = plan; }
+                        std::vector<double> t;
+                        for (const auto& ps : h->passes) t.push_back(median_ms({ps}));
+                        const double tot = median_ms(h->passes);
+                        rep << "T=" << T << " passes=" << plan.tiles.size() << " balance=" << balance << " jit=" << jit
+                            << " stages=" << stages << ": " << tot << " ms | per pass";
+                        for (double x : t) rep << " " << x;
+                        rep << "\n";
+                        if (times) times->push_back(tot);
+                        vars.push_back(h->passes);
+                        per.push_back(t);
                     }
+                // composite: fastest variant of each pass
+                std::vector<esc::DevPass> comp = vars[0];
+                rep << "  composite T=" << T << " balance=" << balance << ": variants";
+                for (size_t p = 0; p < comp.size(); p++) {
+                    size_t bv = 0;
+                    for (size_t k = 1; k < vars.size(); k++)
+                        if (per[k][p] < per[bv][p]) bv = k;
+                    comp[p] = vars[bv][p];
+                    rep << " " << (comp[p].jit >= 0 ? "jit" : "aot") << "/" << comp[p].stages;
+                }
+                install_plan(h, plan, balance, 2);   // model, permutations, diagonal of this plan
+                const double tc = median_ms(comp);
+                rep << ": " << tc << " ms\n";
+                if (tc < best) { best = tc; bplan = plan; bbal = balance; bT = T; bpasses = comp; }
+            }
         }
     } catch (...) {
         cudaEventDestroy(e0);
@@ -675,12 +701,11 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(buf);
-    install_plan(h, bplan, bc.balance, bc.stages);
-    if (bc.jit) specialise(h, h->passes, 1);
-    rep << "chosen: T=" << bc.T << " jit=" << bc.jit << " stages=" << bc.stages << " balance=" << bc.balance << " ("
-        << bc.ms << " ms)\n";
-    if (times)
-        for (const auto& c : cands) times->push_back(c.ms);
+    install_plan(h, bplan, bbal, 2);
+    h->passes = bpasses;
+    rep << "chosen: T=" << bT << " balance=" << bbal << " passes:";
+    for (const auto& ps : bpasses) rep << " " << (ps.jit >= 0 ? "jit" : "aot") << "/" << ps.stages;
+    rep << " (" << best << " ms)\n";
     return rep.str();
 }
 
