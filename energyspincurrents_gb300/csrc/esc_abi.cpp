@@ -610,7 +610,7 @@ void specialise(esc_handle* h, std::vector<esc::DevPass>& passes, int force = -1
 
 // Self-tuning of the complex64 H.v.  For each plan -- tile bits T in {11, 12, 13} (the planner's
 // pass count follows) x first-fit / balanced term assignment -- each kernel variant (ahead-of-time
-// vs run-time specialised, 2 vs 3 tile buffers) is timed pass by pass (CUDA events on the
+// vs run-time specialised; 2 or 3 tile buffers, or 2 plus staged epilogue loads) is timed pass by pass (CUDA events on the
 // handle's stream, median of 3 after a warm-up); the plan's composite takes the fastest variant
 // of every pass (light passes and heavy passes may prefer different tile rings) and is timed as a
 // whole; the fastest composite is installed.  All variants compute the same H.v (the tests hold
@@ -655,7 +655,7 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
             for (int balance : {0, 1}) {
                 std::vector<std::vector<esc::DevPass>> vars;
                 std::vector<std::vector<double>> per;
-                for (int stages : {2, 3})
+                for (int stages : {2, 3, 4})
                     for (int jit : {0, 1}) {
                         if (jit && T == 13) continue;   // no specialised kernel for 8192-state tiles
                         install_plan(h, plan, balance, stages);

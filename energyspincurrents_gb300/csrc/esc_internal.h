@@ -129,7 +129,7 @@ struct DevPass {
     unsigned char gk[MAX_PTERMS + MAX_SITES];     // term code: bond = register mask (0..15); field = 33 + register bit, 32 = thread-bit field
     float ga[MAX_PTERMS + MAX_SITES], gb[MAX_PTERMS + MAX_SITES];   // bond: ceq, cdiff
     int jit;      // kernel specialised for this pass at run time (hv_jit.cu), -1: none
-    int stages;   // tile buffers per CTA of the complex64 pass (2 or 3)
+    int stages;   // complex64 pass: 2 or 3 tile buffers per CTA, 4 = 2 + staged epilogue loads
 };
 // Builds one DevPass per plan pass from the relabelled model; throws if a term fits no tile.
 // balance: term -> pass assignment (0 first eligible pass, 1 balanced, -1 from ESC_PASS_BALANCE);

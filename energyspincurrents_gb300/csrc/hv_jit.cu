@@ -84,7 +84,8 @@ std::string terms_source(const DevPass& p, int k) {
       << "extern \"C\" __global__ void __launch_bounds__(512, 2) esc_jit_pass" << k
       << "(const __grid_constant__ escdev::PassTab p, const float* __restrict__ diag, const float2* __restrict__ in,"
          " float2* __restrict__ out, long long ntiles, const int* __restrict__ active) {\n"
-      << "  escdev::pass_body<" << E << ", " << (p.stages == 3 ? 3 : 2) << ">(p, Terms" << k << "{}, diag, in, out, ntiles, active);\n}\n";
+      << "  escdev::pass_body<" << E << ", " << (p.stages >= 2 && p.stages <= 4 ? p.stages : 2) << ">(p, Terms" << k
+      << "{}, diag, in, out, ntiles, active);\n}\n";
     return o.str();
 }
 
@@ -198,7 +199,7 @@ bool jit_compile(std::vector<DevPass>& passes, std::string& err) {
             JitEntry e;
             e.device = dev;
             e.E = 1 << (p.Tp - 9);
-            e.smem = (size_t)(p.stages == 3 ? 3 : 2) * escdev::TPB * e.E * sizeof(float2);
+            e.smem = (size_t)(p.stages >= 3 ? 3 : 2) * escdev::TPB * e.E * sizeof(float2);
             const std::string name = "esc_jit_pass" + std::to_string(k);
             if (!drv(D.moduleGetFunction(&e.fn, mod, name.c_str()), "cuModuleGetFunction", err)) return false;
             if (!drv(D.funcSetAttribute(e.fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)e.smem),

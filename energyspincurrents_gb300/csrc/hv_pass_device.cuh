@@ -72,15 +72,102 @@ __device__ __forceinline__ void gfield(const float2 (&P)[E], float2 vfx, float f
     }
 }
 
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+// 2-stage tile ring + staged epilogue loads (see pass_body, NS = 4).
+template <int E, class Terms>
+__device__ __forceinline__ void pass_body_staged(const PassTab& p, const Terms& terms, const float* __restrict__ diag,
+                                                 const float2* __restrict__ in, float2* __restrict__ out,
+                                                 long long ntiles, const int* __restrict__ active) {
+    if (active && *active == 0) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* bufs = reinterpret_cast<float2*>(smem_raw);   // 2 x (512 E) states
+    float2* stage = bufs + 2 * TPB * E;                    // 512 E partials (or diagonal entries)
+    __shared__ unsigned long long hi_off[E];
+    const int tid = threadIdx.x;
+    if (tid < E) hi_off[tid] = p.tabHi[tid];
+    const unsigned long long lo = p.tabLo[tid >> 3] | (unsigned long long)(tid & 7);
+    const unsigned long long lo2 = p.tabLo[(tid >> 2) & 63] | (unsigned long long)((2 * tid) & 7);
+    const int hi2 = tid >> 8;
+    const float2 vfx = make_float2(p.fx, p.fx);
+    const float fy = p.fy, fz = p.fz;
+    __syncthreads();
+    const long long g = gridDim.x;
+    auto issue = [&](long long tt, int slot) {
+        if (tt < ntiles) {
+            float2* dst = bufs + slot * (TPB * E);
+            const unsigned long long b2 = tile_bits(p, tt) | lo2;
+#pragma unroll
+            for (int i = 0; i < E / 2; i++) cp_async16(dst + 2 * (tid + TPB * i), in + (b2 | hi_off[hi2 + 2 * i]));
+        }
+        cp_async_commit();
+    };
+    long long t = blockIdx.x;
+    issue(t, 0);
+    for (int cur = 0; t < ntiles; t += g, cur ^= 1) {
+        const unsigned long long base = tile_bits(p, t) | lo;
+        // [partials of tile t]: thread-private staging slots, read back by the same thread
+#pragma unroll
+        for (int j = 0; j < E; j++) {
+            if (p.diag) cp_async4(reinterpret_cast<float*>(stage) + tid + TPB * j, diag + (base | hi_off[j]));
+            else if (p.accumulate) cp_async8(stage + tid + TPB * j, out + (base | hi_off[j]));
+        }
+        cp_async_commit();
+        issue(t + g, cur ^ 1);      // [tile t+g]
+        cp_async_wait<2>();         // tile t has landed
+        __syncthreads();
+        float2* tile = bufs + cur * (TPB * E);
+        float2 acc[E];
+#pragma unroll
+        for (int j = 0; j < E; j++) acc[j] = make_float2(0.f, 0.f);
+        terms(tile, tid, vfx, fy, acc);
+        cp_async_wait<1>();         // partials of tile t have landed (tile t+g may be in flight)
+#pragma unroll
+        for (int j = 0; j < E; j++) {
+            const unsigned long long k = base | hi_off[j];
+            float2 o = acc[j];
+            if (p.diag) {
+                const float dg = fmaf(fz, (float)(p.N - 2 * __popcll(k)), reinterpret_cast<const float*>(stage)[tid + TPB * j]);
+                const float2 v = tile[tid + TPB * j];
+                o.x = fmaf(dg, v.x, o.x);
+                o.y = fmaf(dg, v.y, o.y);
+            } else if (p.accumulate) {
+                const float2 pr = stage[tid + TPB * j];
+                o.x += pr.x;
+                o.y += pr.y;
+            }
+            out[k] = o;
+        }
+        __syncthreads();   // buffer `cur` is refilled two iterations later; staging reused next iteration
+    }
+    cp_async_wait<0>();
+}
+
 // One pass over all tiles.  Terms: functor terms(tile, tid, vfx, fy, acc) adding the off-diagonal
 // terms of the pass for the thread's E states.  diag (pass 1): bond part of the diagonal per state.
 // NS-stage ring of tile buffers: tiles t + g, ..., t + (NS-1) g are in flight while tile t is
 // computed (g = grid size); every iteration commits exactly one cp.async group (possibly empty),
 // so wait_group<NS-1> always means "tile t has landed".
+//
+// NS = 4 is a 2-stage ring plus a staging area for the per-state loads of the epilogue (the
+// partial result of the earlier passes, or the bond diagonal in pass 1): they are copied with
+// cp.async as well, so no register holds them while the terms are applied and the compiler cannot
+// sink them next to their use.  Commit order per iteration: [partials of tile t] [tile t+g].
 template <int E, int NS, class Terms>
 __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, const float* __restrict__ diag,
                                           const float2* __restrict__ in, float2* __restrict__ out, long long ntiles,
                                           const int* __restrict__ active) {
+    if constexpr (NS == 4) {
+        pass_body_staged<E>(p, terms, diag, in, out, ntiles, active);
+        return;
+    }
     if (active && *active == 0) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* bufs = reinterpret_cast<float2*>(smem_raw);   // NS x (512 E) states

@@ -599,7 +599,7 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_o
         DevPass& d = out[pi];
         std::memset(&d, 0, sizeof(d));
         d.jit = -1;
-        d.stages = stages == 2 || stages == 3 ? stages : pass_stages();
+        d.stages = stages >= 2 && stages <= 4 ? stages : pass_stages();
         std::vector<int> B = P.tiles[pi];
         d.Tp = (int)B.size();
         d.c = std::min(P.c, d.Tp);
@@ -754,7 +754,8 @@ static void run_f32(const DevModel& m, const DevPass& p, const void* diag, const
 template <int E, int NS>
 static void run_f32g(const DevModel& m, const DevPass& p, const void* diag, const void* in, void* out, int64_t D, int sms,
                      cudaStream_t s, const int* active) {
-    const size_t smem = (size_t)NS * TILE_THREADS * E * sizeof(float2);   // NS-stage ring of tiles
+    // NS-stage ring of tiles (NS = 4: 2 tiles + staging of the epilogue loads)
+    const size_t smem = (size_t)(NS == 4 ? 3 : NS) * TILE_THREADS * E * sizeof(float2);
     // always raised: dynamic + static shared memory may pass 48 KB even when the ring alone does not
     ESC_CUDA(cudaFuncSetAttribute(k_hv_pass_f32g<E, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
@@ -767,11 +768,9 @@ static void run_f32g(const DevModel& m, const DevPass& p, const void* diag, cons
 }
 
 int pass_stages() {
-    static int v = [] {
-        const char* e = std::getenv("ESC_STAGES");
-        return e && std::atoi(e) == 3 ? 3 : 2;
-    }();
-    return v;
+    const char* e = std::getenv("ESC_STAGES");
+    const int x = e ? std::atoi(e) : 2;
+    return x >= 2 && x <= 4 ? x : 2;
 }
 
 static int kernel_variant() {
@@ -796,11 +795,14 @@ void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, cons
                 continue;
             }
             if (diag && p.c == 3 && (p.Tp == 11 || p.Tp == 12) && kernel_variant() != 1) {
-                const bool two = p.stages != 3;
-                if (p.Tp == 11) two ? run_f32g<4, 2>(m, p, diag, in, out, D, sms, s, active)
-                                : run_f32g<4, 3>(m, p, diag, in, out, D, sms, s, active);
-                else two ? run_f32g<8, 2>(m, p, diag, in, out, D, sms, s, active)
-                         : run_f32g<8, 3>(m, p, diag, in, out, D, sms, s, active);
+                switch ((p.Tp == 11 ? 10 : 20) + p.stages) {
+                    case 12: run_f32g<4, 2>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 13: run_f32g<4, 3>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 14: run_f32g<4, 4>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 23: run_f32g<8, 3>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 24: run_f32g<8, 4>(m, p, diag, in, out, D, sms, s, active); break;
+                    default: run_f32g<8, 2>(m, p, diag, in, out, D, sms, s, active); break;
+                }
                 continue;
             }
             if (diag && p.c == 3 && p.Tp >= 11 && p.Tp <= 13) {

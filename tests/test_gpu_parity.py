@@ -433,3 +433,19 @@ def test_two_point_corr_vs_oracle(pair, tmp_path):
     np.testing.assert_allclose(c, ref, rtol=0, atol=1e-12)
     if f"corr_{a}_{b}" in g.files:
         np.testing.assert_allclose(c, g[f"corr_{a}_{b}"], rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("stages", ["3", "4"])
+@pytest.mark.parametrize("jit", ["0", "require"])
+def test_pass_variants_bitwise_equal(stages, jit, monkeypatch):
+    """The complex64 pass variants (3-stage tile ring; 2 stages + epilogue loads staged through
+    shared memory), ahead-of-time and specialised, give bit-identical H.v to the 2-stage kernel."""
+    p = kitaev(Lx=3, Ly=6, J=0.1)
+    monkeypatch.setenv("ESC_JIT", "0")
+    monkeypatch.setenv("ESC_STAGES", "2")
+    h2 = esc.Handle(p)
+    monkeypatch.setenv("ESC_JIT", jit)
+    monkeypatch.setenv("ESC_STAGES", stages)
+    hv = esc.Handle(p)
+    x = O.random_start(9, h2.D, normalize=False).astype(np.complex64)
+    assert np.array_equal(hv.hv(x), h2.hv(x))
