@@ -578,12 +578,12 @@ std::vector<std::pair<int, int>> bond_pairs(const esc_handle* h) {
 
 // Installs a site relabelling + pass plan: relabelled model, passes, basis permutations.  The
 // bond diagonal depends on the relabelling, so cached diagonal vectors are dropped.
-void install_plan(esc_handle* h, const esc::Plan& plan, int balance, int stages) {
+void install_plan(esc_handle* h, const esc::Plan& plan, int balance, int stages, int tb_bits = 0) {
     h->plan = plan;
     std::vector<esc::Bond> rb(h->bonds);
     for (auto& b : rb) { b.i = h->plan.perm[b.i]; b.j = h->plan.perm[b.j]; }
     h->dm = esc::make_dev_model(h->p, h->L, rb, h->p.Bxx, h->p.Byy, h->p.Bzz);
-    h->passes = esc::make_passes(h->plan, h->dm, balance, stages);
+    h->passes = esc::make_passes(h->plan, h->dm, balance, stages, tb_bits);
     std::vector<int> inv(h->N), fwd(h->N);
     for (int s = 0; s < h->N; s++) { inv[h->plan.perm[s]] = s; fwd[s] = h->plan.perm[s]; }
     h->to_int = esc::make_perm_table(inv);    // internal bit b reads reference bit inv[b]
@@ -608,14 +608,16 @@ void specialise(esc_handle* h, std::vector<esc::DevPass>& passes, int force = -1
         throw Fail(ESC_ERR_CUDA, "run-time specialisation of the H.v passes failed: " + err);
 }
 
-// Self-tuning of the complex64 H.v.  For each plan -- tile bits T in {11, 12, 13} (the planner's
-// pass count follows) x first-fit / balanced term assignment -- each kernel variant (ahead-of-time
-// vs run-time specialised; 2 or 3 tile buffers, or 2 plus staged epilogue loads) is timed pass by pass (CUDA events on the
-// handle's stream, median of 3 after a warm-up); the plan's composite takes the fastest variant
-// of every pass (light passes and heavy passes may prefer different tile rings) and is timed as a
-// whole; the fastest composite is installed.  All variants compute the same H.v (the tests hold
-// each to the oracle); only their speed differs.  Needs two complex64 vectors of scratch; refuses
-// once a ground state exists (a new plan relabels the internal basis).
+// Self-tuning of the complex64 H.v.  Plans: tile bits T in {11, 12, 13} (above 26 sites only 12:
+// the others never win there -- one more pass, or one CTA per SM) x first-fit / balanced
+// term-to-pass assignment.  Kernel variants per plan: ahead-of-time vs run-time specialised;
+// 512 threads per 4096-state tile (8 register states each) vs 256 (16 each); 2 or 3 tile buffers,
+// or 2 plus staged epilogue loads.  Every variant is timed pass by pass (CUDA events on the
+// handle's stream, median of 3 after a warm-up); a plan's composite takes the fastest variant of
+// each pass (light and heavy passes prefer different variants) and is timed as a whole; the
+// fastest composite is installed.  All variants compute the same H.v up to complex64 rounding (the
+// tests hold each to the oracle).  Needs two complex64 vectors of scratch; refuses once a ground
+// state exists (a new plan relabels the internal basis).
 std::string autotune(esc_handle* h, std::vector<double>* times) {
     if (h->have_gs) throw Fail(ESC_ERR_STATE, "autotune before the first Lanczos run (it may relabel the basis)");
     const int64_t D = h->D;
@@ -650,15 +652,16 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
     std::vector<esc::DevPass> bpasses;
     try {
         for (int T : {11, 12, 13}) {
-            if (T > h->N) continue;
+            if (T > h->N || (h->N > 26 && T != 12)) continue;
             const esc::Plan plan = esc::make_plan(h->N, bond_pairs(h), T, 3, 200);
             for (int balance : {0, 1}) {
                 std::vector<std::vector<esc::DevPass>> vars;
                 std::vector<std::vector<double>> per;
+                for (int tb : {9, 8})
                 for (int stages : {2, 3, 4})
                     for (int jit : {0, 1}) {
-                        if (jit && T == 13) continue;   // no specialised kernel for 8192-state tiles
-                        install_plan(h, plan, balance, stages);
+                        if (T == 13 && (jit || tb == 8)) continue;   // 8192-state tiles: generic kernel only
+                        install_plan(h, plan, balance, stages, tb);
                         if (jit) specialise(h, h->passes, 1);
                         bool spec = false;
                         for (const auto& ps : h->passes) spec = spec || ps.jit >= 0;
@@ -666,8 +669,8 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
                         std::vector<double> t;
                         for (const auto& ps : h->passes) t.push_back(median_ms({ps}));
                         const double tot = median_ms(h->passes);
-                        rep << "T=" << T << " passes=" << plan.tiles.size() << " balance=" << balance << " jit=" << jit
-                            << " stages=" << stages << ": " << tot << " ms | per pass";
+                        rep << "T=" << T << " passes=" << plan.tiles.size() << " balance=" << balance << " threads="
+                            << (1 << tb) << " jit=" << jit << " stages=" << stages << ": " << tot << " ms | per pass";
                         for (double x : t) rep << " " << x;
                         rep << "\n";
                         if (times) times->push_back(tot);
@@ -682,7 +685,7 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
                     for (size_t k = 1; k < vars.size(); k++)
                         if (per[k][p] < per[bv][p]) bv = k;
                     comp[p] = vars[bv][p];
-                    rep << " " << (comp[p].jit >= 0 ? "jit" : "aot") << "/" << comp[p].stages;
+                    rep << " " << (comp[p].jit >= 0 ? "jit" : "aot") << "/" << comp[p].stages << "/" << (1 << comp[p].tb_bits);
                 }
                 install_plan(h, plan, balance, 2);   // model, permutations, diagonal of this plan
                 const double tc = median_ms(comp);
@@ -704,7 +707,7 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
     install_plan(h, bplan, bbal, 2);
     h->passes = bpasses;
     rep << "chosen: T=" << bT << " balance=" << bbal << " passes:";
-    for (const auto& ps : bpasses) rep << " " << (ps.jit >= 0 ? "jit" : "aot") << "/" << ps.stages;
+    for (const auto& ps : bpasses) rep << " " << (ps.jit >= 0 ? "jit" : "aot") << "/" << ps.stages << "/" << (1 << ps.tb_bits);
     rep << " (" << best << " ms)\n";
     return rep.str();
 }

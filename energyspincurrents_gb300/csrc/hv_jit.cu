@@ -35,7 +35,7 @@ const char* kPassDeviceSource =
 struct JitEntry {
     int device;
     CUfunction fn;
-    int E;
+    int E, TB;
     int per_sm;
     size_t smem;
 };
@@ -44,7 +44,9 @@ std::mutex g_mu;
 std::vector<JitEntry> g_entries;
 std::map<std::string, std::vector<int>> g_cache;   // device + source -> entry per kernel
 
-bool eligible(const DevPass& p) { return p.c == 3 && (p.Tp == 11 || p.Tp == 12) && p.nterm > 0; }
+bool eligible(const DevPass& p) {
+    return p.c == 3 && (p.Tp == 11 || p.Tp == 12) && (p.tb_bits == 8 || p.tb_bits == 9) && p.nterm > 0;
+}
 
 std::string hexf(float x) {
     unsigned u;
@@ -56,7 +58,8 @@ std::string hexf(float x) {
 
 // Straight-line terms functor of one pass: the group loop of RuntimeTerms (hv_tiled.cu) unrolled.
 std::string terms_source(const DevPass& p, int k) {
-    const int E = 1 << (p.Tp - 9);
+    const int TB = 1 << p.tb_bits;
+    const int E = 1 << (p.Tp - p.tb_bits);
     std::ostringstream o;
     o << "struct Terms" << k << " {\n"
       << "  __device__ __forceinline__ void operator()(const float2* tile, int tid, float2 vfx, float fy, float2 (&acc)["
@@ -64,7 +67,7 @@ std::string terms_source(const DevPass& p, int k) {
     int q = 0;
     for (int g = 0; g < p.ngroup; g++) {
         o << "    {\n      const unsigned glo = " << p.glo[g] << "u;\n      float2 P[" << E << "];\n"
-          << "      escdev::load_group<" << E << ">(tile, tid, glo, P);\n"
+          << "      escdev::load_group<" << E << ", " << TB << ">(tile, tid, glo, P);\n"
           << "      const bool par = __popc((unsigned)tid & glo) & 1; (void)par;\n"
           << "      const float sf = ((unsigned)tid & glo) ? fy : -fy; (void)sf;\n";
         for (int n = 0; n < p.gnt[g]; n++, q++) {
@@ -81,11 +84,11 @@ std::string terms_source(const DevPass& p, int k) {
         o << "    }\n";
     }
     o << "  }\n};\n"
-      << "extern \"C\" __global__ void __launch_bounds__(512, 2) esc_jit_pass" << k
+      << "extern \"C\" __global__ void __launch_bounds__(" << TB << ", 2) esc_jit_pass" << k
       << "(const __grid_constant__ escdev::PassTab p, const float* __restrict__ diag, const float2* __restrict__ in,"
          " float2* __restrict__ out, long long ntiles, const int* __restrict__ active) {\n"
-      << "  escdev::pass_body<" << E << ", " << (p.stages >= 2 && p.stages <= 4 ? p.stages : 2) << ">(p, Terms" << k
-      << "{}, diag, in, out, ntiles, active);\n}\n";
+      << "  escdev::pass_body<" << E << ", " << (p.stages >= 2 && p.stages <= 4 ? p.stages : 2) << ", Terms" << k << ", "
+      << TB << ">(p, Terms" << k << "{}, diag, in, out, ntiles, active);\n}\n";
     return o.str();
 }
 
@@ -198,14 +201,15 @@ bool jit_compile(std::vector<DevPass>& passes, std::string& err) {
             const DevPass& p = passes[which[k]];
             JitEntry e;
             e.device = dev;
-            e.E = 1 << (p.Tp - 9);
-            e.smem = (size_t)(p.stages >= 3 ? 3 : 2) * escdev::TPB * e.E * sizeof(float2);
+            e.TB = 1 << p.tb_bits;
+            e.E = 1 << (p.Tp - p.tb_bits);
+            e.smem = (size_t)(p.stages >= 3 ? 3 : 2) * e.TB * e.E * sizeof(float2);
             const std::string name = "esc_jit_pass" + std::to_string(k);
             if (!drv(D.moduleGetFunction(&e.fn, mod, name.c_str()), "cuModuleGetFunction", err)) return false;
             if (!drv(D.funcSetAttribute(e.fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)e.smem),
                      "cuFuncSetAttribute", err))
                 return false;
-            if (!drv(D.occupancy(&e.per_sm, e.fn, escdev::TPB, e.smem),
+            if (!drv(D.occupancy(&e.per_sm, e.fn, e.TB, e.smem),
                      "cuOccupancyMaxActiveBlocksPerMultiprocessor", err))
                 return false;
             g_entries.push_back(e);
@@ -236,7 +240,7 @@ void jit_launch(const DevPass& p, const escdev::PassTab& pt, const void* diag, c
     const int* act = active;
     void* args[] = {&tab, &dg, &vin, &vout, &nt, &act};
     std::string err;
-    if (!drv(driver().launchKernel(e.fn, (unsigned)g, 1, 1, escdev::TPB, 1, 1, (unsigned)e.smem, (CUstream)s, args, nullptr),
+    if (!drv(driver().launchKernel(e.fn, (unsigned)g, 1, 1, (unsigned)e.TB, 1, 1, (unsigned)e.smem, (CUstream)s, args, nullptr),
              "cuLaunchKernel", err))
         throw CudaError(err);
 }

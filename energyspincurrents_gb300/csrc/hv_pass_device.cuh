@@ -4,8 +4,9 @@
 // and by the kernels specialised per Hamiltonian at run time in hv_jit.cu (terms compiled in as
 // straight-line code).  It includes nothing, because it is also handed verbatim to NVRTC.
 //
-// A CTA of 512 threads owns one tile of 512 E basis states at a time: thread t holds the states
-// t + 512 j (j < E), i.e. tile-local bits 0..8 are thread bits and bits 9.. are register bits.
+// A CTA of TB threads (512, or 256 with twice the registers per thread) owns one tile of TB E
+// basis states at a time: thread t holds the states t + TB j (j < E), i.e. tile-local bits
+// 0..log2(TB)-1 are thread bits and the bits above are register bits.
 // Tiles are copied global -> shared with cp.async (16 B per copy, runs of 8 consecutive states),
 // double buffered: tile n+1 is in flight while tile n is computed.  Terms come in groups of equal
 // thread-bit mask: a thread loads the E partner states of a group from shared memory once and
@@ -40,12 +41,12 @@ __device__ __forceinline__ unsigned long long tile_bits(const PassTab& p, long l
     return b;
 }
 
-// Partners of a group: P[j] = state (t ^ lo) + 512 j of the tile.
-template <int E>
+// Partners of a group: P[j] = state (t ^ lo) + TB j of the tile (TB threads per tile).
+template <int E, int TB = TPB>
 __device__ __forceinline__ void load_group(const float2* tile, int tid, unsigned lo, float2 (&P)[E]) {
     const float2* src = tile + (tid ^ (int)lo);
 #pragma unroll
-    for (int j = 0; j < E; j++) P[j] = src[TPB * j];
+    for (int j = 0; j < E; j++) P[j] = src[TB * j];
 }
 
 // parity of the low 4 bits of x
@@ -81,49 +82,59 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
 
+// Per-CTA set-up shared by both pass bodies: register-index offsets hi_off[j] (global offset of
+// tile state TB j), the thread's own offset `lo`, and the copy offsets.  Tile state s has its
+// local bits 3..8 in tabLo[(s >> 3) & 63] and bits 9.. in tabHi[s >> 9].
+template <int E, int TB>
+__device__ __forceinline__ void tile_offsets(const PassTab& p, int tid, unsigned long long* hi_off,
+                                             unsigned long long& lo, unsigned long long& lo2) {
+    if (tid < E) hi_off[tid] = p.tabLo[((TB * tid) >> 3) & 63] | p.tabHi[(TB * tid) >> 9];
+    lo = p.tabLo[(tid >> 3) & 63] | (unsigned long long)(tid & 7);
+    // 16-byte copies: copy c = tid + TB i moves states 2c and 2c+1 (runs of 8 never split)
+    lo2 = p.tabLo[(tid >> 2) & 63] | (unsigned long long)((2 * tid) & 7);
+}
+template <int E, int TB>
+__device__ __forceinline__ void issue_tile(const PassTab& p, const float2* __restrict__ in, float2* dst, long long tt,
+                                           int tid, unsigned long long lo2) {
+    const unsigned long long b2 = tile_bits(p, tt) | lo2;
+#pragma unroll
+    for (int i = 0; i < E / 2; i++) cp_async16(dst + 2 * (tid + TB * i), in + (b2 | p.tabHi[(tid + TB * i) >> 8]));
+}
+
 // 2-stage tile ring + staged epilogue loads (see pass_body, NS = 4).
-template <int E, class Terms>
+template <int E, int TB, class Terms>
 __device__ __forceinline__ void pass_body_staged(const PassTab& p, const Terms& terms, const float* __restrict__ diag,
                                                  const float2* __restrict__ in, float2* __restrict__ out,
                                                  long long ntiles, const int* __restrict__ active) {
     if (active && *active == 0) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2* bufs = reinterpret_cast<float2*>(smem_raw);   // 2 x (512 E) states
-    float2* stage = bufs + 2 * TPB * E;                    // 512 E partials (or diagonal entries)
+    float2* bufs = reinterpret_cast<float2*>(smem_raw);   // 2 x (TB E) states
+    float2* stage = bufs + 2 * TB * E;                     // TB E partials (or diagonal entries)
     __shared__ unsigned long long hi_off[E];
     const int tid = threadIdx.x;
-    if (tid < E) hi_off[tid] = p.tabHi[tid];
-    const unsigned long long lo = p.tabLo[tid >> 3] | (unsigned long long)(tid & 7);
-    const unsigned long long lo2 = p.tabLo[(tid >> 2) & 63] | (unsigned long long)((2 * tid) & 7);
-    const int hi2 = tid >> 8;
+    unsigned long long lo, lo2;
+    tile_offsets<E, TB>(p, tid, hi_off, lo, lo2);
     const float2 vfx = make_float2(p.fx, p.fx);
     const float fy = p.fy, fz = p.fz;
     __syncthreads();
     const long long g = gridDim.x;
-    auto issue = [&](long long tt, int slot) {
-        if (tt < ntiles) {
-            float2* dst = bufs + slot * (TPB * E);
-            const unsigned long long b2 = tile_bits(p, tt) | lo2;
-#pragma unroll
-            for (int i = 0; i < E / 2; i++) cp_async16(dst + 2 * (tid + TPB * i), in + (b2 | hi_off[hi2 + 2 * i]));
-        }
-        cp_async_commit();
-    };
     long long t = blockIdx.x;
-    issue(t, 0);
+    if (t < ntiles) issue_tile<E, TB>(p, in, bufs, t, tid, lo2);
+    cp_async_commit();
     for (int cur = 0; t < ntiles; t += g, cur ^= 1) {
         const unsigned long long base = tile_bits(p, t) | lo;
         // [partials of tile t]: thread-private staging slots, read back by the same thread
 #pragma unroll
         for (int j = 0; j < E; j++) {
-            if (p.diag) cp_async4(reinterpret_cast<float*>(stage) + tid + TPB * j, diag + (base | hi_off[j]));
-            else if (p.accumulate) cp_async8(stage + tid + TPB * j, out + (base | hi_off[j]));
+            if (p.diag) cp_async4(reinterpret_cast<float*>(stage) + tid + TB * j, diag + (base | hi_off[j]));
+            else if (p.accumulate) cp_async8(stage + tid + TB * j, out + (base | hi_off[j]));
         }
         cp_async_commit();
-        issue(t + g, cur ^ 1);      // [tile t+g]
+        if (t + g < ntiles) issue_tile<E, TB>(p, in, bufs + (cur ^ 1) * (TB * E), t + g, tid, lo2);   // [tile t+g]
+        cp_async_commit();
         cp_async_wait<2>();         // tile t has landed
         __syncthreads();
-        float2* tile = bufs + cur * (TPB * E);
+        float2* tile = bufs + cur * (TB * E);
         float2 acc[E];
 #pragma unroll
         for (int j = 0; j < E; j++) acc[j] = make_float2(0.f, 0.f);
@@ -134,12 +145,12 @@ __device__ __forceinline__ void pass_body_staged(const PassTab& p, const Terms& 
             const unsigned long long k = base | hi_off[j];
             float2 o = acc[j];
             if (p.diag) {
-                const float dg = fmaf(fz, (float)(p.N - 2 * __popcll(k)), reinterpret_cast<const float*>(stage)[tid + TPB * j]);
-                const float2 v = tile[tid + TPB * j];
+                const float dg = fmaf(fz, (float)(p.N - 2 * __popcll(k)), reinterpret_cast<const float*>(stage)[tid + TB * j]);
+                const float2 v = tile[tid + TB * j];
                 o.x = fmaf(dg, v.x, o.x);
                 o.y = fmaf(dg, v.y, o.y);
             } else if (p.accumulate) {
-                const float2 pr = stage[tid + TPB * j];
+                const float2 pr = stage[tid + TB * j];
                 o.x += pr.x;
                 o.y += pr.y;
             }
@@ -160,35 +171,27 @@ __device__ __forceinline__ void pass_body_staged(const PassTab& p, const Terms& 
 // partial result of the earlier passes, or the bond diagonal in pass 1): they are copied with
 // cp.async as well, so no register holds them while the terms are applied and the compiler cannot
 // sink them next to their use.  Commit order per iteration: [partials of tile t] [tile t+g].
-template <int E, int NS, class Terms>
+template <int E, int NS, class Terms, int TB = TPB>
 __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, const float* __restrict__ diag,
                                           const float2* __restrict__ in, float2* __restrict__ out, long long ntiles,
                                           const int* __restrict__ active) {
     if constexpr (NS == 4) {
-        pass_body_staged<E>(p, terms, diag, in, out, ntiles, active);
+        pass_body_staged<E, TB>(p, terms, diag, in, out, ntiles, active);
         return;
     }
     if (active && *active == 0) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2* bufs = reinterpret_cast<float2*>(smem_raw);   // NS x (512 E) states
+    float2* bufs = reinterpret_cast<float2*>(smem_raw);   // NS x (TB E) states
     __shared__ unsigned long long hi_off[E];
     const int tid = threadIdx.x;
-    if (tid < E) hi_off[tid] = p.tabHi[tid];
-    const unsigned long long lo = p.tabLo[tid >> 3] | (unsigned long long)(tid & 7);
-    // 16-byte copies: thread t moves states 2t' and 2t'+1, t' = t + 512 i (runs of 8 never split)
-    const unsigned long long lo2 = p.tabLo[(tid >> 2) & 63] | (unsigned long long)((2 * tid) & 7);
-    const int hi2 = tid >> 8;
+    unsigned long long lo, lo2;
+    tile_offsets<E, TB>(p, tid, hi_off, lo, lo2);
     const float2 vfx = make_float2(p.fx, p.fx);
     const float fy = p.fy, fz = p.fz;
     __syncthreads();
     const long long g = gridDim.x;
     auto issue = [&](long long tt, int slot) {
-        if (tt < ntiles) {
-            float2* dst = bufs + slot * (TPB * E);
-            const unsigned long long b2 = tile_bits(p, tt) | lo2;
-#pragma unroll
-            for (int i = 0; i < E / 2; i++) cp_async16(dst + 2 * (tid + TPB * i), in + (b2 | hi_off[hi2 + 2 * i]));
-        }
+        if (tt < ntiles) issue_tile<E, TB>(p, in, bufs + slot * (TB * E), tt, tid, lo2);
         cp_async_commit();
     };
     long long t = blockIdx.x;
@@ -198,7 +201,7 @@ __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, 
         issue(t + (NS - 1) * g, cur == 0 ? NS - 1 : cur - 1);
         cp_async_wait<NS - 1>();
         __syncthreads();
-        float2* tile = bufs + cur * (TPB * E);
+        float2* tile = bufs + cur * (TB * E);
         const unsigned long long base = tile_bits(p, t) | lo;
         float2 acc[E], pre[E];
         float dpre[E];
@@ -215,7 +218,7 @@ __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, 
             float2 o = acc[j];
             if (p.diag) {
                 const float dg = fmaf(fz, (float)(p.N - 2 * __popcll(k)), dpre[j]);
-                const float2 v = tile[tid + TPB * j];
+                const float2 v = tile[tid + TB * j];
                 o.x = fmaf(dg, v.x, o.x);
                 o.y = fmaf(dg, v.y, o.y);
             } else if (p.accumulate) {

@@ -399,7 +399,7 @@ __device__ __forceinline__ void gfield_dispatch(int fb, const float2 (&P)[E], fl
     }
 }
 
-template <int E>
+template <int E, int TB>
 struct RuntimeTerms {
     const DevPass& p;
     __device__ __forceinline__ void operator()(const float2* tile, int tid, float2 vfx, float fy, float2 (&acc)[E]) const {
@@ -407,7 +407,7 @@ struct RuntimeTerms {
         for (int g = 0; g < p.ngroup; g++) {
             const unsigned int glo = p.glo[g];
             float2 P[E];
-            escdev::load_group<E>(tile, tid, glo, P);
+            escdev::load_group<E, TB>(tile, tid, glo, P);
             const bool par = __popc((unsigned)tid & glo) & 1;
             const float sf = ((unsigned)tid & glo) ? fy : -fy;
             const int qe = q + p.gnt[g];
@@ -426,14 +426,14 @@ struct RuntimeTerms {
     }
 };
 
-template <int E, int NS>
-__global__ void __launch_bounds__(TILE_THREADS, 2) k_hv_pass_f32g(const __grid_constant__ escdev::PassTab pt,
-                                                                const __grid_constant__ DevPass p,
-                                                                const float* __restrict__ diag,
-                                                                const float2* __restrict__ in,
-                                                                float2* __restrict__ out, long long ntiles,
-                                                                const int* __restrict__ active) {
-    escdev::pass_body<E, NS>(pt, RuntimeTerms<E>{p}, diag, in, out, ntiles, active);
+template <int E, int NS, int TB>
+__global__ void __launch_bounds__(TB, 2) k_hv_pass_f32g(const __grid_constant__ escdev::PassTab pt,
+                                                      const __grid_constant__ DevPass p,
+                                                      const float* __restrict__ diag,
+                                                      const float2* __restrict__ in,
+                                                      float2* __restrict__ out, long long ntiles,
+                                                      const int* __restrict__ active) {
+    escdev::pass_body<E, NS, RuntimeTerms<E, TB>, TB>(pt, RuntimeTerms<E, TB>{p}, diag, in, out, ntiles, active);
 }
 
 escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m) {
@@ -548,7 +548,11 @@ template void launch_energy<float>(const DevModel&, const std::vector<DevPass>&,
 template void launch_energy<double>(const DevModel&, const std::vector<DevPass>&, const void*, int64_t, double*, int,
                                     std::vector<double>&, cudaStream_t);
 
-std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_opt, int stages) {
+std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_opt, int stages, int tb_bits) {
+    if (tb_bits != 8 && tb_bits != 9) {
+        const char* e = std::getenv("ESC_TB_BITS");
+        tb_bits = e && std::atoi(e) == 8 ? 8 : 9;
+    }
     const int np = (int)P.tiles.size();
     std::vector<DevPass> out(np);
     const bool field = m.fx != 0.0 || m.fy != 0.0;
@@ -600,6 +604,7 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_o
         std::memset(&d, 0, sizeof(d));
         d.jit = -1;
         d.stages = stages >= 2 && stages <= 4 ? stages : pass_stages();
+        d.tb_bits = tb_bits;
         std::vector<int> B = P.tiles[pi];
         d.Tp = (int)B.size();
         d.c = std::min(P.c, d.Tp);
@@ -611,10 +616,11 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_o
         const std::vector<int>& pb = passb[pi];
         const std::vector<int>& pf = passf[pi];
         if ((int)pb.size() > MAX_PTERMS) throw std::invalid_argument("too many bonds in one pass");
-        // Register sites: the tile has 2^Tp states over 512 threads, so the top r = Tp - 9 local
-        // bits index a thread's registers.  Pick the r non-shared sites that leave the fewest
-        // distinct thread-bit masks (each costs one shared-memory load per state) and put them last.
-        const int r = std::max(0, d.Tp - 9);
+        // Register sites: the tile has 2^Tp states over 2^tb_bits threads, so the top
+        // r = Tp - tb_bits local bits index a thread's registers.  Pick the r non-shared sites that
+        // leave the fewest distinct thread-bit masks (each costs one shared-memory load per state)
+        // and put them last.
+        const int r = std::max(0, d.Tp - tb_bits);
         if (r > 0 && d.Tp - d.c >= r) {
             const int nf = d.Tp - d.c;   // free positions c..Tp-1
             std::vector<int> freeb(B.begin() + d.c, B.end());
@@ -679,8 +685,8 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_o
                 d.fjbit[d.nfield] |= (unsigned)((((unsigned)j << 9) & d.flm[d.nfield]) != 0u) << j;
             d.nfield++;
         }
-        // register groups: thread-bit mask = local bits 0..8
-        const unsigned lanes = (1u << std::min(d.Tp, 9)) - 1u;
+        // register groups: thread-bit mask = local bits below tb_bits
+        const unsigned lanes = (1u << std::min(d.Tp, tb_bits)) - 1u;
         std::vector<unsigned> keys;
         for (int b = 0; b < d.nbond; b++) keys.push_back(d.blm[b] & lanes);
         for (int f = 0; f < d.nfield; f++) keys.push_back(d.flm[f] & lanes);
@@ -693,14 +699,14 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_o
             int n = 0;
             for (int b = 0; b < d.nbond; b++)
                 if ((d.blm[b] & lanes) == g) {
-                    d.gk[d.nterm] = (unsigned char)(d.blm[b] >> 9);
+                    d.gk[d.nterm] = (unsigned char)(d.blm[b] >> tb_bits);
                     d.ga[d.nterm] = d.ceqf[b];
                     d.gb[d.nterm] = d.cdifff[b];
                     d.nterm++; n++;
                 }
             for (int f = 0; f < d.nfield; f++)
                 if ((d.flm[f] & lanes) == g) {
-                    const unsigned hi = d.flm[f] >> 9;
+                    const unsigned hi = d.flm[f] >> tb_bits;
                     d.gk[d.nterm] = (unsigned char)(hi ? 33 + (31 - __builtin_clz(hi)) : 32);
                     d.nterm++; n++;
                 }
@@ -751,19 +757,19 @@ static void run_f32(const DevModel& m, const DevPass& p, const void* diag, const
     ESC_CUDA(cudaGetLastError());
 }
 
-template <int E, int NS>
+template <int E, int NS, int TB = TILE_THREADS>
 static void run_f32g(const DevModel& m, const DevPass& p, const void* diag, const void* in, void* out, int64_t D, int sms,
                      cudaStream_t s, const int* active) {
     // NS-stage ring of tiles (NS = 4: 2 tiles + staging of the epilogue loads)
-    const size_t smem = (size_t)(NS == 4 ? 3 : NS) * TILE_THREADS * E * sizeof(float2);
+    const size_t smem = (size_t)(NS == 4 ? 3 : NS) * TB * E * sizeof(float2);
     // always raised: dynamic + static shared memory may pass 48 KB even when the ring alone does not
-    ESC_CUDA(cudaFuncSetAttribute(k_hv_pass_f32g<E, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ESC_CUDA(cudaFuncSetAttribute(k_hv_pass_f32g<E, NS, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass_f32g<E, NS>, TILE_THREADS, smem));
+    ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass_f32g<E, NS, TB>, TB, smem));
     const long long ntiles = (long long)(D >> p.Tp);
     const long long g = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
-    k_hv_pass_f32g<E, NS><<<(unsigned)g, TILE_THREADS, smem, s>>>(make_pass_tab(p, m), p, (const float*)diag,
-                                                                  (const float2*)in, (float2*)out, ntiles, active);
+    k_hv_pass_f32g<E, NS, TB><<<(unsigned)g, TB, smem, s>>>(make_pass_tab(p, m), p, (const float*)diag,
+                                                            (const float2*)in, (float2*)out, ntiles, active);
     ESC_CUDA(cudaGetLastError());
 }
 
@@ -795,12 +801,19 @@ void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, cons
                 continue;
             }
             if (diag && p.c == 3 && (p.Tp == 11 || p.Tp == 12) && kernel_variant() != 1) {
-                switch ((p.Tp == 11 ? 10 : 20) + p.stages) {
+                // E = 2^(Tp - tb_bits) states per thread
+                switch ((p.tb_bits == 8 ? 100 : 0) + (p.Tp == 11 ? 10 : 20) + p.stages) {
                     case 12: run_f32g<4, 2>(m, p, diag, in, out, D, sms, s, active); break;
                     case 13: run_f32g<4, 3>(m, p, diag, in, out, D, sms, s, active); break;
                     case 14: run_f32g<4, 4>(m, p, diag, in, out, D, sms, s, active); break;
                     case 23: run_f32g<8, 3>(m, p, diag, in, out, D, sms, s, active); break;
                     case 24: run_f32g<8, 4>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 112: run_f32g<8, 2, 256>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 113: run_f32g<8, 3, 256>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 114: run_f32g<8, 4, 256>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 122: run_f32g<16, 2, 256>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 123: run_f32g<16, 3, 256>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 124: run_f32g<16, 4, 256>(m, p, diag, in, out, D, sms, s, active); break;
                     default: run_f32g<8, 2>(m, p, diag, in, out, D, sms, s, active); break;
                 }
                 continue;
