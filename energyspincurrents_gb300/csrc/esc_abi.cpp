@@ -4,6 +4,8 @@
 // vector operation runs on the device; the host only does O(M^2)-O(M^3) work on the tridiagonal
 // matrix and the O(Omega x M) Lehmann / continued-fraction sums.
 #include <algorithm>
+#include <map>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -608,6 +610,79 @@ void specialise(esc_handle* h, std::vector<esc::DevPass>& passes, int force = -1
         throw Fail(ESC_ERR_CUDA, "run-time specialisation of the H.v passes failed: " + err);
 }
 
+// Tuning file (ESC_TUNE_FILE): one line per tuned Hamiltonian and device,
+//   <key> | T balance npasses | jit,stages,tb_bits per pass
+// written by the self-tuner and applied by esc_create, so a tuned configuration is reused without
+// timing again.  The key covers the device name and everything the plan and passes depend on.
+std::string tune_key(const esc_handle* h) {
+    cudaDeviceProp pr{};
+    if (cudaGetDeviceProperties(&pr, h->device) != cudaSuccess) (void)cudaGetLastError();
+    std::ostringstream k;
+    k.precision(17);
+    k << "dev=" << pr.name << " model=" << h->p.model << " Lx=" << h->p.Lx << " Ly=" << h->p.Ly << " pbc=" << h->p.pbcx
+      << h->p.pbcy << " K=" << h->p.Kxx << "," << h->p.Kyy << "," << h->p.Kzz << " B=" << h->p.Bxx << "," << h->p.Byy << ","
+      << h->p.Bzz << " J=" << h->p.jheis;
+    return k.str();
+}
+
+void save_tuning(const esc_handle* h, int T, int balance, const std::vector<esc::DevPass>& ps) {
+    const char* f = std::getenv("ESC_TUNE_FILE");
+    if (!f || !*f) return;
+    FILE* fp = std::fopen(f, "a");
+    if (!fp) return;
+    std::fprintf(fp, "%s | %d %d %d |", tune_key(h).c_str(), T, balance, (int)ps.size());
+    for (const auto& p : ps) std::fprintf(fp, " %d,%d,%d", p.jit >= 0 ? 1 : 0, p.stages, p.tb_bits);
+    std::fprintf(fp, "\n");
+    std::fclose(fp);
+}
+
+// Applies the last matching line of ESC_TUNE_FILE; false if there is none.
+bool load_tuning(esc_handle* h) {
+    const char* f = std::getenv("ESC_TUNE_FILE");
+    if (!f || !*f) return false;
+    FILE* fp = std::fopen(f, "r");
+    if (!fp) return false;
+    const std::string key = tune_key(h);
+    std::string found;
+    char line[4096];
+    while (std::fgets(line, sizeof line, fp)) {
+        std::string l(line);
+        if (l.compare(0, key.size(), key) == 0 && l.size() > key.size() && l[key.size()] == ' ') found = l.substr(key.size());
+    }
+    std::fclose(fp);
+    if (found.empty()) return false;
+    int T = 0, balance = 0, n = 0;
+    std::istringstream in(found);
+    char bar;
+    in >> bar >> T >> balance >> n >> bar;
+    std::vector<std::array<int, 3>> var(n);
+    for (auto& v : var) {
+        char c1, c2;
+        in >> v[0] >> c1 >> v[1] >> c2 >> v[2];
+    }
+    if (!in || T < 4) return false;
+    const esc::Plan plan = esc::make_plan(h->N, bond_pairs(h), T, 3, 200);
+    if ((int)plan.tiles.size() != n) return false;
+    install_plan(h, plan, balance, 2);
+    std::vector<esc::DevPass> comp(h->passes);
+    std::map<std::array<int, 2>, std::vector<esc::DevPass>> built;
+    for (int p = 0; p < n; p++) {
+        const std::array<int, 2> k{var[p][1], var[p][2]};
+        if (!built.count(k)) {
+            built[k] = esc::make_passes(h->plan, h->dm, balance, k[0], k[1]);
+            if (std::any_of(var.begin(), var.end(), [&](const std::array<int, 3>& x) { return x[0] && x[1] == k[0] && x[2] == k[1]; })) {
+                std::vector<esc::DevPass> sp = built[k];
+                std::string err;
+                if (esc::jit_compile(sp, err)) built[std::array<int, 2>{-k[0], k[1]}] = sp;
+            }
+        }
+        const auto it = built.find(var[p][0] ? std::array<int, 2>{-k[0], k[1]} : k);
+        comp[p] = (it != built.end() ? it->second : built[k])[p];
+    }
+    h->passes = comp;
+    return true;
+}
+
 // Self-tuning of the complex64 H.v.  Plans: tile bits T in {11, 12, 13} (above 26 sites only 12:
 // the others never win there -- one more pass, or one CTA per SM) x first-fit / balanced
 // term-to-pass assignment.  Kernel variants per plan: ahead-of-time vs run-time specialised;
@@ -706,6 +781,7 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
     cudaFree(buf);
     install_plan(h, bplan, bbal, 2);
     h->passes = bpasses;
+    save_tuning(h, bT, bbal, bpasses);
     rep << "chosen: T=" << bT << " balance=" << bbal << " passes:";
     for (const auto& ps : bpasses) rep << " " << (ps.jit >= 0 ? "jit" : "aot") << "/" << ps.stages << "/" << (1 << ps.tb_bits);
     rep << " (" << best << " ms)\n";
@@ -743,9 +819,11 @@ esc_status esc_create(const esc_params* p, esc_handle** out) {
         ESC_CUDA(cudaGetDevice(&h->device));
         ESC_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
         ensure_partials(h.get(), 4);
-        specialise(h.get(), h->passes);
-        if (const char* e = std::getenv("ESC_AUTOTUNE"))
-            if (std::atoi(e) == 1) autotune(h.get(), nullptr);
+        if (!load_tuning(h.get())) {
+            specialise(h.get(), h->passes);
+            if (const char* e = std::getenv("ESC_AUTOTUNE"))
+                if (std::atoi(e) == 1) autotune(h.get(), nullptr);
+        }
     });
     if (st != ESC_OK) {
         g_err = h->err;

@@ -466,3 +466,21 @@ def test_256_thread_tiles_match(jit, monkeypatch):
     assert relerr(y8, h9.hv(x).astype(np.complex128)) < 2e-6
     m = O.Model("Kitaev", 3, 6, 1, 1, -1.0, -1.0, -1.0, p["Bxx"], p["Byy"], p["Bzz"], 0.1, 4, False)
     assert relerr(y8, m.hv(x.astype(np.complex128))) < 2e-6
+
+
+def test_tuning_file_roundtrip(tmp_path, monkeypatch):
+    """The self-tuner's choice is written to ESC_TUNE_FILE and a new handle for the same Hamiltonian
+    applies it without timing: same H.v, bit for bit."""
+    f = tmp_path / "tune.txt"
+    monkeypatch.setenv("ESC_TUNE_FILE", str(f))
+    p = kitaev(Lx=3, Ly=6, J=0.1)
+    h1 = esc.Handle(p)
+    h1.autotune()
+    assert f.exists() and len(f.read_text().splitlines()) == 1
+    h2 = esc.Handle(p)
+    x = O.random_start(4, h1.D, normalize=False).astype(np.complex64)
+    assert np.array_equal(h2.hv(x), h1.hv(x))
+    h3 = esc.Handle(kitaev(Lx=3, Ly=6, J=0.2))     # other Hamiltonian: no match, library default
+    assert relerr(h3.hv(x).astype(np.complex128),
+                  O.Model("Kitaev", 3, 6, 1, 1, -1.0, -1.0, -1.0, p["Bxx"], p["Byy"], p["Bzz"], 0.2, 4,
+                          False).hv(x.astype(np.complex128))) < 2e-6
