@@ -686,7 +686,7 @@ bool load_tuning(esc_handle* h) {
 // Self-tuning of the complex64 H.v.  Plans: tile bits T in {11, 12, 13} (above 26 sites only 12:
 // the others never win there -- one more pass, or one CTA per SM) x first-fit / balanced
 // term-to-pass assignment.  Kernel variants per plan: ahead-of-time vs run-time specialised;
-// 512 threads per 4096-state tile (8 register states each) vs 256 (16 each); 2 or 3 tile buffers,
+// 512, 256 or 128 threads per 4096-state tile (8, 16, 32 register states each); 2 or 3 tile buffers,
 // or 2 plus staged epilogue loads.  Every variant is timed pass by pass (CUDA events on the
 // handle's stream, median of 3 after a warm-up); a plan's composite takes the fastest variant of
 // each pass (light and heavy passes prefer different variants) and is timed as a whole; the
@@ -732,10 +732,10 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
             for (int balance : {0, 1}) {
                 std::vector<std::vector<esc::DevPass>> vars;
                 std::vector<std::vector<double>> per;
-                for (int tb : {9, 8})
+                for (int tb : {9, 8, 7})
                 for (int stages : {2, 3, 4})
                     for (int jit : {0, 1}) {
-                        if (T == 13 && (jit || tb == 8)) continue;   // 8192-state tiles: generic kernel only
+                        if (T == 13 && (jit || tb != 9)) continue;   // 8192-state tiles: generic kernel only
                         install_plan(h, plan, balance, stages, tb);
                         if (jit) specialise(h, h->passes, 1);
                         bool spec = false;

@@ -126,16 +126,16 @@ struct DevPass {
     int ngroup, nterm;
     unsigned short glo[MAX_PTERMS + MAX_SITES];   // thread-bit mask of group g
     unsigned char gnt[MAX_PTERMS + MAX_SITES];    // terms in group g
-    unsigned char gk[MAX_PTERMS + MAX_SITES];     // term code: bond = register mask (0..15); field = 33 + register bit, 32 = thread-bit field
+    unsigned char gk[MAX_PTERMS + MAX_SITES];     // term code: bond = register mask (0..31); field = 33 + register bit, 32 = thread-bit field
     float ga[MAX_PTERMS + MAX_SITES], gb[MAX_PTERMS + MAX_SITES];   // bond: ceq, cdiff
     int jit;      // kernel specialised for this pass at run time (hv_jit.cu), -1: none
     int stages;   // complex64 pass: 2 or 3 tile buffers per CTA, 4 = 2 + staged epilogue loads
-    int tb_bits;  // complex64 grouped pass: log2 of the threads per tile (9: 512, 8: 256 with E doubled)
+    int tb_bits;  // complex64 grouped pass: log2 of the threads per tile (9: 512, 8: 256, 7: 128)
 };
 // Builds one DevPass per plan pass from the relabelled model; throws if a term fits no tile.
 // balance: term -> pass assignment (0 first eligible pass, 1 balanced, -1 from ESC_PASS_BALANCE);
 // stages: tile buffers of the complex64 passes (0: from ESC_STAGES, default 2).
-// tb_bits: threads per tile of the grouped complex64 pass, 2^tb_bits (9 or 8; 0: 9, or ESC_TB_BITS).
+// tb_bits: threads per tile of the grouped complex64 pass, 2^tb_bits (7..9; 0: ESC_TB_BITS, else 9).
 std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance = -1, int stages = 0, int tb_bits = 0);
 }  // namespace esc
 namespace escdev { struct PassTab; }

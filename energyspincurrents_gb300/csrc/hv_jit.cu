@@ -45,7 +45,7 @@ std::vector<JitEntry> g_entries;
 std::map<std::string, std::vector<int>> g_cache;   // device + source -> entry per kernel
 
 bool eligible(const DevPass& p) {
-    return p.c == 3 && (p.Tp == 11 || p.Tp == 12) && (p.tb_bits == 8 || p.tb_bits == 9) && p.nterm > 0;
+    return p.c == 3 && (p.Tp == 11 || p.Tp == 12) && p.tb_bits >= 7 && p.tb_bits <= 9 && p.nterm > 0;
 }
 
 std::string hexf(float x) {

@@ -4,7 +4,7 @@
 // and by the kernels specialised per Hamiltonian at run time in hv_jit.cu (terms compiled in as
 // straight-line code).  It includes nothing, because it is also handed verbatim to NVRTC.
 //
-// A CTA of TB threads (512, or 256 with twice the registers per thread) owns one tile of TB E
+// A CTA of TB threads (512, 256 or 128: more register states per thread) owns one tile of TB E
 // basis states at a time: thread t holds the states t + TB j (j < E), i.e. tile-local bits
 // 0..log2(TB)-1 are thread bits and the bits above are register bits.
 // Tiles are copied global -> shared with cp.async (16 B per copy, runs of 8 consecutive states),
@@ -49,8 +49,8 @@ __device__ __forceinline__ void load_group(const float2* tile, int tid, unsigned
     for (int j = 0; j < E; j++) P[j] = src[TB * j];
 }
 
-// parity of the low 4 bits of x
-__host__ __device__ constexpr int par4(int x) { return (x ^ (x >> 1) ^ (x >> 2) ^ (x >> 3)) & 1; }
+// parity of the low 5 bits of x
+__host__ __device__ constexpr int par4(int x) { return (x ^ (x >> 1) ^ (x >> 2) ^ (x >> 3) ^ (x >> 4)) & 1; }
 
 // Bond term with register mask LMH: acc[j] += c * P[j ^ LMH], c = vA or vB by the parity of the
 // register bits under the mask (vA / vB already swapped for the thread-bit parity).
@@ -87,18 +87,23 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
 // local bits 3..8 in tabLo[(s >> 3) & 63] and bits 9.. in tabHi[s >> 9].
 template <int E, int TB>
 __device__ __forceinline__ void tile_offsets(const PassTab& p, int tid, unsigned long long* hi_off,
-                                             unsigned long long& lo, unsigned long long& lo2) {
+                                             unsigned long long& lo, unsigned long long (&lo2)[2]) {
     if (tid < E) hi_off[tid] = p.tabLo[((TB * tid) >> 3) & 63] | p.tabHi[(TB * tid) >> 9];
     lo = p.tabLo[(tid >> 3) & 63] | (unsigned long long)(tid & 7);
-    // 16-byte copies: copy c = tid + TB i moves states 2c and 2c+1 (runs of 8 never split)
-    lo2 = p.tabLo[(tid >> 2) & 63] | (unsigned long long)((2 * tid) & 7);
+    // 16-byte copies: copy c = tid + TB i moves tile states 2c and 2c+1 (runs of 8 never split);
+    // (c >> 2) & 63 depends on i only for TB = 128 (through bit 5: i odd)
+    lo2[0] = p.tabLo[(tid >> 2) & 63] | (unsigned long long)((2 * tid) & 7);
+    lo2[1] = p.tabLo[((tid >> 2) + 32) & 63] | (unsigned long long)((2 * tid) & 7);
 }
 template <int E, int TB>
 __device__ __forceinline__ void issue_tile(const PassTab& p, const float2* __restrict__ in, float2* dst, long long tt,
-                                           int tid, unsigned long long lo2) {
-    const unsigned long long b2 = tile_bits(p, tt) | lo2;
+                                           int tid, const unsigned long long (&lo2)[2]) {
+    const unsigned long long b = tile_bits(p, tt);
 #pragma unroll
-    for (int i = 0; i < E / 2; i++) cp_async16(dst + 2 * (tid + TB * i), in + (b2 | p.tabHi[(tid + TB * i) >> 8]));
+    for (int i = 0; i < E / 2; i++) {
+        const unsigned long long l = (TB == 128 && (i & 1)) ? lo2[1] : lo2[0];
+        cp_async16(dst + 2 * (tid + TB * i), in + (b | l | p.tabHi[(tid + TB * i) >> 8]));
+    }
 }
 
 // 2-stage tile ring + staged epilogue loads (see pass_body, NS = 4).
@@ -112,7 +117,7 @@ __device__ __forceinline__ void pass_body_staged(const PassTab& p, const Terms& 
     float2* stage = bufs + 2 * TB * E;                     // TB E partials (or diagonal entries)
     __shared__ unsigned long long hi_off[E];
     const int tid = threadIdx.x;
-    unsigned long long lo, lo2;
+    unsigned long long lo, lo2[2];
     tile_offsets<E, TB>(p, tid, hi_off, lo, lo2);
     const float2 vfx = make_float2(p.fx, p.fx);
     const float fy = p.fy, fz = p.fz;
@@ -184,7 +189,7 @@ __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, 
     float2* bufs = reinterpret_cast<float2*>(smem_raw);   // NS x (TB E) states
     __shared__ unsigned long long hi_off[E];
     const int tid = threadIdx.x;
-    unsigned long long lo, lo2;
+    unsigned long long lo, lo2[2];
     tile_offsets<E, TB>(p, tid, hi_off, lo, lo2);
     const float2 vfx = make_float2(p.fx, p.fx);
     const float fy = p.fy, fz = p.fz;

@@ -386,6 +386,8 @@ __device__ __forceinline__ void gbond_switch(int lmh, const float2 (&P)[E], floa
     switch (lmh) {
         ESC_GB(0) ESC_GB(1) ESC_GB(2) ESC_GB(3) ESC_GB(4) ESC_GB(5) ESC_GB(6) ESC_GB(7)
         ESC_GB(8) ESC_GB(9) ESC_GB(10) ESC_GB(11) ESC_GB(12) ESC_GB(13) ESC_GB(14) ESC_GB(15)
+        ESC_GB(16) ESC_GB(17) ESC_GB(18) ESC_GB(19) ESC_GB(20) ESC_GB(21) ESC_GB(22) ESC_GB(23)
+        ESC_GB(24) ESC_GB(25) ESC_GB(26) ESC_GB(27) ESC_GB(28) ESC_GB(29) ESC_GB(30) ESC_GB(31)
         default: break;
     }
 #undef ESC_GB
@@ -549,9 +551,9 @@ template void launch_energy<double>(const DevModel&, const std::vector<DevPass>&
                                     std::vector<double>&, cudaStream_t);
 
 std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_opt, int stages, int tb_bits) {
-    if (tb_bits != 8 && tb_bits != 9) {
+    if (tb_bits < 5 || tb_bits > 9) {
         const char* e = std::getenv("ESC_TB_BITS");
-        tb_bits = e && std::atoi(e) == 8 ? 8 : 9;
+        tb_bits = e && std::atoi(e) >= 7 && std::atoi(e) <= 9 ? std::atoi(e) : 9;
     }
     const int np = (int)P.tiles.size();
     std::vector<DevPass> out(np);
@@ -800,9 +802,16 @@ void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, cons
                 jit_launch(p, make_pass_tab(p, m), diag, in, out, D, sms, s, active);
                 continue;
             }
-            if (diag && p.c == 3 && (p.Tp == 11 || p.Tp == 12) && kernel_variant() != 1) {
+            if (diag && p.c == 3 && (p.Tp == 11 || p.Tp == 12) && p.tb_bits >= 7 && p.tb_bits <= 9 &&
+                kernel_variant() != 1) {
                 // E = 2^(Tp - tb_bits) states per thread
-                switch ((p.tb_bits == 8 ? 100 : 0) + (p.Tp == 11 ? 10 : 20) + p.stages) {
+                switch ((p.tb_bits == 8 ? 100 : p.tb_bits == 7 ? 200 : 0) + (p.Tp == 11 ? 10 : 20) + p.stages) {
+                    case 212: run_f32g<16, 2, 128>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 213: run_f32g<16, 3, 128>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 214: run_f32g<16, 4, 128>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 222: run_f32g<32, 2, 128>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 223: run_f32g<32, 3, 128>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 224: run_f32g<32, 4, 128>(m, p, diag, in, out, D, sms, s, active); break;
                     case 12: run_f32g<4, 2>(m, p, diag, in, out, D, sms, s, active); break;
                     case 13: run_f32g<4, 3>(m, p, diag, in, out, D, sms, s, active); break;
                     case 14: run_f32g<4, 4>(m, p, diag, in, out, D, sms, s, active); break;

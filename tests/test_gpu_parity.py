@@ -451,15 +451,18 @@ def test_pass_variants_bitwise_equal(stages, jit, monkeypatch):
     assert np.array_equal(hv.hv(x), h2.hv(x))
 
 
+@pytest.mark.parametrize("tb", ["8", "7"])
+@pytest.mark.parametrize("stages", ["2", "4"])
 @pytest.mark.parametrize("jit", ["0", "require"])
-def test_256_thread_tiles_match(jit, monkeypatch):
-    """Grouped complex64 passes with 256 threads per 4096-state tile (16 register states per thread)
-    agree with the 512-thread kernel to complex64 rounding and with the oracle."""
+def test_smaller_thread_tiles_match(tb, stages, jit, monkeypatch):
+    """Grouped complex64 passes with 256 or 128 threads per 4096-state tile (16 or 32 register
+    states per thread) agree with the 512-thread kernel to complex64 rounding and with the oracle."""
     p = kitaev(Lx=3, Ly=6, J=0.1)
     monkeypatch.setenv("ESC_JIT", "0")
     h9 = esc.Handle(p)
     monkeypatch.setenv("ESC_JIT", jit)
-    monkeypatch.setenv("ESC_TB_BITS", "8")
+    monkeypatch.setenv("ESC_STAGES", stages)
+    monkeypatch.setenv("ESC_TB_BITS", tb)
     h8 = esc.Handle(p)
     x = O.random_start(9, h9.D, normalize=False).astype(np.complex64)
     y8 = h8.hv(x).astype(np.complex128)
