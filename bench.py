@@ -166,6 +166,7 @@ def time_to_spectrum(esc, sites=24, gs_steps=300, cf_steps=1000):
     out = {"sites": sites, "kind": "JeJe, continued fraction", "gs_steps": gs_steps, "cf_steps": cf_steps,
            "omega": "2000 points in [0,6]", "eta": 0.05, "fp64_head": 24}
     h = esc.Handle(P)
+    h.autotune()      # complex64 passes for this Hamiltonian (untimed; before the ground state by design)
     h.lanczos_gs(steps=gs_steps, lanctype="GS", reortho=0, want_gs=False)
     res = {}
     for name, dt in (("mixed", np.complex64), ("fp64", np.complex128)):
