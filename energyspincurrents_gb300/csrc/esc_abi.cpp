@@ -684,8 +684,8 @@ bool load_tuning(esc_handle* h) {
 }
 
 // Self-tuning of the complex64 H.v.  Plans: tile bits T in {11, 12, 13} (above 26 sites only 12:
-// the others never win there -- one more pass, or one CTA per SM) x first-fit / balanced
-// term-to-pass assignment.  Kernel variants per plan: ahead-of-time vs run-time specialised;
+// the others never win there -- one more pass, or one CTA per SM) x first-fit / group-minimising
+// term-to-pass assignment (make_passes modes 0 and 2; the balanced mode 1 never won).  Kernel variants per plan: ahead-of-time vs run-time specialised;
 // 512, 256 or 128 threads per 4096-state tile (8, 16, 32 register states each); 2 or 3 tile buffers,
 // or 2 plus staged epilogue loads.  Every variant is timed pass by pass (CUDA events on the
 // handle's stream, median of 3 after a warm-up); a plan's composite takes the fastest variant of
@@ -729,7 +729,7 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
         for (int T : {11, 12, 13}) {
             if (T > h->N || (h->N > 26 && T != 12)) continue;
             const esc::Plan plan = esc::make_plan(h->N, bond_pairs(h), T, 3, 200);
-            for (int balance : {0, 1}) {
+            for (int balance : {0, 2}) {
                 std::vector<std::vector<esc::DevPass>> vars;
                 std::vector<std::vector<double>> per;
                 for (int tb : {9, 8, 7})

@@ -558,9 +558,9 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_o
     const int np = (int)P.tiles.size();
     std::vector<DevPass> out(np);
     const bool field = m.fx != 0.0 || m.fy != 0.0;
-    // Term -> pass assignment.  Default: a bond or field goes to the first pass whose tile holds
-    // it.  ESC_PASS_BALANCE=1: most constrained term first, each to the eligible pass with the
-    // fewest terms so far.
+    // Term -> pass assignment (balance_opt, or ESC_PASS_BALANCE).  0: a bond or field goes to the
+    // first pass whose tile holds it.  1: most constrained term first, each to the eligible pass
+    // with the fewest terms so far.  2: first-fit, then the fewest register groups (below).
     std::vector<unsigned long long> tm(np, 0);
     for (int pi = 0; pi < np; pi++)
         for (int b : P.tiles[pi]) tm[pi] |= 1ull << b;
@@ -577,8 +577,9 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_o
             return e;
         };
         const char* be = std::getenv("ESC_PASS_BALANCE");
-        const bool balance = balance_opt >= 0 ? balance_opt == 1 : (be && std::atoi(be) == 1);
-        std::vector<int> order(terms.size()), load(np, 0);
+        const int mode = balance_opt >= 0 ? balance_opt : (be ? std::atoi(be) : 0);
+        const bool balance = mode == 1;
+        std::vector<int> order(terms.size()), load(np, 0), asg(terms.size(), -1);
         for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
         if (balance)
             std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
@@ -594,8 +595,55 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_o
             if (balance)
                 for (int pi : e) if (load[pi] < load[pick]) pick = pi;
             load[pick]++;
-            (terms[i].bond ? passb : passf)[pick].push_back(terms[i].id);
+            asg[i] = pick;
         }
+        if (mode == 2) {
+            // ESC_PASS_BALANCE=2: local search from first-fit that moves single terms between
+            // eligible passes while the total number of register groups (shared-memory loads per
+            // state) decreases; a pass's groups are counted with its best register sites, as below.
+            auto pass_cost = [&](int pi, int add, int drop) {
+                std::vector<unsigned long long> gm;
+                for (size_t i = 0; i < terms.size(); i++)
+                    if (((int)i != drop && asg[i] == pi) || (int)i == add) gm.push_back(terms[i].mask);
+                const std::vector<int>& B = P.tiles[pi];
+                const int c = std::min(P.c, (int)B.size());
+                const int nf = (int)B.size() - c, r = std::max(0, (int)B.size() - tb_bits);
+                int best = 1 << 30;
+                for (unsigned sel = 0; sel < (1u << nf); sel++) {
+                    if (__builtin_popcount(sel) != std::min(r, nf)) continue;
+                    unsigned long long regm = 0;
+                    for (int q = 0; q < nf; q++)
+                        if ((sel >> q) & 1u) regm |= 1ull << B[c + q];
+                    std::vector<unsigned long long> g{0ull};
+                    for (unsigned long long x : gm)
+                        if (std::find(g.begin(), g.end(), x & ~regm) == g.end()) g.push_back(x & ~regm);
+                    best = std::min(best, (int)g.size());
+                }
+                return best;
+            };
+            std::vector<int> cost(np);
+            for (int pi = 0; pi < np; pi++) cost[pi] = pass_cost(pi, -1, -1);
+            for (int sweep = 0; sweep < 20; sweep++) {
+                bool moved = false;
+                for (size_t i = 0; i < terms.size(); i++) {
+                    if (asg[i] < 0) continue;
+                    for (int q : elig(terms[i].mask)) {
+                        const int p = asg[i];
+                        if (q == p) continue;
+                        const int cp = pass_cost(p, -1, (int)i), cq = pass_cost(q, (int)i, -1);
+                        if (cp + cq < cost[p] + cost[q]) {
+                            asg[i] = q;
+                            cost[p] = cp;
+                            cost[q] = cq;
+                            moved = true;
+                        }
+                    }
+                }
+                if (!moved) break;
+            }
+        }
+        for (size_t i = 0; i < terms.size(); i++)
+            if (asg[i] >= 0) (terms[i].bond ? passb : passf)[asg[i]].push_back(terms[i].id);
         for (int pi = 0; pi < np; pi++) {
             std::sort(passb[pi].begin(), passb[pi].end());
             std::sort(passf[pi].begin(), passf[pi].end());
