@@ -297,10 +297,14 @@ class Handle:
         n = n.value
         return dict(E0=E0.value, alpha=a[:n], beta=b[: n + 1], ritz=r[:n], steps=n, gs=gs)
 
-    def rayleigh(self, v, flags=0):
-        """<v|H|v>/<v|v> in FP64 arithmetic (v complex128 or complex64)."""
-        v = np.ascontiguousarray(v)
+    def rayleigh(self, v=None, flags=0):
+        """<v|H|v>/<v|v> in FP64 arithmetic (v complex128 or complex64; None: the handle's ground
+        state, in place)."""
         E = ctypes.c_double()
+        if v is None:
+            _check(self.h, lib().esc_rayleigh(self.h, None, C128, 0, ctypes.byref(E)))
+            return E.value
+        v = np.ascontiguousarray(v)
         _check(self.h, lib().esc_rayleigh(self.h, _ptr(v), _dt(v), flags, ctypes.byref(E)))
         return E.value
 

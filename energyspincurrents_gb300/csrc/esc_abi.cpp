@@ -1663,9 +1663,15 @@ extern "C" esc_status esc_plan(const esc_params* p, int tile_bits, int low_bits,
 }
 
 extern "C" esc_status esc_rayleigh(esc_handle* h, const void* v, esc_dtype dt, int flags, double* E) {
-    if (!h || !v || !E) return finish(h, ESC_ERR_PARAM, "null argument");
+    if (!h || !E) return finish(h, ESC_ERR_PARAM, "null argument");
+    if (!v && !h->have_gs) return finish(h, ESC_ERR_STATE, "no ground state: call esc_lanczos_gs first");
     return guarded(h, [&]() {
-        Staged s = stage(h, v, nullptr, 1, h->D, dt, flags);
+        // v == NULL: the handle's ground state, in place (no copy of the vector)
+        if (!v) {
+            dt = h->basis_dt;
+            flags = ESC_DEVICE_PTR | ESC_INTERNAL_ORDER;
+        }
+        Staged s = stage(h, v ? v : h->d_gs, nullptr, 1, h->D, dt, flags);
         ensure_partials(h, 4);
         std::vector<double> num;
         const int maxb = esc::RED_MAX_BLOCKS;

@@ -196,8 +196,8 @@ esc_status esc_apply_op(esc_handle* h, int op, int site, const void* in, void* o
 esc_status esc_start_vector(esc_handle* h, int kind, int seed, void* out, esc_dtype dt, int flags);
 
 /* E = <v|H|v>/<v|v> evaluated in FP64 from a complex128 or complex64 vector, pass by pass without
- * forming H v (the FP64 refinement of a mixed-precision ground-state energy).  No reference
- * counterpart. */
+ * forming H v (the FP64 refinement of a mixed-precision ground-state energy).  v == NULL: the
+ * handle's last ground state in place (dt and flags ignored).  No reference counterpart. */
 esc_status esc_rayleigh(esc_handle* h, const void* v, esc_dtype dt, int flags, double* E);
 
 /* Allocation-free variant of esc_rayleigh, for callers that cannot allocate device memory: code

@@ -487,3 +487,15 @@ def test_tuning_file_roundtrip(tmp_path, monkeypatch):
     assert relerr(h3.hv(x).astype(np.complex128),
                   O.Model("Kitaev", 3, 6, 1, 1, -1.0, -1.0, -1.0, p["Bxx"], p["Byy"], p["Bzz"], 0.2, 4,
                           False).hv(x.astype(np.complex128))) < 2e-6
+
+
+@pytest.mark.parametrize("dt", [np.complex128, np.complex64])
+def test_rayleigh_of_handle_ground_state_in_place(dt):
+    """esc_rayleigh(h, NULL, ...) evaluates the handle's ground state in place: same value as passing
+    the exported vector."""
+    h = esc.Handle(kitaev(J=0.1, seed=0, lanczos_steps=80))
+    r = h.lanczos_gs(start=O.random_start(0, h.D), lanctype="GS", reortho=0, dtype=dt)
+    e_in = h.rayleigh()
+    e_out = h.rayleigh(r["gs"])
+    assert abs(e_in - e_out) <= 1e-13 * abs(e_out)
+    assert abs(e_in - r["E0"]) <= (1e-6 if dt == np.complex64 else 1e-10) * abs(e_out)
