@@ -312,7 +312,7 @@ void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) 
     if (!esc::tridiag_eig(n, d, e, (store || recompute) ? &h->Z : nullptr)) throw Fail(ESC_ERR_NUMERIC, "diag: tridiagonal eigensolver failed");
     h->ritz = d;
     h->nsteps = n;
-    ensure(h->d_gs, h->gs_bytes, (size_t)D * 16);
+    ensure(h->d_gs, h->gs_bytes, (size_t)D * ES);
     if (recompute) {
         // second pass: identical kernels on identical inputs regenerate L_0..L_{n-1} bit for bit
         ESC_CUDA(cudaMemcpyAsync(d_z, h->Z.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
@@ -931,7 +931,9 @@ esc_status esc_apply_op(esc_handle* h, int op, int site, const void* in, void* o
 // order (the reference's draw order) and permuted; uses d_work as scratch.
 static void start_vector_internal(esc_handle* h, int kind, int seed, void* dst, esc_dtype dt) {
     const int64_t D = h->D;
-    ensure(h->d_work, h->work_bytes, std::max(h->work_bytes, (size_t)D * 16));
+    // generation buffer: complex128 staging only for the host-generated reference start vector
+    const size_t gbytes = (size_t)D * (kind == ESC_START_REFUNIFORM ? 16 : esize(dt));
+    ensure(h->d_work, h->work_bytes, std::max(h->work_bytes, gbytes));
     ensure_t(h->d_sc, h->sc_bytes, std::max<size_t>(h->sc_bytes, 64));
     void* gen = h->d_work;
     if (kind == ESC_START_REFUNIFORM) {
@@ -975,7 +977,7 @@ esc_status esc_lanczos_gs(esc_handle* h, const esc_lanczos_cfg* cfg, const void*
         Staged s = stage(h, start, nullptr, 1, D, dt, flags);
         void* d_start = (void*)s.in;
         if (!start) {
-            ensure(h->d_io, h->io_bytes, std::max(h->io_bytes, 2 * (size_t)D * esize(dt)));
+            ensure(h->d_io, h->io_bytes, std::max(h->io_bytes, (size_t)D * esize(dt)));
             d_start = h->d_io;
             start_vector_internal(h, h->p.start_vector, h->p.seed, d_start, dt);
         }
