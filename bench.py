@@ -203,6 +203,20 @@ def ground_state_report(esc, sites, steps=200):
             "tuning": tune, "vectors": "complex64, 3 resident + ground state"}
 
 
+def reduce_max(x, dist, device):
+    """Max over the ranks of a per-rank time (the slowest replica sets the job's time)."""
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_gbs(bytes_per_replica, world, ms):
+    """Whole-job throughput of `world` independent replicas that each move bytes_per_replica in
+    (at most) ms milliseconds: replicas only, no exchange between them."""
+    return world * bytes_per_replica / (ms * 1e-3) / 1e9
+
+
 def torch_sync():
     import torch
     torch.cuda.synchronize()
@@ -286,11 +300,9 @@ def main():
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1) / args.steps
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = reduce_max(ms, dist, "cuda")
     algo_bytes = D * 16                              # read v + write out, complex64
-    gbs_total = world * algo_bytes / (ms * 1e-3) / 1e9
+    gbs_total = replicas_gbs(algo_bytes, world, ms)
     kernel_gbs = algo_bytes / (ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
     prof = traffic_from_profile() or {}
