@@ -829,14 +829,6 @@ int pass_stages() {
     return x >= 2 && x <= 4 ? x : 2;
 }
 
-static int kernel_variant() {
-    static int v = [] {
-        const char* e = std::getenv("ESC_HV_KERNEL");
-        return e ? std::atoi(e) : 0;
-    }();
-    return v;
-}
-
 template <typename R>
 void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in, void* out, int64_t D,
                      const void* diag, cudaStream_t s, const int* active) {
@@ -846,12 +838,11 @@ void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, cons
     ESC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     for (const DevPass& p : passes) {
         if constexpr (sizeof(R) == 4) {
-            if (diag && p.jit >= 0 && kernel_variant() == 0) {
+            if (diag && p.jit >= 0) {
                 jit_launch(p, make_pass_tab(p, m), diag, in, out, D, sms, s, active);
                 continue;
             }
-            if (diag && p.c == 3 && (p.Tp == 11 || p.Tp == 12) && p.tb_bits >= 7 && p.tb_bits <= 9 &&
-                kernel_variant() != 1) {
+            if (diag && p.c == 3 && (p.Tp == 11 || p.Tp == 12) && p.tb_bits >= 7 && p.tb_bits <= 9) {
                 // E = 2^(Tp - tb_bits) states per thread
                 switch ((p.tb_bits == 8 ? 100 : p.tb_bits == 7 ? 200 : 0) + (p.Tp == 11 ? 10 : 20) + p.stages) {
                     case 212: run_f32g<16, 2, 128>(m, p, diag, in, out, D, sms, s, active); break;
