@@ -86,7 +86,7 @@ def build(force=False, verbose=False):
             cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
                    *inc, "-c", path, "-o", obj]
         else:
-            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-fopenmp", *inc, "-c", path, "-o", obj]
+            cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-fopenmp", *inc, "-c", path, "-o", obj]
         jobs.append(cmd)
 
     def run(cmd):

@@ -33,14 +33,15 @@ def build(force=False):
         raise RuntimeError("reference source tree not present")
     os.makedirs(OUT, exist_ok=True)
     blas = _openblas()
-    common = ["g++", "-O2", "-std=c++17", "-fopenmp", "-w", "-I", os.path.join(HERE, "shim"),
+    common = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-w", "-I", os.path.join(HERE, "shim"),
               "-I", os.path.join(REF, "src")]
     link = [os.path.join(HERE, "lapack_bridge.cpp"), blas, "-Wl,-rpath," + os.path.dirname(blas)]
     targets = {
         "LanczosCond": os.path.join(REF, "main.cpp"),
         "golden_driver": os.path.join(HERE, "golden_driver.cpp"),
     }
-    deps = glob.glob(os.path.join(HERE, "shim", "**", "*"), recursive=True) + [os.path.join(HERE, "lapack_bridge.cpp")]
+    deps = glob.glob(os.path.join(HERE, "shim", "**", "*"), recursive=True) + [os.path.join(HERE, "lapack_bridge.cpp"),
+                                                                              os.path.abspath(__file__)]
     for name, src in targets.items():
         exe = os.path.join(OUT, name)
         if os.path.exists(exe) and not force and all(
