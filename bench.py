@@ -217,6 +217,26 @@ def replicas_gbs(bytes_per_replica, world, ms):
     return world * bytes_per_replica / (ms * 1e-3) / 1e9
 
 
+def mixed_spectrum_report(esc, sites, gs_steps=200, cf_steps=500):
+    """JeJe CF spectrum (2000 omega in [0,6], eta=0.05) of the workload entirely in complex64: the
+    ground state of a complex64 Lanczos run (three vectors) and complex64 continued fractions (the
+    complex128 head is skipped when its vectors do not fit, as at 32 sites)."""
+    import numpy as np
+    P = esc.ConstVariables(**workload(sites), omega_steps=1999, domega=6.0 / 1999, eta=0.05)
+    h = esc.Handle(P)
+    tune = h.autotune().strip().splitlines()[-1]
+    t0 = time.perf_counter()
+    r = h.lanczos_gs(steps=gs_steps, lanctype="GS", reortho=0, dtype=np.complex64, want_gs=False)
+    t1 = time.perf_counter()
+    S = h.spectrum("Energy Current", "CF", cf_steps=cf_steps)
+    t2 = time.perf_counter()
+    h.close()
+    return {"sites": sites, "kind": "JeJe, continued fraction, complex64", "gs_steps": gs_steps, "cf_steps": cf_steps,
+            "E0": r["E0"], "gs_s": round(t1 - t0, 2), "time_to_S_s": round(t2 - t1, 2),
+            "max_abs_S": float(np.abs(S[:, 1:]).max()), "omega_at_max_tt": float(S[np.abs(S[:, 5]).argmax(), 0]),
+            "tuning": tune}
+
+
 def torch_sync():
     import torch
     torch.cuda.synchronize()
@@ -233,6 +253,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-spectrum", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="skip the self-tuner (library default plan)")
+    ap.add_argument("--tts-report", action="store_true",
+                    help="time-to-S(omega) of the --sites cluster in mixed precision only (complex64 ground state and "
+                         "continued fractions; for clusters whose FP64 vectors do not fit) and print one JSON line")
     ap.add_argument("--gs-report", action="store_true",
                     help="time a mixed-precision ground state of the --sites cluster (Lanczos on complex64 vectors, "
                          "FP64 Rayleigh refinement) and print one JSON line, then exit")
@@ -257,6 +280,9 @@ def main():
         return
     if args.gs_report:
         print(json.dumps(ground_state_report(esc, args.sites)), flush=True)
+        return
+    if args.tts_report:
+        print(json.dumps(mixed_spectrum_report(esc, args.sites)), flush=True)
         return
     dist = None
     if world > 1:

@@ -182,6 +182,9 @@ void unstage(esc_handle* h, const Staged& s, void* out, int cols, int64_t ld, es
     const bool dev = flags & ESC_DEVICE_PTR, internal = flags & ESC_INTERNAL_ORDER;
     if (!(dev && internal) && out) {
         const size_t vb = (size_t)n * es;
+        // staging for the reference-order / host copy (already there when stage() made it; a
+        // result that lives elsewhere, e.g. the ground state, may need it allocated here)
+        if (!internal && !dev) ensure(h->d_io, h->io_bytes, std::max(h->io_bytes, (size_t)cols * vb));
         char* A = (char*)h->d_io;
         for (int c = 0; c < cols; c++) {
             char* dst = (char*)out + (size_t)c * ld * es;
@@ -521,47 +524,6 @@ struct Spectra {
         }
         return O;
     }
-
-    // CF-mode: Lanczos from phi = A|gs> (plain three-term recurrence, K steps) -> a, b; b[0]=|phi|.
-    void cf_coeffs(const std::vector<esc::OpTerm>& t, int K, double* d_sc, std::vector<double>& a,
-                   std::vector<double>& b) {
-        double* d_a = d_sc;             // 2K
-        double* d_b2 = d_a + 2 * K;     // K+1
-        ESC_CUDA(cudaMemsetAsync(d_sc, 0, (3 * (size_t)K + 1) * sizeof(double), h->stream));
-        int prev = 0, cur = 1, wb = 2;
-        P.apply(esc::make_dev_op(t, &h->plan.perm), h->d_gs, buf(cur));
-        P.nrm2(buf(cur), d_b2);
-        P.scale(buf(cur), buf(cur), d_b2);
-        for (int k = 0; k < K; k++) {
-            P.hv(buf(cur), buf(wb));
-            P.dot(buf(cur), buf(wb), d_a + 2 * k);
-            esc::launch_lanczos_update<R>(buf(wb), buf(cur), k ? buf(prev) : nullptr, d_a + 2 * k, k ? d_b2 + k : nullptr,
-                                          D, h->d_part, d_b2 + k + 1, h->stream);
-            P.scale(buf(wb), buf(wb), d_b2 + k + 1);
-            const int np = cur, nc = wb, nw = prev;
-            prev = np; cur = nc; wb = nw;
-        }
-        std::vector<double> ha(2 * (size_t)K), hb2(K + 1);
-        ESC_CUDA(cudaMemcpyAsync(ha.data(), d_a, ha.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-        ESC_CUDA(cudaMemcpyAsync(hb2.data(), d_b2, hb2.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-        sync(h);
-        a.clear(); b.clear();
-        const double b0 = std::sqrt(hb2[0]);
-        b.push_back(b0);
-        if (b0 == 0.0) return;
-        for (int k = 0; k < K; k++) {
-            a.push_back(ha[2 * k]);
-            const double bn = std::sqrt(hb2[k + 1]);
-            if (k + 1 == K || !(bn > 1e-10 * b0)) break;       // stop at beta < 1e-10 |phi|
-            b.push_back(bn);
-        }
-    }
-};
-
-// S_ab(omega) pieces for CF mode via polarisation: S_ab = (X - iY)/2, S_ba = (X + iY)/2 with
-// X = S(a+b) - S_aa - S_bb, Y = S(a+ib) - S_aa - S_bb.
-struct CFSet {
-    std::vector<std::vector<cplx>> S;   // per run, per omega
 };
 
 }  // namespace
@@ -994,6 +956,11 @@ esc_status esc_lanczos_gs(esc_handle* h, const esc_lanczos_cfg* cfg, const void*
             unstage(h, g, gs_out, 1, D, dt, flags & ~ESC_ASYNC);
         }
         sync(h);
+        if (h->d_io) {   // start vector and export staging are no longer needed: room for the dynamics
+            cudaFree(h->d_io);
+            h->d_io = nullptr;
+            h->io_bytes = 0;
+        }
     });
 }
 
@@ -1015,8 +982,7 @@ void spectrum_impl(esc_handle* h, const esc_dyn_cfg& cfg, std::vector<double>& o
     const double Eg = h->ritz[0];
     const int M = h->nsteps;
     const int K = cfg.cf_steps > 0 ? cfg.cf_steps : M;
-    const int nwork = ritz ? 1 : 3;
-    ensure(h->d_work, h->work_bytes, (size_t)nwork * D * Pipe<R>::ES);
+    ensure(h->d_work, h->work_bytes, (size_t)D * Pipe<R>::ES);   // one operator image at a time
     const size_t nsc = 2 * (size_t)std::max(M, 1) + 8 + 3 * (size_t)K + 8;
     ensure_t(h->d_sc, h->sc_bytes, std::max(h->sc_bytes, nsc * sizeof(double)));
     ensure_partials(h, std::max(M, 4));
