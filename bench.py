@@ -351,21 +351,32 @@ def main():
 
     # end to end through the C ABI: host buffers (pinned) in the reference basis order; the host->
     # device copy, the basis permutations, H.v and the device->host copy are inside the timed region
+    # A step is a batch of 2 vectors through esc_hv_batched when the host has room for 4 pinned
+    # vectors: the library then overlaps one vector's copy in, the other's H.v and copy out (the
+    # host link is full duplex); otherwise 1 vector through esc_hv.
     e2e = None
     if not args.no_e2e:
         try:
-            hin = torch.empty(D, dtype=torch.complex64, pin_memory=True)
-            hout = torch.empty(D, dtype=torch.complex64, pin_memory=True)
+            avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+            ncols = 2 if avail > 4 * D * 8 + (24 << 30) else 1
+            hin = torch.empty((ncols, D), dtype=torch.complex64, pin_memory=True)
+            hout = torch.empty((ncols, D), dtype=torch.complex64, pin_memory=True)
             hin.zero_()
-            h.hv(hin.numpy(), out=hout.numpy())   # warm-up (allocates the staging buffers)
+            if ncols == 1:
+                call = lambda: h.hv(hin[0].numpy(), out=hout[0].numpy())
+            else:
+                call = lambda: h.hv_batched(hin.numpy(), out=hout.numpy())
+            call()   # warm-up (allocates the staging buffers)
             reps = max(1, min(args.steps, 3))
             t0 = time.perf_counter()
             for _ in range(reps):
-                h.hv(hin.numpy(), out=hout.numpy())
+                call()
             el = (time.perf_counter() - t0) / reps
-            e2e = {"value": round(world * algo_bytes / el / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": D * 8,
-                   "d2h_bytes_per_step": D * 8, "ms_per_step": round(el * 1e3, 3),
-                   "path": "esc_hv, host pointers, reference basis order"}
+            e2e = {"value": round(world * ncols * algo_bytes / el / 1e9, 3), "unit": "GB/s",
+                   "h2d_bytes_per_step": ncols * D * 8, "d2h_bytes_per_step": ncols * D * 8,
+                   "ms_per_step": round(el * 1e3, 3), "vectors_per_step": ncols,
+                   "path": ("esc_hv_batched (2 columns, copies overlapped with H.v)" if ncols == 2 else "esc_hv") +
+                           ", host pointers, reference basis order"}
             del hin, hout
         except Exception as ex:
             e2e = {"value": None, "unit": "GB/s", "error": str(ex)[:200]}

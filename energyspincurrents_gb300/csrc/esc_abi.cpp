@@ -31,6 +31,10 @@ struct esc_handle {
     int64_t D = 0;
     int device = 0;
     cudaStream_t stream = nullptr;
+    // copy streams and per-slot events of the pipelined host-buffer batches (created on first use)
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_afree[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr},
+                ev_outfree[2] = {nullptr, nullptr};
     std::string err;
     // device memory owned by the handle
     double* d_part = nullptr; size_t part_bytes = 0;   // reduction partials
@@ -814,6 +818,11 @@ esc_status esc_destroy(esc_handle* h) {
                     h->d_cfb, (void*)h->d_cfs, (void*)h->d_cfi})
         if (p) cudaFree(p);
     if (h->stream) cudaStreamDestroy(h->stream);
+    for (cudaStream_t x : {h->s_in, h->s_out})
+        if (x) cudaStreamDestroy(x);
+    for (int i = 0; i < 2; i++)
+        for (cudaEvent_t e : {h->ev_in[i], h->ev_afree[i], h->ev_out[i], h->ev_outfree[i]})
+            if (e) cudaEventDestroy(e);
     delete h;
     return ESC_OK;
 }
@@ -856,6 +865,78 @@ esc_status esc_hv(esc_handle* h, const void* in, void* out, esc_dtype dt, int fl
     });
 }
 
+}  // extern "C"
+
+namespace {
+
+// Host-buffer batch, pipelined: column c's host->device copy (stream s_in), its H.v with the
+// permutations (handle stream) and its device->host copy (stream s_out) overlap with the
+// neighbouring columns' -- the host link is full duplex, so column c+1 comes in while column c-1
+// goes out.  Two slots of three vectors: A (copy in), B (internal-order input, later the
+// reference-order result), C (internal-order result).  Events keep a slot's buffers from being
+// refilled before their last reader is done.  Returns false (nothing done) when the 6 vectors do
+// not fit.
+template <typename R>
+bool hv_host_pipelined(esc_handle* h, const char* in, char* out, int ncols, int64_t ld, const double* fields,
+                       esc_dtype dt, bool internal) {
+    const int64_t D = h->D;
+    const size_t es = esize(dt), vb = (size_t)D * es;
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { (void)cudaGetLastError(); return false; }
+    if (fr + h->io_bytes < 6 * vb + ((size_t)1 << 30)) return false;
+    ensure(h->d_io, h->io_bytes, std::max(h->io_bytes, 6 * vb));
+    if (!h->s_in) ESC_CUDA(cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking));
+    if (!h->s_out) ESC_CUDA(cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; i++)
+        for (cudaEvent_t* e : {&h->ev_in[i], &h->ev_afree[i], &h->ev_out[i], &h->ev_outfree[i]})
+            if (!*e) ESC_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    const void* dg = diag_for(h, dt);
+    // the copy streams start after the work already queued on the handle's stream
+    ESC_CUDA(cudaEventRecord(h->ev_out[0], h->stream));
+    ESC_CUDA(cudaStreamWaitEvent(h->s_in, h->ev_out[0], 0));
+    ESC_CUDA(cudaStreamWaitEvent(h->s_out, h->ev_out[0], 0));
+    for (int c = 0; c < ncols; c++) {
+        const int s = c & 1;
+        char* A = (char*)h->d_io + (size_t)(3 * s) * vb;
+        char* B = A + vb;
+        char* C = B + vb;
+        const double* b = fields ? fields + 3 * c : nullptr;
+        const esc::DevModel m = b ? model_with_field(h, b[0], b[1], b[2]) : h->dm;
+        // copy in (slot's A free once column c-2 has read it)
+        if (c >= 2) ESC_CUDA(cudaStreamWaitEvent(h->s_in, h->ev_afree[s], 0));
+        ESC_CUDA(cudaMemcpyAsync(A, in + (size_t)c * ld * es, vb, cudaMemcpyHostToDevice, h->s_in));
+        ESC_CUDA(cudaEventRecord(h->ev_in[s], h->s_in));
+        // compute (slot's result buffer free once column c-2 has been copied out)
+        ESC_CUDA(cudaStreamWaitEvent(h->stream, h->ev_in[s], 0));
+        if (c >= 2) ESC_CUDA(cudaStreamWaitEvent(h->stream, h->ev_outfree[s], 0));
+        const char* res;
+        if (internal) {
+            esc::launch_hv_tiled<R>(m, h->passes, A, C, D, dg, h->stream);
+            ESC_CUDA(cudaEventRecord(h->ev_afree[s], h->stream));
+            res = C;
+        } else {
+            permute(h, h->to_int, A, B, D, dt);
+            ESC_CUDA(cudaEventRecord(h->ev_afree[s], h->stream));
+            esc::launch_hv_tiled<R>(m, h->passes, B, C, D, dg, h->stream);
+            permute(h, h->to_ref, C, B, D, dt);
+            res = B;
+        }
+        ESC_CUDA(cudaEventRecord(h->ev_out[s], h->stream));
+        // copy out
+        ESC_CUDA(cudaStreamWaitEvent(h->s_out, h->ev_out[s], 0));
+        ESC_CUDA(cudaMemcpyAsync(out + (size_t)c * ld * es, res, vb, cudaMemcpyDeviceToHost, h->s_out));
+        ESC_CUDA(cudaEventRecord(h->ev_outfree[s], h->s_out));
+    }
+    ESC_CUDA(cudaStreamSynchronize(h->s_out));
+    ESC_CUDA(cudaStreamSynchronize(h->s_in));
+    sync(h);
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
 esc_status esc_hv_batched(esc_handle* h, const void* in, void* out, int ncols, int64_t ld, const double* fields,
                           esc_dtype dt, int flags) {
     if (!h || !in || !out) return finish(h, ESC_ERR_PARAM, "null argument");
@@ -869,6 +950,13 @@ esc_status esc_hv_batched(esc_handle* h, const void* in, void* out, int ncols, i
             f.fy[c] = 0.5 * (b ? b[1] : h->p.Byy);
             f.fz[c] = 0.5 * (b ? b[2] : h->p.Bzz);
             f.fxf[c] = (float)f.fx[c]; f.fyf[c] = (float)f.fy[c]; f.fzf[c] = (float)f.fz[c];
+        }
+        if (!(flags & ESC_DEVICE_PTR) && ncols >= 2) {
+            const bool internal = flags & ESC_INTERNAL_ORDER;
+            const bool done = dt == ESC_C64
+                                  ? hv_host_pipelined<float>(h, (const char*)in, (char*)out, ncols, ld, fields, dt, internal)
+                                  : hv_host_pipelined<double>(h, (const char*)in, (char*)out, ncols, ld, fields, dt, internal);
+            if (done) return;
         }
         Staged s = stage(h, in, out, ncols, ld, dt, flags);
         if (dt == ESC_C64) esc::launch_hv_batched<float>(h->dm, f, s.in, s.out, ncols, s.ld, h->D, h->stream);
