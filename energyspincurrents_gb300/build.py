@@ -24,7 +24,8 @@ EXE = os.path.join(OUT, "LanczosCond")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kernels.cu", "hv_tiled.cu", "batched.cu", "hv_jit.cu"]
-CPP_SOURCES = ["esc_abi.cpp", "params.cpp", "model.cpp", "numerics.cpp", "planner.cpp"]
+CPP_SOURCES = ["esc_abi.cpp", "lanczos.cpp", "spectra.cpp", "grad.cpp", "tune.cpp", "params.cpp", "model.cpp", "numerics.cpp",
+               "planner.cpp"]
 
 
 def _nvcc():

@@ -1,11 +1,11 @@
-// esc_abi.cpp -- the C ABI (include/esc.h): handle, operators, GPU Lanczos, spectra.
+// esc_abi.cpp -- the C ABI (include/esc.h): handle life cycle, staging of vectors across the
+// boundary, H.v, operators, start vectors, and the entry points whose work lives in lanczos.cpp,
+// spectra.cpp, grad.cpp and tune.cpp.
 //
-// Host C++ drives hand-written sm_103a kernels (kernels.cu).  No CPU fallback exists: every
-// vector operation runs on the device; the host only does O(M^2)-O(M^3) work on the tridiagonal
-// matrix and the O(Omega x M) Lehmann / continued-fraction sums.
+// Host C++ drives hand-written sm_103a kernels.  No CPU fallback exists: every vector operation
+// runs on the device; the host only does O(M^2)-O(M^3) work on the tridiagonal matrix and the
+// O(Omega x M) Lehmann / continued-fraction sums.
 #include <algorithm>
-#include <map>
-#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -15,85 +15,25 @@
 #include <string>
 #include <type_traits>
 
-#include "esc_internal.h"
+#include "abi_common.h"
 
 using esc::cplx;
-
-struct esc_handle {
-    esc_params p{};
-    esc::Lattice L;
-    std::vector<esc::Bond> bonds;
-    esc::DevModel dm{};                 // model on relabelled sites (internal basis order)
-    esc::Plan plan;                     // site relabelling + pass plan of the tiled H.v
-    std::vector<esc::DevPass> passes;
-    esc::DevPerm to_int{}, to_ref{};    // basis permutations reference <-> internal
-    int N = 0;
-    int64_t D = 0;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    // copy streams and per-slot events of the pipelined host-buffer batches (created on first use)
-    cudaStream_t s_in = nullptr, s_out = nullptr;
-    cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_afree[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr},
-                ev_outfree[2] = {nullptr, nullptr};
-    std::string err;
-    // device memory owned by the handle
-    double* d_part = nullptr; size_t part_bytes = 0;   // reduction partials
-    double* d_sc = nullptr; size_t sc_bytes = 0;       // scalars (alpha, |w|^2, projections, ...)
-    void* d_L = nullptr; size_t L_bytes = 0;           // Krylov basis
-    void* d_work = nullptr; size_t work_bytes = 0;     // work vectors
-    void* d_gs = nullptr; size_t gs_bytes = 0;         // ground state
-    void* d_io = nullptr; size_t io_bytes = 0;         // staging for host-pointer calls
-    void* d_cfb = nullptr; size_t cfb_bytes = 0;       // batched CF vectors (3 x ncols x D)
-    double* d_cfs = nullptr; size_t cfs_bytes = 0;     // batched CF scalars
-    int* d_cfi = nullptr; size_t cfi_bytes = 0;        // batched CF flags / counters
-    void* d_diag[2] = {nullptr, nullptr};              // diagonal of the bond terms per dtype
-    size_t diag_bytes[2] = {0, 0};
-    // ground-state Lanczos results
-    int nsteps = 0;
-    bool have_gs = false, have_basis = false;
-    esc_dtype basis_dt = ESC_C128;
-    int64_t L_ld = 0;
-    std::vector<double> alpha, beta, ritz, Z;
-};
+using namespace escabi;
 
 namespace {
 
 thread_local std::string g_err;
 
-struct Fail : std::runtime_error {
-    esc_status st;
-    Fail(esc_status s, const std::string& m) : std::runtime_error(m), st(s) {}
-};
-
 }  // namespace
 
 void esc::set_last_error(const std::string& msg) { g_err = msg; }
 
-namespace {
+namespace escabi {
 
 esc_status finish(esc_handle* h, esc_status st, const std::string& msg) {
     g_err = msg;
     if (h) h->err = msg;
     return st;
-}
-
-template <typename F>
-esc_status guarded(esc_handle* h, F&& f) {
-    try {
-        f();
-        if (h) h->err.clear();
-        return ESC_OK;
-    } catch (Fail& e) {
-        return finish(h, e.st, e.what());
-    } catch (esc::CudaError& e) {
-        return finish(h, ESC_ERR_CUDA, e.what());
-    } catch (std::invalid_argument& e) {
-        return finish(h, ESC_ERR_PARAM, e.what());
-    } catch (std::bad_alloc&) {
-        return finish(h, ESC_ERR_MEMORY, "host allocation failed");
-    } catch (std::exception& e) {
-        return finish(h, ESC_ERR_NUMERIC, e.what());
-    }
 }
 
 size_t esize(esc_dtype dt) { return dt == ESC_C64 ? 8 : 16; }
@@ -111,13 +51,6 @@ void ensure(void*& p, size_t& cap, size_t need) {
     }
     cap = need;
 }
-template <typename T>
-void ensure_t(T*& p, size_t& cap, size_t need) {
-    void* q = p;
-    ensure(q, cap, need);
-    p = (T*)q;
-}
-
 void sync(esc_handle* h) { ESC_CUDA(cudaStreamSynchronize(h->stream)); }
 
 // Precomputed bond diagonal (the analogue of the reference's HDiag without the field term),
@@ -152,11 +85,6 @@ void permute(esc_handle* h, const esc::DevPerm& p, const void* in, void* out, in
 // Staged input/output.  The kernels work in the internal basis order; unless the caller says
 // ESC_INTERNAL_ORDER, inputs are permuted in and outputs permuted out (through d_io), and host
 // pointers are copied.  One call handles `cols` vectors of `n` elements with stride `ld`.
-struct Staged {
-    const void* in;
-    void* out;
-    int64_t ld;
-};
 Staged stage(esc_handle* h, const void* in, void* out, int cols, int64_t ld, esc_dtype dt, int flags) {
     const size_t es = esize(dt);
     const int64_t n = h->D;
@@ -206,267 +134,6 @@ void unstage(esc_handle* h, const Staged& s, void* out, int cols, int64_t ld, es
     if (!(flags & ESC_ASYNC) || !dev) sync(h);
 }
 
-// ---------------------------------------------------------------------------------------------
-// Templated device pipelines
-// ---------------------------------------------------------------------------------------------
-template <typename R>
-struct Pipe {
-    esc_handle* h;
-    static constexpr size_t ES = 2 * sizeof(R);
-    int64_t D;
-    explicit Pipe(esc_handle* hh) : h(hh), D(hh->D) {}
-    void hv(const void* in, void* out) {
-        esc::launch_hv_tiled<R>(h->dm, h->passes, in, out, D, diag_for(h, sizeof(R) == 4 ? ESC_C64 : ESC_C128),
-                                h->stream);
-    }
-    void apply(const esc::DevOp& op, const void* in, void* out) { esc::launch_apply<R>(op, in, out, D, h->stream); }
-    void dot(const void* a, const void* b, double* dst) { esc::launch_dot<R>(a, b, D, h->d_part, dst, h->stream); }
-    void nrm2(const void* a, double* dst) { esc::launch_nrm2<R>(a, D, h->d_part, dst, h->stream); }
-    void scale(const void* in, void* out, const double* d_nrm2) { esc::launch_scale_rsqrt<R>(in, out, d_nrm2, D, h->stream); }
-};
-
-// Ground-state Lanczos, DynLanczosSolver::Lanczos_Nirav (src/DynLanczosSolver.h:38-239).
-template <typename R>
-void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) {
-    Pipe<R> P(h);
-    const int64_t D = h->D;
-    const size_t ES = Pipe<R>::ES;
-    const int M = cfg.steps;
-    // GS without reorthogonalisation keeps three vectors and rebuilds |gs> in a second pass
-    // (the Lanczos vectors are recomputed from the recorded alpha/beta, not stored): the mode for
-    // bases too large to hold M+1 vectors (N = 28..32).
-    const bool recompute = cfg.lanctype == 1 && !cfg.reortho;
-    const bool store = cfg.lanctype != 0 && !recompute;  // OnlyEgs keeps no basis (returns a zero vector)
-    const bool reo = store && cfg.reortho;
-    const int nvec = store ? M + 1 : 3;
-    h->have_gs = h->have_basis = false;
-    ensure(h->d_L, h->L_bytes, (size_t)nvec * D * ES);
-    ensure(h->d_work, h->work_bytes, (size_t)D * ES);
-    // scalars: alpha[2M] | b2[M+2] | tmp[8] | r[2(M+2)] | z[M+2]
-    const size_t n_sc = 2 * (size_t)M + (M + 2) + 8 + 2 * (size_t)(M + 2) + (M + 2);
-    ensure_t(h->d_sc, h->sc_bytes, n_sc * sizeof(double));
-    double* d_alpha = h->d_sc;
-    double* d_b2 = d_alpha + 2 * M;
-    double* d_tmp = d_b2 + (M + 2);
-    double* d_r = d_tmp + 8;
-    double* d_z = d_r + 2 * (M + 2);
-    ensure_partials(h, reo ? M + 2 : 4);
-    ESC_CUDA(cudaMemsetAsync(h->d_sc, 0, n_sc * sizeof(double), h->stream));
-    auto Lv = [&](int i) -> char* { return (char*)h->d_L + (size_t)(store ? i : i % 3) * D * ES; };
-    void* w = h->d_work;
-
-    // Vorig.normalize(); V0 = Vorig (:58-66)
-    P.nrm2(d_start, d_tmp);
-    P.scale(d_start, Lv(0), d_tmp);
-    // iteration 0 (:75-83): V1 = H V0; alpha0 = <V0|V1>; V1 -= alpha0 V0; beta1 = |V1|; normalise
-    P.hv(Lv(0), w);
-    P.dot(Lv(0), w, d_alpha);
-    esc::launch_lanczos_update<R>(w, Lv(0), nullptr, d_alpha, nullptr, D, h->d_part, d_b2 + 1, h->stream);
-    P.scale(w, Lv(1), d_b2 + 1);
-    int exit_iter = M - 1;
-    double E0 = 1.0;
-    for (int iter = 1; iter <= M - 1; iter++) {             // :91-163
-        P.hv(Lv(iter), w);
-        P.dot(Lv(iter), w, d_alpha + 2 * iter);
-        esc::launch_lanczos_update<R>(w, Lv(iter), Lv(iter - 1), d_alpha + 2 * iter, d_b2 + iter, D, h->d_part,
-                                      d_b2 + iter + 1, h->stream);
-        P.scale(w, Lv(iter + 1), d_b2 + iter + 1);
-        if (reo) {
-            // Full reorthogonalisation against L_0..L_iter (:105-119).  The reference does one
-            // modified Gram-Schmidt sweep; here two classical sweeps (CGS2) as two GEMV pairs,
-            // which orthogonalise to the same working precision.
-            for (int pass = 0; pass < 2; pass++) {
-                esc::launch_gemv_h<R>(h->d_L, D, iter + 1, Lv(iter + 1), D, h->d_part, part_cap_doubles(h), d_r,
-                                      h->stream);
-                esc::launch_gemv_sub<R>(h->d_L, D, iter + 1, d_r, Lv(iter + 1), D, h->stream);
-            }
-            P.nrm2(Lv(iter + 1), d_tmp + 1);
-            P.scale(Lv(iter + 1), Lv(iter + 1), d_tmp + 1);
-        }
-        if (cfg.eps > 0.0) {                                 // :125-151 (convergence test)
-            std::vector<double> a(2 * (iter + 1)), b2(iter + 2);
-            ESC_CUDA(cudaMemcpyAsync(a.data(), d_alpha, a.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-            ESC_CUDA(cudaMemcpyAsync(b2.data(), d_b2, b2.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-            sync(h);
-            std::vector<double> d(iter + 1), e(iter + 1, 0.0);
-            for (int i = 0; i <= iter; i++) d[i] = a[2 * i];
-            for (int i = 0; i < iter; i++) e[i] = std::sqrt(b2[i + 1]);
-            if (!esc::tridiag_eig(iter + 1, d, e, nullptr)) throw Fail(ESC_ERR_NUMERIC, "diag: tridiagonal eigensolver failed");
-            const double diff = std::fabs(E0 - d[0]);
-            E0 = d[0];
-            if (diff < cfg.eps) { exit_iter = iter; break; }
-        }
-    }
-    const int n = exit_iter + 1;                             // EXITiter (:164)
-    std::vector<double> a(2 * (size_t)M), b2(M + 2);
-    ESC_CUDA(cudaMemcpyAsync(a.data(), d_alpha, a.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    ESC_CUDA(cudaMemcpyAsync(b2.data(), d_b2, b2.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    sync(h);
-    h->alpha.assign(n, 0.0);
-    h->beta.assign(n + 1, 0.0);
-    for (int i = 0; i < n; i++) h->alpha[i] = a[2 * i];
-    for (int i = 1; i <= n; i++) h->beta[i] = std::sqrt(b2[i]);
-    for (int i = 0; i < n; i++)
-        if (!std::isfinite(h->alpha[i]) || !std::isfinite(h->beta[i + 1]))
-            throw Fail(ESC_ERR_NUMERIC, "NaN/Inf in Lanczos coefficients at step " + std::to_string(i));
-    for (int i = 1; i < n; i++)
-        if (h->beta[i] == 0.0)
-            throw Fail(ESC_ERR_NUMERIC, "Lanczos breakdown: beta=0 at step " + std::to_string(i) +
-                                            " (Krylov space exhausted; use fewer LanczosSteps)");
-    std::vector<double> d(h->alpha), e(n, 0.0);
-    for (int i = 0; i < n - 1; i++) e[i] = h->beta[i + 1];
-    h->Z.clear();
-    if (!esc::tridiag_eig(n, d, e, (store || recompute) ? &h->Z : nullptr)) throw Fail(ESC_ERR_NUMERIC, "diag: tridiagonal eigensolver failed");
-    h->ritz = d;
-    h->nsteps = n;
-    ensure(h->d_gs, h->gs_bytes, (size_t)D * ES);
-    if (recompute) {
-        // second pass: identical kernels on identical inputs regenerate L_0..L_{n-1} bit for bit
-        ESC_CUDA(cudaMemcpyAsync(d_z, h->Z.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-        ESC_CUDA(cudaMemsetAsync(h->d_gs, 0, (size_t)D * ES, h->stream));
-        P.nrm2(d_start, d_tmp);
-        P.scale(d_start, Lv(0), d_tmp);
-        esc::launch_axpy_dev<R>(Lv(0), h->d_gs, d_z, D, h->stream);
-        for (int it = 0; it + 1 < n; it++) {
-            P.hv(Lv(it), w);
-            esc::launch_lanczos_update<R>(w, Lv(it), it ? Lv(it - 1) : nullptr, d_alpha + 2 * it, it ? d_b2 + it : nullptr,
-                                          D, h->d_part, d_tmp + 2, h->stream);
-            P.scale(w, Lv(it + 1), d_b2 + it + 1);
-            esc::launch_axpy_dev<R>(Lv(it + 1), h->d_gs, d_z + it + 1, D, h->stream);
-        }
-    } else if (store) {
-        // PsiAll[0] = sum_m L_m Z(m,0) (:208-234), without forming the other Ritz vectors
-        ESC_CUDA(cudaMemcpyAsync(d_z, h->Z.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-        esc::launch_lincomb<R>(h->d_L, D, n, d_z, h->d_gs, D, h->stream);
-        h->have_basis = cfg.lanctype == 2;
-    } else {
-        ESC_CUDA(cudaMemsetAsync(h->d_gs, 0, (size_t)D * ES, h->stream));   // OnlyEgs returns zeros (:178-180)
-    }
-    if ((recompute || store) && !reo) {
-        // Without reorthogonalisation the Lanczos vectors lose orthogonality once the ground state
-        // has converged, and sum_m Z(m,0) L_m is then not a unit vector: normalise it.  (With full
-        // reorthogonalisation, the reference's mode, the sum is kept exactly as the reference forms it.)
-        P.nrm2(h->d_gs, d_tmp + 3);
-        P.scale(h->d_gs, h->d_gs, d_tmp + 3);
-    }
-    if (!store && h->d_L) {   // the three recurrence vectors are not needed any more: free them for the dynamics
-        cudaFree(h->d_L);
-        h->d_L = nullptr;
-        h->L_bytes = 0;
-    }
-    h->basis_dt = sizeof(R) == 8 ? ESC_C128 : ESC_C64;
-    h->L_ld = D;
-    h->have_gs = true;
-    sync(h);
-}
-
-// ---------------------------------------------------------------------------------------------
-// Batched continued-fraction Lanczos (batched.cu)
-// ---------------------------------------------------------------------------------------------
-int cf_batch_width(esc_handle* h, size_t es, int want) {
-    size_t fr = 0, tot = 0;
-    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { (void)cudaGetLastError(); fr = 0; }
-    const size_t per = 3 * (size_t)h->D * es;
-    const size_t have = fr + h->cfb_bytes;
-    int w = (int)std::min<size_t>((size_t)want, have > (size_t)1 << 30 ? (have - ((size_t)1 << 30)) / per : 0);
-    return std::max(1, std::min(w, esc::MAX_COLS));
-}
-
-// Start vectors must already be in column slots of set 1 of d_cfb.  Returns a (Re alpha),
-// b (b[0] = |phi|) and the number of steps per column.
-//
-// head > 0 (complex64 columns only): the first `head` iterations run on complex128 copies of the
-// columns; the last two vectors are then rounded to complex64 and the recurrence continues in
-// complex64 from iteration `head`.  The leading iterations fix the converged, low-lying poles of
-// the continued fraction, so their rounding in FP32 is what costs accuracy; the tail only adds
-// resolution.  The head needs 3 x ncols complex128 vectors for its duration; without that much
-// free device memory the run is all complex64.
-template <typename R>
-void cf_batch_run(esc_handle* h, int ncols, int kmax, const std::vector<int>& steps, const std::vector<esc::DevModel>& ms,
-                  double tol, bool graph, std::vector<std::vector<double>>& A, std::vector<std::vector<double>>& B,
-                  int head = 0) {
-    const size_t nd = (size_t)ncols * esc::CFB_GRID * 2 + (size_t)ncols * kmax * 2 + (size_t)ncols * (kmax + 1);
-    ensure_t(h->d_cfs, h->cfs_bytes, nd * sizeof(double));
-    ensure_t(h->d_cfi, h->cfi_bytes, (2 * (size_t)ncols + 2) * sizeof(int));
-    auto setup = [&](auto& cb, void* bufs, const void* dg) {
-        typedef typename std::remove_reference<decltype(cb)>::type CB;
-        cb.ncols = ncols; cb.kmax = kmax; cb.D = h->D; cb.tol = tol; cb.use_graph = graph;
-        cb.bufs = bufs;
-        cb.d_part = h->d_cfs;
-        cb.d_alpha = cb.d_part + (size_t)ncols * esc::CFB_GRID * 2;
-        cb.d_b2 = cb.d_alpha + (size_t)ncols * kmax * 2;
-        cb.d_active = h->d_cfi;
-        cb.d_steps = h->d_cfi + ncols;
-        cb.d_it = h->d_cfi + 2 * ncols;
-        typedef typename std::conditional<std::is_same<CB, esc::CFBatch<float>>::value, float, double>::type RR;
-        cb.hv_column = [h, &ms, dg](int c, const void* in, void* out, const int* active, cudaStream_t s) {
-            esc::launch_hv_tiled<RR>(ms[c], h->passes, in, out, h->D, dg, s, active);
-        };
-    };
-    ESC_CUDA(cudaMemsetAsync(h->d_cfs, 0, nd * sizeof(double), h->stream));
-    esc::CFBatch<R> cb;
-    setup(cb, h->d_cfb, diag_for(h, sizeof(R) == 4 ? ESC_C64 : ESC_C128));
-    head = std::min(head, kmax);
-    void* dd = nullptr;
-    if (sizeof(R) == 4 && head > 0) {
-        const size_t vs = (size_t)ncols * h->D;   // states per set
-        size_t fr = 0, tot = 0;
-        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { (void)cudaGetLastError(); fr = 0; }
-        const size_t need = 3 * vs * 16 + (h->d_diag[0] ? 0 : (size_t)h->D * 8);
-        if (fr > need + ((size_t)1 << 30) && cudaMalloc(&dd, 3 * vs * 16) == cudaSuccess) {
-            char* d1 = (char*)dd + vs * 16;
-            esc::launch_convert_c64_to_c128((char*)h->d_cfb + vs * 8, d1, (int64_t)vs, h->stream);
-            std::vector<int> hs(ncols);
-            for (int c = 0; c < ncols; c++) hs[c] = std::min(steps[c], head);
-            ESC_CUDA(cudaMemcpyAsync(cb.d_steps, hs.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, h->stream));
-            esc::CFBatch<double> c64;
-            setup(c64, dd, diag_for(h, ESC_C128));
-            c64.run(h->stream);   // synchronises
-            // columns that ran the whole head without stopping continue in complex64
-            std::vector<double> b2((size_t)ncols * (kmax + 1));
-            ESC_CUDA(cudaMemcpy(b2.data(), cb.d_b2, b2.size() * sizeof(double), cudaMemcpyDeviceToHost));
-            std::vector<int> act(ncols, 0);
-            for (int c = 0; c < ncols; c++) {
-                const double b0 = std::sqrt(b2[(size_t)c * (kmax + 1)]);
-                bool live = b0 > 0.0 && steps[c] > head;
-                for (int k = 1; live && k <= head; k++)
-                    if (!(std::sqrt(b2[(size_t)c * (kmax + 1) + k]) > tol * b0)) live = false;
-                act[c] = live ? 1 : 0;
-            }
-            for (int j = 0; j < 2; j++) {
-                const int set = (head + j) % 3;
-                esc::launch_convert_c128_to_c64((char*)dd + set * vs * 16, (char*)h->d_cfb + set * vs * 8, (int64_t)vs,
-                                                h->stream);
-            }
-            ESC_CUDA(cudaMemcpyAsync(cb.d_active, act.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, h->stream));
-            sync(h);
-            cudaFree(dd);
-            cb.start_it = head;
-        } else {
-            (void)cudaGetLastError();
-            dd = nullptr;
-        }
-    }
-    ESC_CUDA(cudaMemcpyAsync(cb.d_steps, steps.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, h->stream));
-    cb.run(h->stream);
-    std::vector<double> al((size_t)ncols * kmax * 2), b2((size_t)ncols * (kmax + 1));
-    ESC_CUDA(cudaMemcpyAsync(al.data(), cb.d_alpha, al.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    ESC_CUDA(cudaMemcpyAsync(b2.data(), cb.d_b2, b2.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    sync(h);
-    A.assign(ncols, {});
-    B.assign(ncols, {});
-    for (int c = 0; c < ncols; c++) {
-        const double b0 = std::sqrt(b2[(size_t)c * (kmax + 1)]);
-        B[c].push_back(b0);
-        if (b0 == 0.0) continue;
-        for (int k = 0; k < kmax; k++) {
-            A[c].push_back(al[((size_t)c * kmax + k) * 2]);
-            const double bn = std::sqrt(b2[(size_t)c * (kmax + 1) + k + 1]);
-            B[c].push_back(bn);
-            if (k + 1 >= steps[c] || !(bn > tol * b0)) break;
-        }
-    }
-}
 
 esc::DevModel model_with_field(const esc_handle* h, double bx, double by, double bz) {
     esc::DevModel m = h->dm;
@@ -475,67 +142,12 @@ esc::DevModel model_with_field(const esc_handle* h, double bx, double by, double
     return m;
 }
 
-// ---------------------------------------------------------------------------------------------
-// Spectra
-// ---------------------------------------------------------------------------------------------
-struct Grid {
-    int nw;
-    double dw, eta;
-};
-
-// One operator "channel": a combination of operator strings applied to |gs>.
-std::vector<esc::OpTerm> combine(const std::vector<esc::OpTerm>& a, const std::vector<esc::OpTerm>& b, cplx cb) {
-    std::vector<esc::OpTerm> t(a);
-    for (auto x : b) { x.coef *= cb; t.push_back(x); }
-    return t;
-}
-
-template <typename R>
-struct Spectra {
-    esc_handle* h;
-    Pipe<R> P;
-    const int64_t D;
-    char* buf(int i) { return (char*)h->d_work + (size_t)i * D * Pipe<R>::ES; }
-    explicit Spectra(esc_handle* hh) : h(hh), P(hh), D(hh->D) {}
-
-    // <gs| A |gs> with A given as terms; uses work vector `slot`.
-    cplx expect(const std::vector<esc::OpTerm>& t, int slot, double* d_tmp) {
-        P.apply(esc::make_dev_op(t, &h->plan.perm), h->d_gs, buf(slot));
-        P.dot(h->d_gs, buf(slot), d_tmp);
-        double r[2];
-        ESC_CUDA(cudaMemcpyAsync(r, d_tmp, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-        sync(h);
-        return cplx(r[0], r[1]);
-    }
-
-    // Ritz-mode overlaps O[n] = <psi_n | A gs> = sum_m Z(m,n) <L_m | A gs>  (dynamics.h:256-263)
-    std::vector<cplx> ritz_overlaps(const std::vector<esc::OpTerm>& t, int slot, double* d_r, double* d_tmp,
-                                    cplx* elastic) {
-        const int M = h->nsteps;
-        P.apply(esc::make_dev_op(t, &h->plan.perm), h->d_gs, buf(slot));
-        P.dot(h->d_gs, buf(slot), d_tmp);
-        esc::launch_gemv_h<R>(h->d_L, h->L_ld, M, buf(slot), D, h->d_part, part_cap_doubles(h), d_r, h->stream);
-        std::vector<double> r(2 * (size_t)M), el(2);
-        ESC_CUDA(cudaMemcpyAsync(r.data(), d_r, r.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-        ESC_CUDA(cudaMemcpyAsync(el.data(), d_tmp, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-        sync(h);
-        *elastic = cplx(el[0], el[1]);
-        std::vector<cplx> O(M);
-        for (int n = 0; n < M; n++) {
-            cplx s(0, 0);
-            for (int m = 0; m < M; m++) s += h->Z[(size_t)n * M + m] * cplx(r[2 * m], r[2 * m + 1]);
-            O[n] = s;
-        }
-        return O;
-    }
-};
-
-}  // namespace
+}  // namespace escabi
 
 // =============================================================================================
 // C ABI
 // =============================================================================================
-namespace {
+namespace escabi {
 
 std::vector<std::pair<int, int>> bond_pairs(const esc_handle* h) {
     std::vector<std::pair<int, int>> pairs;
@@ -546,7 +158,7 @@ std::vector<std::pair<int, int>> bond_pairs(const esc_handle* h) {
 
 // Installs a site relabelling + pass plan: relabelled model, passes, basis permutations.  The
 // bond diagonal depends on the relabelling, so cached diagonal vectors are dropped.
-void install_plan(esc_handle* h, const esc::Plan& plan, int balance, int stages, int tb_bits = 0) {
+void install_plan(esc_handle* h, const esc::Plan& plan, int balance, int stages, int tb_bits) {
     h->plan = plan;
     std::vector<esc::Bond> rb(h->bonds);
     for (auto& b : rb) { b.i = h->plan.perm[b.i]; b.j = h->plan.perm[b.j]; }
@@ -566,7 +178,7 @@ void install_plan(esc_handle* h, const esc::Plan& plan, int balance, int stages,
 
 // Run-time specialised complex64 passes (hv_jit.cu): ESC_JIT=0 off, =1 on, =require on and an
 // error if it fails; by default on from 2^22 states, where the compile time is repaid.
-void specialise(esc_handle* h, std::vector<esc::DevPass>& passes, int force = -1) {
+void specialise(esc_handle* h, std::vector<esc::DevPass>& passes, int force) {
     const char* je = std::getenv("ESC_JIT");
     bool jit = je ? std::strcmp(je, "0") != 0 : h->D >= (int64_t(1) << 22);
     if (force >= 0) jit = force == 1;
@@ -576,185 +188,7 @@ void specialise(esc_handle* h, std::vector<esc::DevPass>& passes, int force = -1
         throw Fail(ESC_ERR_CUDA, "run-time specialisation of the H.v passes failed: " + err);
 }
 
-// Tuning file (ESC_TUNE_FILE): one line per tuned Hamiltonian and device,
-//   <key> | T balance npasses | jit,stages,tb_bits per pass
-// written by the self-tuner and applied by esc_create, so a tuned configuration is reused without
-// timing again.  The key covers the device name and everything the plan and passes depend on.
-std::string tune_key(const esc_handle* h) {
-    cudaDeviceProp pr{};
-    if (cudaGetDeviceProperties(&pr, h->device) != cudaSuccess) (void)cudaGetLastError();
-    std::ostringstream k;
-    k.precision(17);
-    k << "dev=" << pr.name << " model=" << h->p.model << " Lx=" << h->p.Lx << " Ly=" << h->p.Ly << " pbc=" << h->p.pbcx
-      << h->p.pbcy << " K=" << h->p.Kxx << "," << h->p.Kyy << "," << h->p.Kzz << " B=" << h->p.Bxx << "," << h->p.Byy << ","
-      << h->p.Bzz << " J=" << h->p.jheis;
-    return k.str();
-}
-
-void save_tuning(const esc_handle* h, int T, int balance, const std::vector<esc::DevPass>& ps) {
-    const char* f = std::getenv("ESC_TUNE_FILE");
-    if (!f || !*f) return;
-    FILE* fp = std::fopen(f, "a");
-    if (!fp) return;
-    std::fprintf(fp, "%s | %d %d %d |", tune_key(h).c_str(), T, balance, (int)ps.size());
-    for (const auto& p : ps) std::fprintf(fp, " %d,%d,%d", p.jit >= 0 ? 1 : 0, p.stages, p.tb_bits);
-    std::fprintf(fp, "\n");
-    std::fclose(fp);
-}
-
-// Applies the last matching line of ESC_TUNE_FILE; false if there is none.
-bool load_tuning(esc_handle* h) {
-    const char* f = std::getenv("ESC_TUNE_FILE");
-    if (!f || !*f) return false;
-    FILE* fp = std::fopen(f, "r");
-    if (!fp) return false;
-    const std::string key = tune_key(h);
-    std::string found;
-    char line[4096];
-    while (std::fgets(line, sizeof line, fp)) {
-        std::string l(line);
-        if (l.compare(0, key.size(), key) == 0 && l.size() > key.size() && l[key.size()] == ' ') found = l.substr(key.size());
-    }
-    std::fclose(fp);
-    if (found.empty()) return false;
-    int T = 0, balance = 0, n = 0;
-    std::istringstream in(found);
-    char bar;
-    in >> bar >> T >> balance >> n >> bar;
-    std::vector<std::array<int, 3>> var(n);
-    for (auto& v : var) {
-        char c1, c2;
-        in >> v[0] >> c1 >> v[1] >> c2 >> v[2];
-    }
-    if (!in || T < 4) return false;
-    const esc::Plan plan = esc::make_plan(h->N, bond_pairs(h), T, 3, 200);
-    if ((int)plan.tiles.size() != n) return false;
-    install_plan(h, plan, balance, 2);
-    std::vector<esc::DevPass> comp(h->passes);
-    std::map<std::array<int, 2>, std::vector<esc::DevPass>> built;
-    for (int p = 0; p < n; p++) {
-        const std::array<int, 2> k{var[p][1], var[p][2]};
-        if (!built.count(k)) {
-            built[k] = esc::make_passes(h->plan, h->dm, balance, k[0], k[1]);
-            if (std::any_of(var.begin(), var.end(), [&](const std::array<int, 3>& x) { return x[0] && x[1] == k[0] && x[2] == k[1]; })) {
-                std::vector<esc::DevPass> sp = built[k];
-                std::string err;
-                if (esc::jit_compile(sp, err)) built[std::array<int, 2>{-k[0], k[1]}] = sp;
-            }
-        }
-        const auto it = built.find(var[p][0] ? std::array<int, 2>{-k[0], k[1]} : k);
-        comp[p] = (it != built.end() ? it->second : built[k])[p];
-    }
-    h->passes = comp;
-    return true;
-}
-
-// Self-tuning of the complex64 H.v.  Plans: tile bits T in {11, 12, 13} (above 26 sites only 12:
-// the others never win there -- one more pass, or one CTA per SM) x first-fit / group-minimising
-// term-to-pass assignment (make_passes modes 0 and 2; the balanced mode 1 never won).  Kernel variants per plan: ahead-of-time vs run-time specialised;
-// 512, 256 or 128 threads per 4096-state tile (8, 16, 32 register states each); 2 or 3 tile buffers,
-// or 2 plus staged epilogue loads.  Every variant is timed pass by pass (CUDA events on the
-// handle's stream, median of 3 after a warm-up); a plan's composite takes the fastest variant of
-// each pass (light and heavy passes prefer different variants) and is timed as a whole; the
-// fastest composite is installed.  All variants compute the same H.v up to complex64 rounding (the
-// tests hold each to the oracle).  Needs two complex64 vectors of scratch; refuses once a ground
-// state exists (a new plan relabels the internal basis).
-std::string autotune(esc_handle* h, std::vector<double>* times) {
-    if (h->have_gs) throw Fail(ESC_ERR_STATE, "autotune before the first Lanczos run (it may relabel the basis)");
-    const int64_t D = h->D;
-    void* buf = nullptr;
-    ESC_CUDA(cudaMalloc(&buf, (size_t)D * 16));
-    void* v = buf;
-    void* w = (char*)buf + (size_t)D * 8;
-    esc::launch_start_normal<float>(12345, v, D, h->stream);
-    cudaEvent_t e0, e1;
-    ESC_CUDA(cudaEventCreate(&e0));
-    ESC_CUDA(cudaEventCreate(&e1));
-    auto median_ms = [&](const std::vector<esc::DevPass>& ps) {
-        const void* dg = diag_for(h, ESC_C64);
-        esc::launch_hv_tiled<float>(h->dm, ps, v, w, D, dg, h->stream);
-        std::vector<float> ms(3);
-        for (float& x : ms) {
-            ESC_CUDA(cudaEventRecord(e0, h->stream));
-            esc::launch_hv_tiled<float>(h->dm, ps, v, w, D, dg, h->stream);
-            ESC_CUDA(cudaEventRecord(e1, h->stream));
-            ESC_CUDA(cudaEventSynchronize(e1));
-            ESC_CUDA(cudaEventElapsedTime(&x, e0, e1));
-        }
-        std::sort(ms.begin(), ms.end());
-        return (double)ms[1];
-    };
-    std::ostringstream rep;
-    const esc::Plan keep = h->plan;
-    const std::vector<esc::DevPass> keep_passes = h->passes;
-    double best = 1e300;
-    esc::Plan bplan;
-    int bbal = 0, bT = 0;
-    std::vector<esc::DevPass> bpasses;
-    try {
-        for (int T : {11, 12, 13}) {
-            if (T > h->N || (h->N > 26 && T != 12)) continue;
-            const esc::Plan plan = esc::make_plan(h->N, bond_pairs(h), T, 3, 200);
-            for (int balance : {0, 2}) {
-                std::vector<std::vector<esc::DevPass>> vars;
-                std::vector<std::vector<double>> per;
-                for (int tb : {9, 8, 7})
-                for (int stages : {2, 3, 4})
-                    for (int jit : {0, 1}) {
-                        if (T == 13 && (jit || tb != 9)) continue;   // 8192-state tiles: generic kernel only
-                        install_plan(h, plan, balance, stages, tb);
-                        if (jit) specialise(h, h->passes, 1);
-                        bool spec = false;
-                        for (const auto& ps : h->passes) spec = spec || ps.jit >= 0;
-                        if (jit && !spec) continue;
-                        std::vector<double> t;
-                        for (const auto& ps : h->passes) t.push_back(median_ms({ps}));
-                        const double tot = median_ms(h->passes);
-                        rep << "T=" << T << " passes=" << plan.tiles.size() << " balance=" << balance << " threads="
-                            << (1 << tb) << " jit=" << jit << " stages=" << stages << ": " << tot << " ms | per pass";
-                        for (double x : t) rep << " " << x;
-                        rep << "\n";
-                        if (times) times->push_back(tot);
-                        vars.push_back(h->passes);
-                        per.push_back(t);
-                    }
-                // composite: fastest variant of each pass
-                std::vector<esc::DevPass> comp = vars[0];
-                rep << "  composite T=" << T << " balance=" << balance << ": variants";
-                for (size_t p = 0; p < comp.size(); p++) {
-                    size_t bv = 0;
-                    for (size_t k = 1; k < vars.size(); k++)
-                        if (per[k][p] < per[bv][p]) bv = k;
-                    comp[p] = vars[bv][p];
-                    rep << " " << (comp[p].jit >= 0 ? "jit" : "aot") << "/" << comp[p].stages << "/" << (1 << comp[p].tb_bits);
-                }
-                install_plan(h, plan, balance, 2);   // model, permutations, diagonal of this plan
-                const double tc = median_ms(comp);
-                rep << ": " << tc << " ms\n";
-                if (tc < best) { best = tc; bplan = plan; bbal = balance; bT = T; bpasses = comp; }
-            }
-        }
-    } catch (...) {
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        cudaFree(buf);
-        install_plan(h, keep, -1, 0);
-        h->passes = keep_passes;
-        throw;
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaFree(buf);
-    install_plan(h, bplan, bbal, 2);
-    h->passes = bpasses;
-    save_tuning(h, bT, bbal, bpasses);
-    rep << "chosen: T=" << bT << " balance=" << bbal << " passes:";
-    for (const auto& ps : bpasses) rep << " " << (ps.jit >= 0 ? "jit" : "aot") << "/" << ps.stages << "/" << (1 << ps.tb_bits);
-    rep << " (" << best << " ms)\n";
-    return rep.str();
-}
-
-}  // namespace
+}  // namespace escabi
 
 extern "C" {
 
@@ -867,7 +301,7 @@ esc_status esc_hv(esc_handle* h, const void* in, void* out, esc_dtype dt, int fl
 
 }  // extern "C"
 
-namespace {
+namespace escabi {
 
 // Host-buffer batch, pipelined: column c's host->device copy (stream s_in), its H.v with the
 // permutations (handle stream) and its device->host copy (stream s_out) overlap with the
@@ -933,7 +367,7 @@ bool hv_host_pipelined(esc_handle* h, const char* in, char* out, int ncols, int6
     return true;
 }
 
-}  // namespace
+}  // namespace escabi
 
 extern "C" {
 
@@ -979,7 +413,11 @@ esc_status esc_apply_op(esc_handle* h, int op, int site, const void* in, void* o
 
 // Start vector into `dst` (device, internal order, normalised).  Generated in the reference basis
 // order (the reference's draw order) and permuted; uses d_work as scratch.
-static void start_vector_internal(esc_handle* h, int kind, int seed, void* dst, esc_dtype dt) {
+}  // extern "C"
+
+namespace escabi {
+
+void start_vector_internal(esc_handle* h, int kind, int seed, void* dst, esc_dtype dt) {
     const int64_t D = h->D;
     // generation buffer: complex128 staging only for the host-generated reference start vector
     const size_t gbytes = (size_t)D * (kind == ESC_START_REFUNIFORM ? 16 : esize(dt));
@@ -1005,6 +443,10 @@ static void start_vector_internal(esc_handle* h, int kind, int seed, void* dst, 
     if (dt == ESC_C128) { esc::launch_nrm2<double>(dst, D, h->d_part, h->d_sc, h->stream); esc::launch_scale_rsqrt<double>(dst, dst, h->d_sc, D, h->stream); }
     else { esc::launch_nrm2<float>(dst, D, h->d_part, h->d_sc, h->stream); esc::launch_scale_rsqrt<float>(dst, dst, h->d_sc, D, h->stream); }
 }
+
+}  // namespace escabi
+
+extern "C" {
 
 esc_status esc_start_vector(esc_handle* h, int kind, int seed, void* out, esc_dtype dt, int flags) {
     if (!h || !out) return finish(h, ESC_ERR_PARAM, "null argument");
@@ -1053,546 +495,6 @@ esc_status esc_lanczos_gs(esc_handle* h, const esc_lanczos_cfg* cfg, const void*
 }
 
 }  // extern "C"
-
-namespace {
-
-// Lehmann sum helpers (src/dynamics.h:277-316, :396-425, :133-187)
-inline cplx lehmann_term(cplx a, cplx b, double w, double dE, double eta) { return std::conj(a) * b / cplx(w - dE, -eta); }
-
-template <typename R>
-void spectrum_impl(esc_handle* h, const esc_dyn_cfg& cfg, std::vector<double>& out, int& ncols) {
-    Spectra<R> S(h);
-    const int64_t D = h->D;
-    const int N = h->N;
-    const int nw = cfg.omega_steps + 1;
-    const double eta = cfg.eta;
-    const bool ritz = cfg.mode == ESC_DYNMODE_RITZ;
-    const double Eg = h->ritz[0];
-    const int M = h->nsteps;
-    const int K = cfg.cf_steps > 0 ? cfg.cf_steps : M;
-    ensure(h->d_work, h->work_bytes, (size_t)D * Pipe<R>::ES);   // one operator image at a time
-    const size_t nsc = 2 * (size_t)std::max(M, 1) + 8 + 3 * (size_t)K + 8;
-    ensure_t(h->d_sc, h->sc_bytes, std::max(h->sc_bytes, nsc * sizeof(double)));
-    ensure_partials(h, std::max(M, 4));
-    double* d_r = h->d_sc;
-    double* d_tmp = d_r + 2 * std::max(M, 1);
-    double* d_cf = d_tmp + 8;
-    auto T = [&](int op, int site) { return esc::operator_terms(op, site, h->p, h->L); };
-    auto omega = [&](int k) { return cfg.domega * k; };
-
-    // CF resolvents G_A(omega) = <A gs|(z-H)^-1|A gs>, z = omega + E0 - i eta, for a list of
-    // operators, run as columns of the batched CF Lanczos (batched.cu)
-    // default complex128 head: 24 steps for JeJe, 48 for the larger-amplitude JsJs and local
-    // spectra -- measured max |S_mixed - S_FP64| <= 3e-7 at N = 18, 24 (1000 CF steps, eta 0.05)
-    const int head = cfg.fp64_head == 0 ? (cfg.kind == ESC_DYN_JEJE ? 24 : 48) : std::max(0, cfg.fp64_head);
-    auto cf_runs = [&](const std::vector<std::vector<esc::OpTerm>>& ts) {
-        std::vector<std::vector<cplx>> G(ts.size());
-        const int width = cf_batch_width(h, Pipe<R>::ES, (int)ts.size());
-        ensure(h->d_cfb, h->cfb_bytes, std::max(h->cfb_bytes, 3 * (size_t)width * D * Pipe<R>::ES));
-        for (size_t r0 = 0; r0 < ts.size(); r0 += width) {
-            const int nc = (int)std::min<size_t>(width, ts.size() - r0);
-            char* set1 = (char*)h->d_cfb + (size_t)nc * D * Pipe<R>::ES;
-            for (int c = 0; c < nc; c++)
-                S.P.apply(esc::make_dev_op(ts[r0 + c], &h->plan.perm), h->d_gs, set1 + (size_t)c * D * Pipe<R>::ES);
-            std::vector<int> steps(nc, K);
-            std::vector<esc::DevModel> ms(nc, h->dm);
-            std::vector<std::vector<double>> A, B;
-            cf_batch_run<R>(h, nc, K, steps, ms, 1e-10, true, A, B, head);
-            for (int c = 0; c < nc; c++) {
-                std::vector<cplx> g(nw);
-                for (int k = 0; k < nw; k++)
-                    g[k] = esc::cf_eval(A[c].data(), B[c].data(), (int)A[c].size(), cplx(omega(k) + Eg, -eta));
-                G[r0 + c] = g;
-            }
-        }
-        return G;
-    };
-    auto cf_run = [&](const std::vector<esc::OpTerm>& t) { return cf_runs({t})[0]; };
-
-    if (cfg.kind == ESC_DYN_JEJE || cfg.kind == ESC_DYN_JSJS) {
-        const bool je = cfg.kind == ESC_DYN_JEJE;
-        // channels: Je -> x, y, t = x+y ; Js -> x, y, z, t = x+y+z   (dynamics.h:365-367, :244-247)
-        std::vector<std::vector<esc::OpTerm>> ch;
-        if (je) {
-            ch.push_back(T(ESC_OP_JEX_TOTAL, 0));
-            ch.push_back(T(ESC_OP_JEY_TOTAL, 0));
-            ch.push_back(combine(ch[0], ch[1], 1.0));
-        } else {
-            ch.push_back(T(ESC_OP_JSX_TOTAL, 0));
-            ch.push_back(T(ESC_OP_JSY_TOTAL, 0));
-            ch.push_back(T(ESC_OP_JSZ_TOTAL, 0));
-            ch.push_back(combine(combine(ch[0], ch[1], 1.0), ch[2], 1.0));
-        }
-        const int nc = (int)ch.size();
-        std::vector<cplx> el(nc);
-        // pairs whose off-diagonal correlation the file needs
-        std::vector<std::pair<int, int>> pairs = je ? std::vector<std::pair<int, int>>{{0, 1}}
-                                                    : std::vector<std::pair<int, int>>{{0, 1}, {0, 2}, {1, 2}};
-        // S[a][b][omega]
-        std::vector<std::vector<std::vector<cplx>>> Sab(nc, std::vector<std::vector<cplx>>(nc, std::vector<cplx>(nw)));
-        if (ritz) {
-            std::vector<std::vector<cplx>> O(nc);
-            for (int c = 0; c < nc; c++) O[c] = S.ritz_overlaps(ch[c], 0, d_r, d_tmp, &el[c]);
-            for (int k = 0; k < nw; k++) {
-                const double w = omega(k);
-                for (int a = 0; a < nc; a++)
-                    for (int b = 0; b < nc; b++) {
-                        if (!(a == b || (a < 3 && b < 3))) continue;
-                        cplx s(0, 0);
-                        for (int n = 0; n < M; n++) s = s + lehmann_term(O[a][n], O[b][n], w, h->ritz[n] - Eg, eta);
-                        Sab[a][b][k] = s;
-                    }
-            }
-        } else {
-            std::vector<std::vector<esc::OpTerm>> runs;
-            for (int c = 0; c < nc; c++) {
-                el[c] = S.expect(ch[c], 0, d_tmp);
-                runs.push_back(ch[c]);
-            }
-            // per pair: the a+b and a+ib resolvents; for JeJe a+b is the total channel t = x+y itself
-            std::vector<std::pair<int, int>> at;
-            for (auto pr : pairs) {
-                int ip = -1;
-                if (je) ip = nc - 1;
-                else { ip = (int)runs.size(); runs.push_back(combine(ch[pr.first], ch[pr.second], 1.0)); }
-                at.push_back({ip, (int)runs.size()});
-                runs.push_back(combine(ch[pr.first], ch[pr.second], cplx(0, 1)));
-            }
-            auto G = cf_runs(runs);
-            for (int c = 0; c < nc; c++) Sab[c][c] = G[c];
-            for (size_t q = 0; q < pairs.size(); q++) {
-                const int a = pairs[q].first, b = pairs[q].second;
-                const auto& Sp = G[at[q].first];
-                const auto& Sq = G[at[q].second];
-                for (int k = 0; k < nw; k++) {
-                    const cplx X = Sp[k] - Sab[a][a][k] - Sab[b][b][k];
-                    const cplx Y = Sq[k] - Sab[a][a][k] - Sab[b][b][k];
-                    Sab[a][b][k] = 0.5 * (X - cplx(0, 1) * Y);
-                    Sab[b][a][k] = 0.5 * (X + cplx(0, 1) * Y);
-                }
-            }
-        }
-        const int t = nc - 1;
-        if (je) {
-            ncols = 6;
-            out.assign((size_t)nw * ncols, 0.0);
-            for (int k = 0; k < nw; k++) {
-                const cplx dn(omega(k), -eta);
-                const cplx xx = Sab[0][0][k] - std::conj(el[0]) * el[0] / dn;
-                const cplx xy = Sab[0][1][k] - std::conj(el[0]) * el[1] / dn;
-                const cplx yy = Sab[1][1][k] - std::conj(el[1]) * el[1] / dn;
-                const cplx yx = Sab[1][0][k];   // reference subtracts conj(Jey)*Jez[0] with Jez[0] never set (:368-369,424)
-                const cplx tt = Sab[t][t][k] - std::conj(el[t]) * el[t] / dn;
-                double* r = &out[(size_t)k * ncols];
-                r[0] = omega(k); r[1] = xx.imag(); r[2] = yy.imag(); r[3] = xy.imag(); r[4] = yx.imag(); r[5] = tt.imag();
-            }
-        } else {
-            ncols = 15;
-            out.assign((size_t)nw * ncols, 0.0);
-            const int ord[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};   // dynamics.h:318-323
-            for (int k = 0; k < nw; k++) {
-                const cplx dn(omega(k), -eta);
-                double* r = &out[(size_t)k * ncols];
-                r[0] = omega(k);
-                for (int q = 0; q < 6; q++) {
-                    const int a = ord[q][0], b = ord[q][1];
-                    const cplx v = Sab[a][b][k] - std::conj(el[a]) * el[b] / dn;
-                    r[1 + 2 * q] = v.real(); r[2 + 2 * q] = v.imag();
-                }
-                const cplx tt = Sab[t][t][k] - std::conj(el[t]) * el[t] / dn;
-                r[13] = tt.real(); r[14] = tt.imag();
-            }
-        }
-        return;
-    }
-    if (cfg.kind != ESC_DYN_LOCALSZSZ) throw std::invalid_argument("Unknown dynstr parameter");
-    // LocalDynSzSz (dynamics.h:64-217): per site Sx, Sy, Sz, Sx+Sy+Sz, Spe3, Sme3
-    ncols = 9;
-    std::vector<cplx> acc((size_t)nw * 8, cplx(0, 0));
-    const int ops[6] = {ESC_OP_SX, ESC_OP_SY, ESC_OP_SZ, ESC_OP_SXSYSZ, ESC_OP_SPE3, ESC_OP_SME3};
-    for (int si = 0; si < N; si++) {
-        std::vector<std::vector<esc::OpTerm>> ch(6);
-        for (int c = 0; c < 6; c++) ch[c] = T(ops[c], si);
-        std::vector<cplx> el(6);
-        // Sab for (xx, yy, zz, xy, xz, yz, tt, pp, mm)
-        std::vector<std::vector<cplx>> R9(9, std::vector<cplx>(nw));
-        const int pa[9] = {0, 1, 2, 0, 0, 1, 3, 4, 5}, pb[9] = {0, 1, 2, 1, 2, 2, 3, 4, 5};
-        if (ritz) {
-            std::vector<std::vector<cplx>> O(6);
-            for (int c = 0; c < 6; c++) O[c] = S.ritz_overlaps(ch[c], 0, d_r, d_tmp, &el[c]);
-            for (int k = 0; k < nw; k++)
-                for (int q = 0; q < 9; q++) {
-                    cplx s(0, 0);
-                    for (int n = 0; n < M; n++) s = s + lehmann_term(O[pa[q]][n], O[pb[q]][n], omega(k), h->ritz[n] - Eg, eta);
-                    R9[q][k] = s;
-                }
-        } else {
-            std::vector<std::vector<esc::OpTerm>> runs;
-            for (int c = 0; c < 6; c++) {
-                el[c] = S.expect(ch[c], 0, d_tmp);
-                runs.push_back(ch[c]);
-            }
-            const int pp[3][3] = {{0, 1, 3}, {0, 2, 4}, {1, 2, 5}};
-            for (auto& q : pp) {
-                runs.push_back(combine(ch[q[0]], ch[q[1]], 1.0));
-                runs.push_back(combine(ch[q[0]], ch[q[1]], cplx(0, 1)));
-            }
-            auto G = cf_runs(runs);   // 12 columns per site
-            R9[0] = G[0]; R9[1] = G[1]; R9[2] = G[2]; R9[6] = G[3]; R9[7] = G[4]; R9[8] = G[5];
-            for (int qi = 0; qi < 3; qi++) {
-                const auto& q = pp[qi];
-                const auto& Sp = G[6 + 2 * qi];
-                const auto& Sq = G[7 + 2 * qi];
-                for (int k = 0; k < nw; k++) {
-                    const cplx X = Sp[k] - G[q[0]][k] - G[q[1]][k];
-                    const cplx Y = Sq[k] - G[q[0]][k] - G[q[1]][k];
-                    R9[q[2]][k] = 0.5 * (X - cplx(0, 1) * Y);
-                }
-            }
-        }
-        for (int k = 0; k < nw; k++) {
-            const cplx dn(omega(k), -eta);
-            cplx* A = &acc[(size_t)k * 8];
-            for (int q = 0; q < 6; q++) A[q] += R9[q][k];
-            A[6] += R9[7][k];
-            A[7] += R9[8][k];
-            A[0] -= std::conj(el[0]) * el[0] / dn; A[3] -= std::conj(el[0]) * el[1] / dn; A[4] -= std::conj(el[0]) * el[2] / dn;
-            A[1] -= std::conj(el[1]) * el[1] / dn; A[5] -= std::conj(el[1]) * el[2] / dn; A[2] -= std::conj(el[2]) * el[2] / dn;
-            A[6] -= el[5] * el[4] / dn;   // Sm*Sp without conjugate, as written (dynamics.h:185-186)
-            A[7] -= el[4] * el[5] / dn;
-        }
-    }
-    out.assign((size_t)nw * ncols, 0.0);
-    for (int k = 0; k < nw; k++) {
-        double* r = &out[(size_t)k * ncols];
-        r[0] = omega(k);
-        // data order: xx, yy, zz, xy, xz, yz, SmSp, SpSm (dynamics.h:189-196)
-        for (int q = 0; q < 8; q++) r[1 + q] = acc[(size_t)k * 8 + q].imag();
-    }
-}
-
-}  // namespace
-
-namespace {
-
-// Parameter-derivative operators dH/dK, dH/dJ, dH/dh (K the common Kitaev coupling, J the
-// Heisenberg coupling, h the [111] field with Bxx=Byy=Bzz=-h/sqrt3), on relabelled sites.
-void derivative_models(const esc_handle* h, esc::DevModel ms[3]) {
-    esc_params pk = h->p, pj = h->p, ph = h->p;
-    pk.Kxx = pk.Kyy = pk.Kzz = 1.0; pk.jheis = 0.0;
-    pj.Kxx = pj.Kyy = pj.Kzz = 0.0; pj.jheis = 1.0;
-    ph.Kxx = ph.Kyy = ph.Kzz = 0.0; ph.jheis = 0.0;
-    const double s3 = -1.0 / std::sqrt(3.0);
-    const esc_params* ps[3] = {&pk, &pj, &ph};
-    for (int q = 0; q < 3; q++) {
-        std::vector<esc::Bond> b;
-        esc::build_bonds(*ps[q], h->L, b);
-        for (auto& x : b) { x.i = h->plan.perm[x.i]; x.j = h->plan.perm[x.j]; }
-        ms[q] = esc::make_dev_model(*ps[q], h->L, b, q == 2 ? s3 : 0.0, q == 2 ? s3 : 0.0, q == 2 ? s3 : 0.0);
-    }
-}
-
-struct GradVecs {
-    esc_handle* h;
-    int64_t D;
-    std::vector<void*> v;
-    GradVecs(esc_handle* hh, int n) : h(hh), D(hh->D) {
-        v.assign(n, nullptr);
-        for (int i = 0; i < n; i++) {
-            if (cudaMalloc(&v[i], (size_t)D * 16) != cudaSuccess) {
-                (void)cudaGetLastError();
-                for (int j = 0; j < i; j++) cudaFree(v[j]);
-                v.clear();
-                throw Fail(ESC_ERR_MEMORY, "gradient work vectors do not fit on the device");
-            }
-        }
-    }
-    ~GradVecs() { for (void* p : v) if (p) cudaFree(p); }
-    void* operator[](int i) { return v[i]; }
-};
-
-cplx dotc(esc_handle* h, const void* a, const void* b) {
-    esc::launch_dot<double>(a, b, h->D, h->d_part, h->d_sc, h->stream);
-    double r[2];
-    ESC_CUDA(cudaMemcpyAsync(r, h->d_sc, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    sync(h);
-    return cplx(r[0], r[1]);
-}
-void axpby(esc_handle* h, const void* x, const void* y, void* out, cplx a, cplx b) {
-    esc::launch_axpby<double>(x, y, out, a, b, h->D, h->stream);
-}
-void copyv(esc_handle* h, const void* x, void* y) {
-    ESC_CUDA(cudaMemcpyAsync(y, x, (size_t)h->D * 16, cudaMemcpyDeviceToDevice, h->stream));
-}
-
-// Reverse sweep of G = b0^2/(z - a0 - b1^2/(z - a1 - ...)): dG/da_k, dG/db_k (k >= 0), dG/dz.
-void cf_adjoint(const std::vector<double>& a, const std::vector<double>& b, cplx z, cplx& G, std::vector<cplx>& ga,
-                std::vector<cplx>& gb, cplx& gz) {
-    const int n = (int)a.size();
-    std::vector<cplx> Dk(n);
-    cplx t(0, 0);
-    for (int k = n - 1; k >= 0; k--) {
-        Dk[k] = z - a[k] - t;
-        t = (k >= 1) ? (b[k] * b[k]) / Dk[k] : cplx(0, 0);
-    }
-    G = b[0] * b[0] / Dk[0];
-    ga.assign(n, 0.0); gb.assign(n + 1, 0.0);
-    gb[0] = 2.0 * b[0] / Dk[0];
-    cplx g = -G / Dk[0];          // dG/dD_0
-    gz = 0.0;
-    for (int k = 0; k < n; k++) {
-        ga[k] = -g;
-        gz += g;
-        if (k + 1 < n) {
-            // D_k = z - a_k - b_{k+1}^2 / D_{k+1}
-            gb[k + 1] = g * (-2.0 * b[k + 1] / Dk[k + 1]);
-            g = g * (b[k + 1] * b[k + 1]) / (Dk[k + 1] * Dk[k + 1]);
-        }
-    }
-}
-
-void grad_impl(esc_handle* h, const esc_dyn_cfg* cfg, double* dE0, double* dS) {
-    const int64_t D = h->D;
-    ensure_t(h->d_sc, h->sc_bytes, std::max(h->sc_bytes, (size_t)64 * sizeof(double)));
-    ensure_partials(h, 4);
-    esc::DevModel dm[3];
-    derivative_models(h, dm);
-    if (!dS) {
-        // Hellmann-Feynman only (either precision)
-        auto run = [&](auto tag) {
-            typedef decltype(tag) R;
-            ensure(h->d_work, h->work_bytes, std::max(h->work_bytes, (size_t)D * Pipe<R>::ES));
-            esc::launch_dot<R>(h->d_gs, h->d_gs, D, h->d_part, h->d_sc + 8, h->stream);
-            for (int q = 0; q < 3; q++) {
-                esc::launch_hv<R>(dm[q], h->d_gs, h->d_work, D, h->stream);
-                esc::launch_dot<R>(h->d_gs, h->d_work, D, h->d_part, h->d_sc + 2 * q, h->stream);
-            }
-            double r[10];
-            ESC_CUDA(cudaMemcpyAsync(r, h->d_sc, 10 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-            sync(h);
-            for (int q = 0; q < 3; q++) dE0[q] = r[2 * q] / r[8];
-        };
-        if (h->basis_dt == ESC_C64) run(float()); else run(double());
-        return;
-    }
-    // ---- FP64 gradient of Im S_tt(omega) --------------------------------------------------------
-    const bool je = cfg->kind == ESC_DYN_JEJE;
-    if (!je && cfg->kind != ESC_DYN_JSJS) throw Fail(ESC_ERR_PARAM, "dS(omega) is provided for the JeJe and JsJs tt channels");
-    const double K = h->p.Kxx;
-    if (!(h->p.Kxx == h->p.Kyy && h->p.Kyy == h->p.Kzz) || K == 0.0)
-        throw Fail(ESC_ERR_PARAM, "gradients are with respect to a common nonzero Kitaev coupling Kxx=Kyy=Kzz");
-    const int steps = cfg->cf_steps > 0 ? cfg->cf_steps : h->nsteps;
-    const int nw = cfg->omega_steps + 1;
-    // vectors: 0 gs(normalised) 1 tmp 2..4 dH_q gs -> later dgs_q, 5..7 dphi_q, CG (8..11), Lanczos
-    // q_prev 12, q 13, w 14, tangents dq_prev 15..17, dq 18..20, dw 21..23
-    GradVecs V(h, 24);
-    void* gs = V[0];
-    copyv(h, h->d_gs, gs);
-    const double ngs = std::sqrt(dotc(h, gs, gs).real());
-    axpby(h, gs, gs, gs, cplx(1.0 / ngs, 0), cplx(0, 0));
-    const double E0 = h->ritz[0];
-    double dE[3];
-    for (int q = 0; q < 3; q++) {
-        esc::launch_hv<double>(dm[q], gs, V[2 + q], D, h->stream);
-        dE[q] = dotc(h, gs, V[2 + q]).real();
-        dE0[q] = dE[q];
-    }
-    auto Hv = [&](const void* in, void* out) {
-        esc::launch_hv_tiled<double>(h->dm, h->passes, in, out, D, diag_for(h, ESC_C128), h->stream);
-    };
-    auto project = [&](void* x) {   // x -= <gs|x> gs
-        const cplx c = dotc(h, gs, x);
-        axpby(h, x, gs, x, cplx(1, 0), -c);
-    };
-    // Sternheimer: (H - E0) dgs = -(dH - dE) gs, dgs orthogonal to gs  (projected conjugate gradients)
-    for (int q = 0; q < 3; q++) {
-        void *x = V[8], *r = V[9], *p = V[10], *Ap = V[11];
-        axpby(h, V[2 + q], gs, r, cplx(-1, 0), cplx(dE[q], 0));
-        project(r);
-        ESC_CUDA(cudaMemsetAsync(x, 0, (size_t)D * 16, h->stream));
-        copyv(h, r, p);
-        double rr = dotc(h, r, r).real();
-        const double rr0 = rr;
-        for (int it = 0; it < 3000 && rr > 1e-26 * rr0; it++) {
-            Hv(p, Ap);
-            axpby(h, Ap, p, Ap, cplx(1, 0), cplx(-E0, 0));
-            project(Ap);
-            const double pAp = dotc(h, p, Ap).real();
-            if (!(pAp > 0)) break;
-            const double al = rr / pAp;
-            axpby(h, x, p, x, cplx(1, 0), cplx(al, 0));
-            axpby(h, r, Ap, r, cplx(1, 0), cplx(-al, 0));
-            const double rn = dotc(h, r, r).real();
-            axpby(h, r, p, p, cplx(1, 0), cplx(rn / rr, 0));
-            rr = rn;
-        }
-        project(x);
-        copyv(h, x, V[2 + q]);   // dgs_q
-    }
-    // phi = A gs, dphi_q = (dA/dq) gs + A dgs_q; A homogeneous of degree 2 (Je) or 1 (Js) in K
-    const esc::DevOp A = esc::make_dev_op(esc::operator_terms(je ? ESC_OP_JE_TOTAL : ESC_OP_JS_TOTAL, 0, h->p, h->L),
-                                          &h->plan.perm);
-    const double deg = je ? 2.0 : 1.0;
-    void* phi = V[1];
-    esc::launch_apply<double>(A, gs, phi, D, h->stream);
-    for (int q = 0; q < 3; q++) esc::launch_apply<double>(A, V[2 + q], V[5 + q], D, h->stream);
-    axpby(h, V[5], phi, V[5], cplx(1, 0), cplx(deg / K, 0));
-    // elastic term m = <gs|A|gs> (real), dm_q = 2 Re <phi|dgs_q> + <gs|dA|gs>
-    const double m = dotc(h, gs, phi).real();
-    double dmel[3];
-    for (int q = 0; q < 3; q++) dmel[q] = 2.0 * dotc(h, phi, V[2 + q]).real() + (q == 0 ? deg / K * m : 0.0);
-    // tangent Lanczos on phi
-    const double b0 = std::sqrt(dotc(h, phi, phi).real());
-    double db0[3];
-    for (int q = 0; q < 3; q++) db0[q] = dotc(h, phi, V[5 + q]).real() / b0;
-    void *qp = V[12], *qc = V[13], *w = V[14];
-    void* dqp[3] = {V[15], V[16], V[17]};
-    void* dqc[3] = {V[18], V[19], V[20]};
-    void* dw[3] = {V[21], V[22], V[23]};
-    axpby(h, phi, phi, qc, cplx(1.0 / b0, 0), cplx(0, 0));
-    for (int q = 0; q < 3; q++) {
-        // dq0 = (dphi - db0 q0) / b0
-        axpby(h, V[5 + q], qc, dqc[q], cplx(1.0 / b0, 0), cplx(-db0[q] / b0, 0));
-        ESC_CUDA(cudaMemsetAsync(dqp[q], 0, (size_t)D * 16, h->stream));
-    }
-    ESC_CUDA(cudaMemsetAsync(qp, 0, (size_t)D * 16, h->stream));
-    std::vector<double> a, b{b0}, da[3], db[3];
-    for (int q = 0; q < 3; q++) db[q].push_back(db0[q]);
-    void* tmp = V[8];
-    for (int k = 0; k < steps; k++) {
-        Hv(qc, w);                                   // w = H q
-        const double ak = dotc(h, qc, w).real();
-        double dak[3];
-        for (int q = 0; q < 3; q++) {
-            Hv(dqc[q], dw[q]);                       // dw = H dq + dH q
-            esc::launch_hv<double>(dm[q], qc, tmp, D, h->stream);
-            axpby(h, dw[q], tmp, dw[q], cplx(1, 0), cplx(1, 0));
-            dak[q] = (dotc(h, dqc[q], w) + dotc(h, qc, dw[q])).real();
-        }
-        const double bk = b.back();
-        // w = Hq - a q - b q_prev ; dw -= da q + a dq + db q_prev + b dq_prev
-        axpby(h, w, qc, w, cplx(1, 0), cplx(-ak, 0));
-        if (k > 0) axpby(h, w, qp, w, cplx(1, 0), cplx(-bk, 0));
-        for (int q = 0; q < 3; q++) {
-            axpby(h, dw[q], qc, dw[q], cplx(1, 0), cplx(-dak[q], 0));
-            axpby(h, dw[q], dqc[q], dw[q], cplx(1, 0), cplx(-ak, 0));
-            if (k > 0) {
-                axpby(h, dw[q], qp, dw[q], cplx(1, 0), cplx(-db[q].back(), 0));
-                axpby(h, dw[q], dqp[q], dw[q], cplx(1, 0), cplx(-bk, 0));
-            }
-        }
-        a.push_back(ak);
-        for (int q = 0; q < 3; q++) da[q].push_back(dak[q]);
-        const double bn = std::sqrt(dotc(h, w, w).real());
-        if (k + 1 == steps || !(bn > 1e-10 * b0)) break;
-        double dbn[3];
-        for (int q = 0; q < 3; q++) dbn[q] = dotc(h, w, dw[q]).real() / bn;
-        b.push_back(bn);
-        for (int q = 0; q < 3; q++) db[q].push_back(dbn[q]);
-        // rotate: q_prev <- q, q <- w / bn ; dq_prev <- dq, dq <- (dw - dbn q_new) / bn
-        std::swap(qp, qc);                            // qp = old q
-        axpby(h, w, w, qc, cplx(1.0 / bn, 0), cplx(0, 0));
-        for (int q = 0; q < 3; q++) {
-            std::swap(dqp[q], dqc[q]);
-            axpby(h, dw[q], qc, dqc[q], cplx(1.0 / bn, 0), cplx(-dbn[q] / bn, 0));
-        }
-    }
-    // assemble d Im S_tt(omega) per parameter
-    const double eta = cfg->eta;
-    std::vector<cplx> ga, gb;
-    for (int kw = 0; kw < nw; kw++) {
-        const double om = cfg->domega * kw;
-        const cplx z(om + E0, -eta);
-        cplx G, gz;
-        cf_adjoint(a, b, z, G, ga, gb, gz);
-        const cplx dn(om, -eta);
-        for (int q = 0; q < 3; q++) {
-            cplx dG = gz * dE[q];
-            for (size_t k = 0; k < a.size(); k++) dG += ga[k] * da[q][k];
-            for (size_t k = 0; k < b.size() && k < gb.size(); k++) dG += gb[k] * db[q][k];
-            const cplx del = 2.0 * m * dmel[q] / dn;
-            dS[(size_t)kw * 3 + q] = (dG - del).imag();
-        }
-    }
-    sync(h);
-}
-
-}  // namespace
-
-namespace {
-
-// Observables::TwoPointCorr (src/Observables.h:131-158): C(si, sj) = <gs| A_si B_sj |gs> for
-// si >= sj, and C(sj, si) = the same value (the reference mirrors it without conjugation).
-// GPU form: U_j = B_sj |gs> for all j; for a Hermitian A, Phi_i = A_si |gs> and one GEMV per
-// column gives <Phi_i|U_j> for all i (2N operator applications instead of N(N+1)/2); otherwise
-// A_si U_j is applied per pair and dotted with |gs>.  Falls back to the pairwise form when the
-// 2N vectors do not fit in device memory.
-bool hermitian_op(int op) {
-    switch (op) {
-        case ESC_OP_SP: case ESC_OP_SM: case ESC_OP_SPE3: case ESC_OP_SME3: return false;
-        default: return true;
-    }
-}
-
-template <typename R>
-void two_point_impl(esc_handle* h, int opA, int opB, std::vector<cplx>& C) {
-    Pipe<R> P(h);
-    const int N = h->N;
-    const int64_t D = h->D;
-    const size_t ES = Pipe<R>::ES;
-    auto T = [&](int op, int site) { return esc::make_dev_op(esc::operator_terms(op, site, h->p, h->L), &h->plan.perm); };
-    C.assign((size_t)N * N, cplx(0, 0));
-    ensure_t(h->d_sc, h->sc_bytes, std::max(h->sc_bytes, (size_t)(2 * N + 8) * sizeof(double)));
-    ensure_partials(h, N + 2);
-    double* d_r = h->d_sc;
-    std::vector<double> r(2 * (size_t)N);
-    void* U = nullptr;
-    void* Phi = nullptr;
-    const bool herm = hermitian_op(opA);
-    if (cudaMalloc(&U, (size_t)N * D * ES) != cudaSuccess || (herm && cudaMalloc(&Phi, (size_t)N * D * ES) != cudaSuccess)) {
-        (void)cudaGetLastError();
-        if (U) cudaFree(U);
-        U = Phi = nullptr;
-    }
-    try {
-        if (U && herm) {
-            for (int j = 0; j < N; j++) P.apply(T(opB, j), h->d_gs, (char*)U + (size_t)j * D * ES);
-            for (int i = 0; i < N; i++) P.apply(T(opA, i), h->d_gs, (char*)Phi + (size_t)i * D * ES);
-            for (int j = 0; j < N; j++) {
-                esc::launch_gemv_h<R>(Phi, D, N, (char*)U + (size_t)j * D * ES, D, h->d_part, part_cap_doubles(h), d_r,
-                                      h->stream);
-                ESC_CUDA(cudaMemcpyAsync(r.data(), d_r, r.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-                sync(h);
-                for (int i = j; i < N; i++) C[(size_t)i * N + j] = C[(size_t)j * N + i] = cplx(r[2 * i], r[2 * i + 1]);
-            }
-        } else {
-            ensure(h->d_work, h->work_bytes, std::max(h->work_bytes, 2 * (size_t)D * ES));
-            char* u = (char*)h->d_work;
-            char* w = u + (size_t)D * ES;
-            for (int j = 0; j < N; j++) {
-                P.apply(T(opB, j), h->d_gs, u);
-                for (int i = j; i < N; i++) {
-                    P.apply(T(opA, i), u, w);
-                    P.dot(h->d_gs, w, d_r);
-                    double c[2];
-                    ESC_CUDA(cudaMemcpyAsync(c, d_r, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-                    sync(h);
-                    C[(size_t)i * N + j] = C[(size_t)j * N + i] = cplx(c[0], c[1]);
-                }
-            }
-        }
-    } catch (...) {
-        (void)cudaStreamSynchronize(h->stream);
-        if (U) cudaFree(U);
-        if (Phi) cudaFree(Phi);
-        throw;
-    }
-    sync(h);
-    if (U) cudaFree(U);
-    if (Phi) cudaFree(Phi);
-}
-
-}  // namespace
 
 extern "C" {
 

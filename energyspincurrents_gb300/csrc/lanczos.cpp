@@ -1,0 +1,259 @@
+// lanczos.cpp -- the ground-state Lanczos (DynLanczosSolver::Lanczos_Nirav) and the batched
+// continued-fraction recurrences on the device; the host keeps only scalars and the tridiagonal.
+#include <type_traits>
+
+#include "abi_common.h"
+
+namespace escabi {
+
+// Ground-state Lanczos, DynLanczosSolver::Lanczos_Nirav (src/DynLanczosSolver.h:38-239).
+template <typename R>
+void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) {
+    Pipe<R> P(h);
+    const int64_t D = h->D;
+    const size_t ES = Pipe<R>::ES;
+    const int M = cfg.steps;
+    // GS without reorthogonalisation keeps three vectors and rebuilds |gs> in a second pass
+    // (the Lanczos vectors are recomputed from the recorded alpha/beta, not stored): the mode for
+    // bases too large to hold M+1 vectors (N = 28..32).
+    const bool recompute = cfg.lanctype == 1 && !cfg.reortho;
+    const bool store = cfg.lanctype != 0 && !recompute;  // OnlyEgs keeps no basis (returns a zero vector)
+    const bool reo = store && cfg.reortho;
+    const int nvec = store ? M + 1 : 3;
+    h->have_gs = h->have_basis = false;
+    ensure(h->d_L, h->L_bytes, (size_t)nvec * D * ES);
+    ensure(h->d_work, h->work_bytes, (size_t)D * ES);
+    // scalars: alpha[2M] | b2[M+2] | tmp[8] | r[2(M+2)] | z[M+2]
+    const size_t n_sc = 2 * (size_t)M + (M + 2) + 8 + 2 * (size_t)(M + 2) + (M + 2);
+    ensure_t(h->d_sc, h->sc_bytes, n_sc * sizeof(double));
+    double* d_alpha = h->d_sc;
+    double* d_b2 = d_alpha + 2 * M;
+    double* d_tmp = d_b2 + (M + 2);
+    double* d_r = d_tmp + 8;
+    double* d_z = d_r + 2 * (M + 2);
+    ensure_partials(h, reo ? M + 2 : 4);
+    ESC_CUDA(cudaMemsetAsync(h->d_sc, 0, n_sc * sizeof(double), h->stream));
+    auto Lv = [&](int i) -> char* { return (char*)h->d_L + (size_t)(store ? i : i % 3) * D * ES; };
+    void* w = h->d_work;
+
+    // Vorig.normalize(); V0 = Vorig (:58-66)
+    P.nrm2(d_start, d_tmp);
+    P.scale(d_start, Lv(0), d_tmp);
+    // iteration 0 (:75-83): V1 = H V0; alpha0 = <V0|V1>; V1 -= alpha0 V0; beta1 = |V1|; normalise
+    P.hv(Lv(0), w);
+    P.dot(Lv(0), w, d_alpha);
+    esc::launch_lanczos_update<R>(w, Lv(0), nullptr, d_alpha, nullptr, D, h->d_part, d_b2 + 1, h->stream);
+    P.scale(w, Lv(1), d_b2 + 1);
+    int exit_iter = M - 1;
+    double E0 = 1.0;
+    for (int iter = 1; iter <= M - 1; iter++) {             // :91-163
+        P.hv(Lv(iter), w);
+        P.dot(Lv(iter), w, d_alpha + 2 * iter);
+        esc::launch_lanczos_update<R>(w, Lv(iter), Lv(iter - 1), d_alpha + 2 * iter, d_b2 + iter, D, h->d_part,
+                                      d_b2 + iter + 1, h->stream);
+        P.scale(w, Lv(iter + 1), d_b2 + iter + 1);
+        if (reo) {
+            // Full reorthogonalisation against L_0..L_iter (:105-119).  The reference does one
+            // modified Gram-Schmidt sweep; here two classical sweeps (CGS2) as two GEMV pairs,
+            // which orthogonalise to the same working precision.
+            for (int pass = 0; pass < 2; pass++) {
+                esc::launch_gemv_h<R>(h->d_L, D, iter + 1, Lv(iter + 1), D, h->d_part, part_cap_doubles(h), d_r,
+                                      h->stream);
+                esc::launch_gemv_sub<R>(h->d_L, D, iter + 1, d_r, Lv(iter + 1), D, h->stream);
+            }
+            P.nrm2(Lv(iter + 1), d_tmp + 1);
+            P.scale(Lv(iter + 1), Lv(iter + 1), d_tmp + 1);
+        }
+        if (cfg.eps > 0.0) {                                 // :125-151 (convergence test)
+            std::vector<double> a(2 * (iter + 1)), b2(iter + 2);
+            ESC_CUDA(cudaMemcpyAsync(a.data(), d_alpha, a.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            ESC_CUDA(cudaMemcpyAsync(b2.data(), d_b2, b2.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            sync(h);
+            std::vector<double> d(iter + 1), e(iter + 1, 0.0);
+            for (int i = 0; i <= iter; i++) d[i] = a[2 * i];
+            for (int i = 0; i < iter; i++) e[i] = std::sqrt(b2[i + 1]);
+            if (!esc::tridiag_eig(iter + 1, d, e, nullptr)) throw Fail(ESC_ERR_NUMERIC, "diag: tridiagonal eigensolver failed");
+            const double diff = std::fabs(E0 - d[0]);
+            E0 = d[0];
+            if (diff < cfg.eps) { exit_iter = iter; break; }
+        }
+    }
+    const int n = exit_iter + 1;                             // EXITiter (:164)
+    std::vector<double> a(2 * (size_t)M), b2(M + 2);
+    ESC_CUDA(cudaMemcpyAsync(a.data(), d_alpha, a.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    ESC_CUDA(cudaMemcpyAsync(b2.data(), d_b2, b2.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    sync(h);
+    h->alpha.assign(n, 0.0);
+    h->beta.assign(n + 1, 0.0);
+    for (int i = 0; i < n; i++) h->alpha[i] = a[2 * i];
+    for (int i = 1; i <= n; i++) h->beta[i] = std::sqrt(b2[i]);
+    for (int i = 0; i < n; i++)
+        if (!std::isfinite(h->alpha[i]) || !std::isfinite(h->beta[i + 1]))
+            throw Fail(ESC_ERR_NUMERIC, "NaN/Inf in Lanczos coefficients at step " + std::to_string(i));
+    for (int i = 1; i < n; i++)
+        if (h->beta[i] == 0.0)
+            throw Fail(ESC_ERR_NUMERIC, "Lanczos breakdown: beta=0 at step " + std::to_string(i) +
+                                            " (Krylov space exhausted; use fewer LanczosSteps)");
+    std::vector<double> d(h->alpha), e(n, 0.0);
+    for (int i = 0; i < n - 1; i++) e[i] = h->beta[i + 1];
+    h->Z.clear();
+    if (!esc::tridiag_eig(n, d, e, (store || recompute) ? &h->Z : nullptr)) throw Fail(ESC_ERR_NUMERIC, "diag: tridiagonal eigensolver failed");
+    h->ritz = d;
+    h->nsteps = n;
+    ensure(h->d_gs, h->gs_bytes, (size_t)D * ES);
+    if (recompute) {
+        // second pass: identical kernels on identical inputs regenerate L_0..L_{n-1} bit for bit
+        ESC_CUDA(cudaMemcpyAsync(d_z, h->Z.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        ESC_CUDA(cudaMemsetAsync(h->d_gs, 0, (size_t)D * ES, h->stream));
+        P.nrm2(d_start, d_tmp);
+        P.scale(d_start, Lv(0), d_tmp);
+        esc::launch_axpy_dev<R>(Lv(0), h->d_gs, d_z, D, h->stream);
+        for (int it = 0; it + 1 < n; it++) {
+            P.hv(Lv(it), w);
+            esc::launch_lanczos_update<R>(w, Lv(it), it ? Lv(it - 1) : nullptr, d_alpha + 2 * it, it ? d_b2 + it : nullptr,
+                                          D, h->d_part, d_tmp + 2, h->stream);
+            P.scale(w, Lv(it + 1), d_b2 + it + 1);
+            esc::launch_axpy_dev<R>(Lv(it + 1), h->d_gs, d_z + it + 1, D, h->stream);
+        }
+    } else if (store) {
+        // PsiAll[0] = sum_m L_m Z(m,0) (:208-234), without forming the other Ritz vectors
+        ESC_CUDA(cudaMemcpyAsync(d_z, h->Z.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        esc::launch_lincomb<R>(h->d_L, D, n, d_z, h->d_gs, D, h->stream);
+        h->have_basis = cfg.lanctype == 2;
+    } else {
+        ESC_CUDA(cudaMemsetAsync(h->d_gs, 0, (size_t)D * ES, h->stream));   // OnlyEgs returns zeros (:178-180)
+    }
+    if ((recompute || store) && !reo) {
+        // Without reorthogonalisation the Lanczos vectors lose orthogonality once the ground state
+        // has converged, and sum_m Z(m,0) L_m is then not a unit vector: normalise it.  (With full
+        // reorthogonalisation, the reference's mode, the sum is kept exactly as the reference forms it.)
+        P.nrm2(h->d_gs, d_tmp + 3);
+        P.scale(h->d_gs, h->d_gs, d_tmp + 3);
+    }
+    if (!store && h->d_L) {   // the three recurrence vectors are not needed any more: free them for the dynamics
+        cudaFree(h->d_L);
+        h->d_L = nullptr;
+        h->L_bytes = 0;
+    }
+    h->basis_dt = sizeof(R) == 8 ? ESC_C128 : ESC_C64;
+    h->L_ld = D;
+    h->have_gs = true;
+    sync(h);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Batched continued-fraction Lanczos (batched.cu)
+// ---------------------------------------------------------------------------------------------
+int cf_batch_width(esc_handle* h, size_t es, int want) {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { (void)cudaGetLastError(); fr = 0; }
+    const size_t per = 3 * (size_t)h->D * es;
+    const size_t have = fr + h->cfb_bytes;
+    int w = (int)std::min<size_t>((size_t)want, have > (size_t)1 << 30 ? (have - ((size_t)1 << 30)) / per : 0);
+    return std::max(1, std::min(w, esc::MAX_COLS));
+}
+
+// Start vectors must already be in column slots of set 1 of d_cfb.  Returns a (Re alpha),
+// b (b[0] = |phi|) and the number of steps per column.
+//
+// head > 0 (complex64 columns only): the first `head` iterations run on complex128 copies of the
+// columns; the last two vectors are then rounded to complex64 and the recurrence continues in
+// complex64 from iteration `head`.  The leading iterations fix the converged, low-lying poles of
+// the continued fraction, so their rounding in FP32 is what costs accuracy; the tail only adds
+// resolution.  The head needs 3 x ncols complex128 vectors for its duration; without that much
+// free device memory the run is all complex64.
+template <typename R>
+void cf_batch_run(esc_handle* h, int ncols, int kmax, const std::vector<int>& steps, const std::vector<esc::DevModel>& ms,
+                  double tol, bool graph, std::vector<std::vector<double>>& A, std::vector<std::vector<double>>& B,
+                  int head) {
+    const size_t nd = (size_t)ncols * esc::CFB_GRID * 2 + (size_t)ncols * kmax * 2 + (size_t)ncols * (kmax + 1);
+    ensure_t(h->d_cfs, h->cfs_bytes, nd * sizeof(double));
+    ensure_t(h->d_cfi, h->cfi_bytes, (2 * (size_t)ncols + 2) * sizeof(int));
+    auto setup = [&](auto& cb, void* bufs, const void* dg) {
+        typedef typename std::remove_reference<decltype(cb)>::type CB;
+        cb.ncols = ncols; cb.kmax = kmax; cb.D = h->D; cb.tol = tol; cb.use_graph = graph;
+        cb.bufs = bufs;
+        cb.d_part = h->d_cfs;
+        cb.d_alpha = cb.d_part + (size_t)ncols * esc::CFB_GRID * 2;
+        cb.d_b2 = cb.d_alpha + (size_t)ncols * kmax * 2;
+        cb.d_active = h->d_cfi;
+        cb.d_steps = h->d_cfi + ncols;
+        cb.d_it = h->d_cfi + 2 * ncols;
+        typedef typename std::conditional<std::is_same<CB, esc::CFBatch<float>>::value, float, double>::type RR;
+        cb.hv_column = [h, &ms, dg](int c, const void* in, void* out, const int* active, cudaStream_t s) {
+            esc::launch_hv_tiled<RR>(ms[c], h->passes, in, out, h->D, dg, s, active);
+        };
+    };
+    ESC_CUDA(cudaMemsetAsync(h->d_cfs, 0, nd * sizeof(double), h->stream));
+    esc::CFBatch<R> cb;
+    setup(cb, h->d_cfb, diag_for(h, sizeof(R) == 4 ? ESC_C64 : ESC_C128));
+    head = std::min(head, kmax);
+    void* dd = nullptr;
+    if (sizeof(R) == 4 && head > 0) {
+        const size_t vs = (size_t)ncols * h->D;   // states per set
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { (void)cudaGetLastError(); fr = 0; }
+        const size_t need = 3 * vs * 16 + (h->d_diag[0] ? 0 : (size_t)h->D * 8);
+        if (fr > need + ((size_t)1 << 30) && cudaMalloc(&dd, 3 * vs * 16) == cudaSuccess) {
+            char* d1 = (char*)dd + vs * 16;
+            esc::launch_convert_c64_to_c128((char*)h->d_cfb + vs * 8, d1, (int64_t)vs, h->stream);
+            std::vector<int> hs(ncols);
+            for (int c = 0; c < ncols; c++) hs[c] = std::min(steps[c], head);
+            ESC_CUDA(cudaMemcpyAsync(cb.d_steps, hs.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+            esc::CFBatch<double> c64;
+            setup(c64, dd, diag_for(h, ESC_C128));
+            c64.run(h->stream);   // synchronises
+            // columns that ran the whole head without stopping continue in complex64
+            std::vector<double> b2((size_t)ncols * (kmax + 1));
+            ESC_CUDA(cudaMemcpy(b2.data(), cb.d_b2, b2.size() * sizeof(double), cudaMemcpyDeviceToHost));
+            std::vector<int> act(ncols, 0);
+            for (int c = 0; c < ncols; c++) {
+                const double b0 = std::sqrt(b2[(size_t)c * (kmax + 1)]);
+                bool live = b0 > 0.0 && steps[c] > head;
+                for (int k = 1; live && k <= head; k++)
+                    if (!(std::sqrt(b2[(size_t)c * (kmax + 1) + k]) > tol * b0)) live = false;
+                act[c] = live ? 1 : 0;
+            }
+            for (int j = 0; j < 2; j++) {
+                const int set = (head + j) % 3;
+                esc::launch_convert_c128_to_c64((char*)dd + set * vs * 16, (char*)h->d_cfb + set * vs * 8, (int64_t)vs,
+                                                h->stream);
+            }
+            ESC_CUDA(cudaMemcpyAsync(cb.d_active, act.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+            sync(h);
+            cudaFree(dd);
+            cb.start_it = head;
+        } else {
+            (void)cudaGetLastError();
+            dd = nullptr;
+        }
+    }
+    ESC_CUDA(cudaMemcpyAsync(cb.d_steps, steps.data(), ncols * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    cb.run(h->stream);
+    std::vector<double> al((size_t)ncols * kmax * 2), b2((size_t)ncols * (kmax + 1));
+    ESC_CUDA(cudaMemcpyAsync(al.data(), cb.d_alpha, al.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    ESC_CUDA(cudaMemcpyAsync(b2.data(), cb.d_b2, b2.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    sync(h);
+    A.assign(ncols, {});
+    B.assign(ncols, {});
+    for (int c = 0; c < ncols; c++) {
+        const double b0 = std::sqrt(b2[(size_t)c * (kmax + 1)]);
+        B[c].push_back(b0);
+        if (b0 == 0.0) continue;
+        for (int k = 0; k < kmax; k++) {
+            A[c].push_back(al[((size_t)c * kmax + k) * 2]);
+            const double bn = std::sqrt(b2[(size_t)c * (kmax + 1) + k + 1]);
+            B[c].push_back(bn);
+            if (k + 1 >= steps[c] || !(bn > tol * b0)) break;
+        }
+    }
+}
+
+template void lanczos_gs<float>(esc_handle*, const esc_lanczos_cfg&, const void*);
+template void lanczos_gs<double>(esc_handle*, const esc_lanczos_cfg&, const void*);
+template void cf_batch_run<float>(esc_handle*, int, int, const std::vector<int>&, const std::vector<esc::DevModel>&, double,
+                                  bool, std::vector<std::vector<double>>&, std::vector<std::vector<double>>&, int);
+template void cf_batch_run<double>(esc_handle*, int, int, const std::vector<int>&, const std::vector<esc::DevModel>&, double,
+                                   bool, std::vector<std::vector<double>>&, std::vector<std::vector<double>>&, int);
+
+}  // namespace escabi

@@ -1,0 +1,190 @@
+// tune.cpp -- the self-tuner of the complex64 H.v and its tuning file.
+#include <array>
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <sstream>
+
+#include "abi_common.h"
+
+namespace escabi {
+
+// Tuning file (ESC_TUNE_FILE): one line per tuned Hamiltonian and device,
+//   <key> | T balance npasses | jit,stages,tb_bits per pass
+// written by the self-tuner and applied by esc_create, so a tuned configuration is reused without
+// timing again.  The key covers the device name and everything the plan and passes depend on.
+std::string tune_key(const esc_handle* h) {
+    cudaDeviceProp pr{};
+    if (cudaGetDeviceProperties(&pr, h->device) != cudaSuccess) (void)cudaGetLastError();
+    std::ostringstream k;
+    k.precision(17);
+    k << "dev=" << pr.name << " model=" << h->p.model << " Lx=" << h->p.Lx << " Ly=" << h->p.Ly << " pbc=" << h->p.pbcx
+      << h->p.pbcy << " K=" << h->p.Kxx << "," << h->p.Kyy << "," << h->p.Kzz << " B=" << h->p.Bxx << "," << h->p.Byy << ","
+      << h->p.Bzz << " J=" << h->p.jheis;
+    return k.str();
+}
+
+void save_tuning(const esc_handle* h, int T, int balance, const std::vector<esc::DevPass>& ps) {
+    const char* f = std::getenv("ESC_TUNE_FILE");
+    if (!f || !*f) return;
+    FILE* fp = std::fopen(f, "a");
+    if (!fp) return;
+    std::fprintf(fp, "%s | %d %d %d |", tune_key(h).c_str(), T, balance, (int)ps.size());
+    for (const auto& p : ps) std::fprintf(fp, " %d,%d,%d", p.jit >= 0 ? 1 : 0, p.stages, p.tb_bits);
+    std::fprintf(fp, "\n");
+    std::fclose(fp);
+}
+
+// Applies the last matching line of ESC_TUNE_FILE; false if there is none.
+bool load_tuning(esc_handle* h) {
+    const char* f = std::getenv("ESC_TUNE_FILE");
+    if (!f || !*f) return false;
+    FILE* fp = std::fopen(f, "r");
+    if (!fp) return false;
+    const std::string key = tune_key(h);
+    std::string found;
+    char line[4096];
+    while (std::fgets(line, sizeof line, fp)) {
+        std::string l(line);
+        if (l.compare(0, key.size(), key) == 0 && l.size() > key.size() && l[key.size()] == ' ') found = l.substr(key.size());
+    }
+    std::fclose(fp);
+    if (found.empty()) return false;
+    int T = 0, balance = 0, n = 0;
+    std::istringstream in(found);
+    char bar;
+    in >> bar >> T >> balance >> n >> bar;
+    std::vector<std::array<int, 3>> var(n);
+    for (auto& v : var) {
+        char c1, c2;
+        in >> v[0] >> c1 >> v[1] >> c2 >> v[2];
+    }
+    if (!in || T < 4) return false;
+    const esc::Plan plan = esc::make_plan(h->N, bond_pairs(h), T, 3, 200);
+    if ((int)plan.tiles.size() != n) return false;
+    install_plan(h, plan, balance, 2);
+    std::vector<esc::DevPass> comp(h->passes);
+    std::map<std::array<int, 2>, std::vector<esc::DevPass>> built;
+    for (int p = 0; p < n; p++) {
+        const std::array<int, 2> k{var[p][1], var[p][2]};
+        if (!built.count(k)) {
+            built[k] = esc::make_passes(h->plan, h->dm, balance, k[0], k[1]);
+            if (std::any_of(var.begin(), var.end(), [&](const std::array<int, 3>& x) { return x[0] && x[1] == k[0] && x[2] == k[1]; })) {
+                std::vector<esc::DevPass> sp = built[k];
+                std::string err;
+                if (esc::jit_compile(sp, err)) built[std::array<int, 2>{-k[0], k[1]}] = sp;
+            }
+        }
+        const auto it = built.find(var[p][0] ? std::array<int, 2>{-k[0], k[1]} : k);
+        comp[p] = (it != built.end() ? it->second : built[k])[p];
+    }
+    h->passes = comp;
+    return true;
+}
+
+// Self-tuning of the complex64 H.v.  Plans: tile bits T in {11, 12, 13} (above 26 sites only 12:
+// the others never win there -- one more pass, or one CTA per SM) x first-fit / group-minimising
+// term-to-pass assignment (make_passes modes 0 and 2; the balanced mode 1 never won).  Kernel variants per plan: ahead-of-time vs run-time specialised;
+// 512, 256 or 128 threads per 4096-state tile (8, 16, 32 register states each); 2 or 3 tile buffers,
+// or 2 plus staged epilogue loads.  Every variant is timed pass by pass (CUDA events on the
+// handle's stream, median of 3 after a warm-up); a plan's composite takes the fastest variant of
+// each pass (light and heavy passes prefer different variants) and is timed as a whole; the
+// fastest composite is installed.  All variants compute the same H.v up to complex64 rounding (the
+// tests hold each to the oracle).  Needs two complex64 vectors of scratch; refuses once a ground
+// state exists (a new plan relabels the internal basis).
+std::string autotune(esc_handle* h, std::vector<double>* times) {
+    if (h->have_gs) throw Fail(ESC_ERR_STATE, "autotune before the first Lanczos run (it may relabel the basis)");
+    const int64_t D = h->D;
+    void* buf = nullptr;
+    ESC_CUDA(cudaMalloc(&buf, (size_t)D * 16));
+    void* v = buf;
+    void* w = (char*)buf + (size_t)D * 8;
+    esc::launch_start_normal<float>(12345, v, D, h->stream);
+    cudaEvent_t e0, e1;
+    ESC_CUDA(cudaEventCreate(&e0));
+    ESC_CUDA(cudaEventCreate(&e1));
+    auto median_ms = [&](const std::vector<esc::DevPass>& ps) {
+        const void* dg = diag_for(h, ESC_C64);
+        esc::launch_hv_tiled<float>(h->dm, ps, v, w, D, dg, h->stream);
+        std::vector<float> ms(3);
+        for (float& x : ms) {
+            ESC_CUDA(cudaEventRecord(e0, h->stream));
+            esc::launch_hv_tiled<float>(h->dm, ps, v, w, D, dg, h->stream);
+            ESC_CUDA(cudaEventRecord(e1, h->stream));
+            ESC_CUDA(cudaEventSynchronize(e1));
+            ESC_CUDA(cudaEventElapsedTime(&x, e0, e1));
+        }
+        std::sort(ms.begin(), ms.end());
+        return (double)ms[1];
+    };
+    std::ostringstream rep;
+    const esc::Plan keep = h->plan;
+    const std::vector<esc::DevPass> keep_passes = h->passes;
+    double best = 1e300;
+    esc::Plan bplan;
+    int bbal = 0, bT = 0;
+    std::vector<esc::DevPass> bpasses;
+    try {
+        for (int T : {11, 12, 13}) {
+            if (T > h->N || (h->N > 26 && T != 12)) continue;
+            const esc::Plan plan = esc::make_plan(h->N, bond_pairs(h), T, 3, 200);
+            for (int balance : {0, 2}) {
+                std::vector<std::vector<esc::DevPass>> vars;
+                std::vector<std::vector<double>> per;
+                for (int tb : {9, 8, 7})
+                for (int stages : {2, 3, 4})
+                    for (int jit : {0, 1}) {
+                        if (T == 13 && (jit || tb != 9)) continue;   // 8192-state tiles: generic kernel only
+                        install_plan(h, plan, balance, stages, tb);
+                        if (jit) specialise(h, h->passes, 1);
+                        bool spec = false;
+                        for (const auto& ps : h->passes) spec = spec || ps.jit >= 0;
+                        if (jit && !spec) continue;
+                        std::vector<double> t;
+                        for (const auto& ps : h->passes) t.push_back(median_ms({ps}));
+                        const double tot = median_ms(h->passes);
+                        rep << "T=" << T << " passes=" << plan.tiles.size() << " balance=" << balance << " threads="
+                            << (1 << tb) << " jit=" << jit << " stages=" << stages << ": " << tot << " ms | per pass";
+                        for (double x : t) rep << " " << x;
+                        rep << "\n";
+                        if (times) times->push_back(tot);
+                        vars.push_back(h->passes);
+                        per.push_back(t);
+                    }
+                // composite: fastest variant of each pass
+                std::vector<esc::DevPass> comp = vars[0];
+                rep << "  composite T=" << T << " balance=" << balance << ": variants";
+                for (size_t p = 0; p < comp.size(); p++) {
+                    size_t bv = 0;
+                    for (size_t k = 1; k < vars.size(); k++)
+                        if (per[k][p] < per[bv][p]) bv = k;
+                    comp[p] = vars[bv][p];
+                    rep << " " << (comp[p].jit >= 0 ? "jit" : "aot") << "/" << comp[p].stages << "/" << (1 << comp[p].tb_bits);
+                }
+                install_plan(h, plan, balance, 2);   // model, permutations, diagonal of this plan
+                const double tc = median_ms(comp);
+                rep << ": " << tc << " ms\n";
+                if (tc < best) { best = tc; bplan = plan; bbal = balance; bT = T; bpasses = comp; }
+            }
+        }
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(buf);
+        install_plan(h, keep, -1, 0);
+        h->passes = keep_passes;
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    install_plan(h, bplan, bbal, 2);
+    h->passes = bpasses;
+    save_tuning(h, bT, bbal, bpasses);
+    rep << "chosen: T=" << bT << " balance=" << bbal << " passes:";
+    for (const auto& ps : bpasses) rep << " " << (ps.jit >= 0 ? "jit" : "aot") << "/" << ps.stages << "/" << (1 << ps.tb_bits);
+    rep << " (" << best << " ms)\n";
+    return rep.str();
+}
+
+}  // namespace escabi
