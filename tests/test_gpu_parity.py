@@ -499,3 +499,21 @@ def test_rayleigh_of_handle_ground_state_in_place(dt):
     e_out = h.rayleigh(r["gs"])
     assert abs(e_in - e_out) <= 1e-13 * abs(e_out)
     assert abs(e_in - r["E0"]) <= (1e-6 if dt == np.complex64 else 1e-10) * abs(e_out)
+
+
+@pytest.mark.parametrize("kind", ["Energy Current", "Spin Current", "LocalSzSz"])
+def test_cf_spectra_all_kinds_vs_exact_eigenpairs(kind):
+    """CF mode of every dynamics kind (8 sites: the Krylov spaces are exhausted, so the continued
+    fractions are exact) against the oracle's Lehmann sums over all exact eigenpairs (the
+    reference's Solver=ED path), quirks included."""
+    p = kitaev(Lx=2, Ly=4, J=0.1, seed=0, lanczos_steps=100)
+    h = esc.Handle(p)
+    m = O.Model("Kitaev", 2, 4, 1, 1, -1.0, -1.0, -1.0, p["Bxx"], p["Byy"], p["Bzz"], 0.1, 2, True)
+    w, V = np.linalg.eigh(m.dense())
+    m.set_eigenpairs(w, V)
+    nw, dw, eta = 300, 0.02, 0.05
+    ref = m.dynamics(kind, omegasteps=nw - 1, domega=dw, eta=eta)
+    h.lanczos_gs(start=O.random_start(0, h.D))
+    s = h.spectrum(kind, "CF", omega_steps=nw - 1, domega=dw, eta=eta, cf_steps=256)
+    assert s.shape == ref.shape
+    assert np.abs(s - ref).max() < 1e-8 * max(1.0, np.abs(ref).max())
