@@ -357,8 +357,11 @@ def main():
     e2e = None
     if not args.no_e2e:
         try:
+            # every rank pins its own host buffers: size them so that all ranks fit in host memory
             avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
-            ncols = 2 if avail > 4 * D * 8 + (24 << 30) else 1
+            ncols = 2 if avail > world * 4 * D * 8 + (24 << 30) else 1
+            if avail < world * 2 * D * 8 + (24 << 30):
+                raise MemoryError(f"host memory for {world} replicas' pinned vectors: {avail >> 30} GiB available")
             hin = torch.empty((ncols, D), dtype=torch.complex64, pin_memory=True)
             hout = torch.empty((ncols, D), dtype=torch.complex64, pin_memory=True)
             hin.zero_()
