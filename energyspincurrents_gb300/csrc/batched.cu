@@ -8,6 +8,12 @@
 // prev = V[it % 3], cur = V[(it + 1) % 3], w = V[(it + 2) % 3]; a graph holds three unrolled
 // iterations (one per rotation), so every kernel parameter is fixed and the iteration counter is
 // read from device memory.
+//
+// The Lanczos vectors are kept unnormalised: u_k = beta_k v_k with beta_0 = |phi| and beta_k the
+// usual off-diagonal, so no pass over the vectors only rescales them.  With w = H u_k:
+//   alpha_k   = <u_k|w> / beta_k^2
+//   u_{k+1}   = (w - alpha_k u_k) / beta_k - (beta_k / beta_{k-1}) u_{k-1},   beta_{k+1} = |u_{k+1}|
+// which is the three-term recurrence of the normalised vectors multiplied through by beta_{k+1}.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -102,9 +108,10 @@ __global__ void __launch_bounds__(BTPB) kb_dot(const typename V2B<R>::T* __restr
     block_sum2(re, im, part + ((size_t)c * gridDim.x + blockIdx.x) * 2);
 }
 
-// alpha_c[it] = sum of partials (one block per column)
+// alpha_c[it] = (sum of partials) / |u_it|^2 (one block per column)
 __global__ void __launch_bounds__(BTPB) kb_alpha(const double* __restrict__ part, int G, const int* __restrict__ it_p,
-                                                 const int* __restrict__ active, double* __restrict__ alpha, int kmax) {
+                                                 const int* __restrict__ active, double* __restrict__ alpha,
+                                                 const double* __restrict__ b2, int kmax) {
     const int c = blockIdx.x;
     if (!active[c]) return;
     double re = 0.0, im = 0.0;
@@ -116,12 +123,13 @@ __global__ void __launch_bounds__(BTPB) kb_alpha(const double* __restrict__ part
     block_sum2(re, im, out);
     if (threadIdx.x == 0) {
         const int it = *it_p;
-        alpha[((size_t)c * kmax + it) * 2] = out[0];
-        alpha[((size_t)c * kmax + it) * 2 + 1] = out[1];
+        const double nb2 = b2[(size_t)c * (kmax + 1) + it];   // |u_it|^2
+        alpha[((size_t)c * kmax + it) * 2] = out[0] / nb2;
+        alpha[((size_t)c * kmax + it) * 2 + 1] = out[1] / nb2;
     }
 }
 
-// w -= alpha cur + beta prev (beta = sqrt(b2[it]), none at it = 0); |w|^2 partials
+// w <- u_{it+1} (the recurrence above); |u_{it+1}|^2 partials
 template <typename R>
 __global__ void __launch_bounds__(BTPB) kb_update(typename V2B<R>::T* __restrict__ w,
                                                   const typename V2B<R>::T* __restrict__ cur,
@@ -133,8 +141,12 @@ __global__ void __launch_bounds__(BTPB) kb_update(typename V2B<R>::T* __restrict
     const int c = blockIdx.y;
     if (!active[c]) return;
     const int it = *it_p;
-    const R ar = (R)alpha[((size_t)c * kmax + it) * 2], ai = (R)alpha[((size_t)c * kmax + it) * 2 + 1];
-    const R be = it > 0 ? (R)sqrt(b2[(size_t)c * (kmax + 1) + it]) : (R)0;
+    // u_{it+1} = c1 w - (c2r + i c2i) u_it - c3 u_{it-1}
+    const double bk = sqrt(b2[(size_t)c * (kmax + 1) + it]);
+    const double bp = it > 0 ? sqrt(b2[(size_t)c * (kmax + 1) + it - 1]) : 1.0;
+    const R c1 = (R)(1.0 / bk);
+    const R ar = (R)(alpha[((size_t)c * kmax + it) * 2] / bk), ai = (R)(alpha[((size_t)c * kmax + it) * 2 + 1] / bk);
+    const R be = it > 0 ? (R)(bk / bp) : (R)0;
     C* W = w + (size_t)c * D;
     const C* X = cur + (size_t)c * D;
     const C* P = prev + (size_t)c * D;
@@ -153,8 +165,8 @@ __global__ void __launch_bounds__(BTPB) kb_update(typename V2B<R>::T* __restrict
         for (int u = 0; u < UNR; u++) {
             if (u >= n) break;
             C o = a[u];
-            o.x = o.x - (ar * x[u].x - ai * x[u].y);
-            o.y = o.y - (ar * x[u].y + ai * x[u].x);
+            o.x = c1 * o.x - (ar * x[u].x - ai * x[u].y);
+            o.y = c1 * o.y - (ar * x[u].y + ai * x[u].x);
             o.x = o.x - be * p[u].x;
             o.y = o.y - be * p[u].y;
             W[i + u * st] = o;
@@ -180,36 +192,9 @@ __global__ void __launch_bounds__(BTPB) kb_beta(const double* __restrict__ part,
         const int it = *it_p;
         b2[(size_t)c * (kmax + 1) + it + 1] = out[0];
         const double b0 = sqrt(b2[(size_t)c * (kmax + 1)]);
-        // 2: stops after this iteration; kb_scale still normalises its last vector, kb_advance clears it
+        // 2: stops after this iteration (kb_advance clears it)
         if (!(sqrt(out[0]) > tol * b0) || it + 1 >= steps[c]) active[c] = 2;
     }
-}
-
-// w /= beta (columns still active, and the column that just stopped)
-template <typename R>
-__global__ void __launch_bounds__(BTPB) kb_scale(typename V2B<R>::T* __restrict__ w, long long D,
-                                                 const int* __restrict__ it_p, const int* __restrict__ active,
-                                                 const double* __restrict__ b2, int kmax) {
-    typedef typename V2B<R>::T C;
-    const int c = blockIdx.y;
-    if (!active[c]) return;
-    const int it = *it_p;
-    const double nb = sqrt(b2[(size_t)c * (kmax + 1) + it + 1]);
-    const R inv = (R)(nb > 0.0 ? 1.0 / nb : 0.0);
-    C* W = w + (size_t)c * D;
-    stream_loop(D, [&](long long i, long long st, int n) {
-        C a[UNR];
-#pragma unroll
-        for (int u = 0; u < UNR; u++)
-            if (u < n) a[u] = W[i + u * st];
-#pragma unroll
-        for (int u = 0; u < UNR; u++)
-            if (u < n) {
-                a[u].x *= inv;
-                a[u].y *= inv;
-                W[i + u * st] = a[u];
-            }
-    });
 }
 
 __global__ void kb_advance(int* it_p, int* active, int ncols) {
@@ -218,7 +203,7 @@ __global__ void kb_advance(int* it_p, int* active, int ncols) {
     *it_p += 1;
 }
 
-// |phi_c|^2 -> b2[c][0]; cur_c /= |phi_c|
+// |phi_c|^2 -> b2[c][0] (u_0 = phi_c, unnormalised)
 template <typename R>
 __global__ void __launch_bounds__(BTPB) kb_norm0(const typename V2B<R>::T* __restrict__ v, long long D,
                                                  double* __restrict__ part) {
@@ -247,21 +232,6 @@ __global__ void __launch_bounds__(BTPB) kb_norm0_final(const double* __restrict_
         active[c] = out[0] > 0.0 ? 1 : 0;
     }
 }
-template <typename R>
-__global__ void __launch_bounds__(BTPB) kb_scale0(typename V2B<R>::T* __restrict__ w, long long D,
-                                                  const double* __restrict__ b2, int kmax) {
-    const int c = blockIdx.y;
-    const double nb = sqrt(b2[(size_t)c * (kmax + 1)]);
-    const R inv = (R)(nb > 0.0 ? 1.0 / nb : 0.0);
-    typename V2B<R>::T* W = w + (size_t)c * D;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) {
-        typename V2B<R>::T a = W[i];
-        a.x *= inv;
-        a.y *= inv;
-        W[i] = a;
-    }
-}
 
 template <typename R>
 void CFBatch<R>::run(cudaStream_t s) {
@@ -274,7 +244,6 @@ void CFBatch<R>::run(cudaStream_t s) {
         ESC_CUDA(cudaMemsetAsync(d_it, 0, sizeof(int), s));
         kb_norm0<R><<<gcol, BTPB, 0, s>>>(V[1], D, d_part);
         kb_norm0_final<<<ncols, BTPB, 0, s>>>(d_part, BGRID, d_b2, kmax, d_active);
-        kb_scale0<R><<<gcol, BTPB, 0, s>>>(V[1], D, d_b2, kmax);
         ESC_CUDA(cudaGetLastError());
     } else {
         // pageable source: the copy completes before cudaMemcpyAsync returns
@@ -286,10 +255,9 @@ void CFBatch<R>::run(cudaStream_t s) {
         C* w = V[(r + 2) % 3];
         for (int c = 0; c < ncols; c++) hv_column(c, cur + (size_t)c * D, w + (size_t)c * D, d_active + c, s);
         kb_dot<R><<<gcol, BTPB, 0, s>>>(cur, w, D, d_active, d_part);
-        kb_alpha<<<ncols, BTPB, 0, s>>>(d_part, BGRID, d_it, d_active, d_alpha, kmax);
+        kb_alpha<<<ncols, BTPB, 0, s>>>(d_part, BGRID, d_it, d_active, d_alpha, d_b2, kmax);
         kb_update<R><<<gcol, BTPB, 0, s>>>(w, cur, prev, D, d_it, d_active, d_alpha, d_b2, kmax, d_part);
         kb_beta<<<ncols, BTPB, 0, s>>>(d_part, BGRID, d_it, d_active, d_b2, kmax, d_steps, tol);
-        kb_scale<R><<<gcol, BTPB, 0, s>>>(w, D, d_it, d_active, d_b2, kmax);
         kb_advance<<<1, 1, 0, s>>>(d_it, d_active, ncols);
         ESC_CUDA(cudaGetLastError());
     };
