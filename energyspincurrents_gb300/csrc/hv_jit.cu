@@ -44,9 +44,14 @@ std::mutex g_mu;
 std::vector<JitEntry> g_entries;
 std::map<std::string, std::vector<int>> g_cache;   // device + source -> entry per kernel
 
+// 4096-state tiles (and 2048): 512, 256 or 128 threads; 8192-state tiles: 512 or 256 threads
 bool eligible(const DevPass& p) {
-    return p.c == 3 && (p.Tp == 11 || p.Tp == 12) && p.tb_bits >= 7 && p.tb_bits <= 9 && p.nterm > 0;
+    const bool shape = (p.Tp == 11 || p.Tp == 12) ? p.tb_bits >= 7 && p.tb_bits <= 9 : p.Tp == 13 && (p.tb_bits == 8 || p.tb_bits == 9);
+    return p.c == 3 && shape && p.nterm > 0;
 }
+
+// CTAs per SM of the register budget: two for 4096-state tiles, one for 8192 (2 x 64 KB ring)
+int min_ctas(const DevPass& p) { return p.Tp >= 13 ? 1 : 2; }
 
 std::string hexf(float x) {
     unsigned u;
@@ -84,7 +89,7 @@ std::string terms_source(const DevPass& p, int k) {
         o << "    }\n";
     }
     o << "  }\n};\n"
-      << "extern \"C\" __global__ void __launch_bounds__(" << TB << ", 2) esc_jit_pass" << k
+      << "extern \"C\" __global__ void __launch_bounds__(" << TB << ", " << min_ctas(p) << ") esc_jit_pass" << k
       << "(const __grid_constant__ escdev::PassTab p, const float* __restrict__ diag, const float2* __restrict__ in,"
          " float2* __restrict__ out, long long ntiles, const int* __restrict__ active) {\n"
       << "  escdev::pass_body<" << E << ", " << (p.stages >= 2 && p.stages <= 4 ? p.stages : 2) << ", Terms" << k << ", "

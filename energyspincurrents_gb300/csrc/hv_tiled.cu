@@ -428,8 +428,10 @@ struct RuntimeTerms {
     }
 };
 
+// Two CTAs per SM for 4096-state tiles; one for 8192-state tiles (2 x 64 KB ring, 128 registers
+// for each of 512 threads).
 template <int E, int NS, int TB>
-__global__ void __launch_bounds__(TB, 2) k_hv_pass_f32g(const __grid_constant__ escdev::PassTab pt,
+__global__ void __launch_bounds__(TB, TB * E >= 8192 ? 1 : 2) k_hv_pass_f32g(const __grid_constant__ escdev::PassTab pt,
                                                       const __grid_constant__ DevPass p,
                                                       const float* __restrict__ diag,
                                                       const float2* __restrict__ in,
@@ -842,9 +844,12 @@ void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, cons
                 jit_launch(p, make_pass_tab(p, m), diag, in, out, D, sms, s, active);
                 continue;
             }
-            if (diag && p.c == 3 && (p.Tp == 11 || p.Tp == 12) && p.tb_bits >= 7 && p.tb_bits <= 9) {
+            if (diag && p.c == 3 && ((p.Tp == 11 || p.Tp == 12) ? p.tb_bits >= 7 && p.tb_bits <= 9 : p.Tp == 13 && p.tb_bits == 9)) {
                 // E = 2^(Tp - tb_bits) states per thread
-                switch ((p.tb_bits == 8 ? 100 : p.tb_bits == 7 ? 200 : 0) + (p.Tp == 11 ? 10 : 20) + p.stages) {
+                switch ((p.tb_bits == 8 ? 100 : p.tb_bits == 7 ? 200 : 0) + (p.Tp == 11 ? 10 : p.Tp == 12 ? 20 : 30) + p.stages) {
+                    case 32: run_f32g<16, 2, 512>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 33: run_f32g<16, 3, 512>(m, p, diag, in, out, D, sms, s, active); break;
+                    case 34: run_f32g<16, 4, 512>(m, p, diag, in, out, D, sms, s, active); break;
                     case 212: run_f32g<16, 2, 128>(m, p, diag, in, out, D, sms, s, active); break;
                     case 213: run_f32g<16, 3, 128>(m, p, diag, in, out, D, sms, s, active); break;
                     case 214: run_f32g<16, 4, 128>(m, p, diag, in, out, D, sms, s, active); break;

@@ -6,7 +6,8 @@
 //   1. picks c "shared" sites that are tile bits of every pass (the lowest index bits, so every
 //      tile is made of runs of 2^c consecutive states: coalesced loads),
 //   2. covers every bond by clusters of at most T-c further sites (greedy growth that maximises
-//      newly covered bonds, many random restarts, keeps the fewest passes),
+//      newly covered bonds, many random restarts, keeps the fewest passes), then looks for a
+//      covering with one cluster less at a time by simulated annealing,
 //   3. numbers the sites so that pass 1 is the contiguous block of the T lowest bits and each later
 //      pass's new sites are contiguous too,
 //   4. assigns every term to the first pass whose tile contains it (the diagonal to pass 1).
@@ -104,6 +105,155 @@ Cand greedy(int N, int T, int c, const std::vector<std::pair<int, int>>& bonds, 
     return r;
 }
 
+// exp(x) for x <= 0 from basic IEEE operations only (Taylor series of exp(x / 64), squared six
+// times), so that the planner makes the same choices on every host.
+double exp_basic(double x) {
+    const double y = x / 64.0;
+    double t = 1.0, s = 1.0;
+    for (int k = 1; k <= 10; k++) { t = t * y / k; s += t; }
+    for (int k = 0; k < 6; k++) s *= s;
+    return s;
+}
+
+// Annealed covering with a fixed number of passes P: c shared sites plus P clusters of exactly T-c
+// further sites each; the cost is the number of bonds that lie in no tile plus the number of sites
+// in none.  Moves: swap one cluster site for an outside site (biased towards the ends of uncovered
+// bonds), or swap a shared site with another site.  Only the bonds at the moved sites are
+// re-examined, so a move costs O(P x degree).  Returns an empty candidate when no zero-cost
+// covering is reached within the budget.
+Cand anneal(int N, int T, int c, int P, const std::vector<std::pair<int, int>>& bonds,
+            const std::vector<std::vector<int>>& adj, std::mt19937_64& rng, long iters) {
+    const int free = T - c, B = (int)bonds.size();
+    if (free <= 0 || c + P * free < N) return {};
+    std::vector<std::vector<int>> inc(N);   // bonds at each site
+    for (int b = 0; b < B; b++) { inc[bonds[b].first].push_back(b); inc[bonds[b].second].push_back(b); }
+    std::uniform_real_distribution<double> U01(0.0, 1.0);
+    auto rnd = [&](int n) { return std::uniform_int_distribution<int>(0, n - 1)(rng); };
+    std::vector<char> inC(N, 0);
+    std::vector<std::vector<char>> inS(P, std::vector<char>(N, 0));
+    std::vector<std::vector<int>> S(P);
+    // initial state: shared sites along a random path, clusters grown breadth-first from random seeds
+    {
+        int s0 = rnd(N);
+        std::vector<int> C{s0};
+        inC[s0] = 1;
+        while ((int)C.size() < c) {
+            std::vector<int> nb;
+            for (int x : C) for (int y : adj[x]) if (!inC[y]) nb.push_back(y);
+            int y = nb.empty() ? rnd(N) : nb[rnd((int)nb.size())];
+            if (!inC[y]) { inC[y] = 1; C.push_back(y); }
+        }
+        for (int p = 0; p < P; p++) {
+            std::vector<int> q{rnd(N)};
+            for (size_t h = 0; h < q.size() && (int)S[p].size() < free; h++) {
+                const int x = q[h];
+                if (inC[x] || inS[p][x]) continue;
+                inS[p][x] = 1;
+                S[p].push_back(x);
+                for (int y : adj[x]) q.push_back(y);
+            }
+            while ((int)S[p].size() < free) {
+                const int x = rnd(N);
+                if (!inC[x] && !inS[p][x]) { inS[p][x] = 1; S[p].push_back(x); }
+            }
+        }
+    }
+    auto in_tile = [&](int p, int x) { return inC[x] || inS[p][x]; };
+    std::vector<int> bcov(B, 0), scov(N, 0);
+    for (int b = 0; b < B; b++)
+        for (int p = 0; p < P; p++) bcov[b] += in_tile(p, bonds[b].first) && in_tile(p, bonds[b].second);
+    for (int x = 0; x < N; x++) scov[x] = inC[x] ? P : 0;
+    for (int p = 0; p < P; p++) for (int x : S[p]) scov[x]++;
+    int cost = 0;
+    for (int b = 0; b < B; b++) cost += bcov[b] == 0;
+    for (int x = 0; x < N; x++) cost += scov[x] == 0;
+    // re-examine the bonds at the given sites (each once); returns the cost change
+    std::vector<int> mark(B, -1);
+    int stamp = 0;
+    auto refresh = [&](const int* xs, int nx) {
+        int d = 0;
+        stamp++;
+        for (int i = 0; i < nx; i++)
+            for (int b : inc[xs[i]]) {
+                if (mark[b] == stamp) continue;
+                mark[b] = stamp;
+                int n = 0;
+                for (int p = 0; p < P; p++) n += in_tile(p, bonds[b].first) && in_tile(p, bonds[b].second);
+                d += (n == 0) - (bcov[b] == 0);
+                bcov[b] = n;
+            }
+        return d;
+    };
+    std::vector<int> open_ends;
+    const double t0 = 0.6, log_t1_t0 = -2.995732273553991;   // final temperature 0.03 = 0.05 t0
+    for (long it = 0; it < iters && cost > 0; it++) {
+        const double temp = t0 * exp_basic(log_t1_t0 * (double)it / (double)iters);
+        if (c > 0 && rnd(20) == 0) {
+            // swap shared site a with outside site b: b leaves every cluster it was in, and a takes
+            // its place there (cluster sizes are kept)
+            int ai = rnd(N), bi = rnd(N);
+            if (!inC[ai] || inC[bi]) continue;
+            std::vector<int> had;
+            for (int p = 0; p < P; p++) if (inS[p][bi]) had.push_back(p);
+            auto apply = [&](int a, int b2, bool fwd) {
+                inC[a] = 0; inC[b2] = 1;
+                for (int p : had) {
+                    if (fwd) { inS[p][bi] = 0; inS[p][ai] = 1; std::replace(S[p].begin(), S[p].end(), bi, ai); }
+                    else { inS[p][ai] = 0; inS[p][bi] = 1; std::replace(S[p].begin(), S[p].end(), ai, bi); }
+                }
+            };
+            auto site_cost = [&](int x) { return scov[x] == 0 ? 1 : 0; };
+            const int before = site_cost(ai) + site_cost(bi);
+            apply(ai, bi, true);
+            const int sa = scov[ai], sb = scov[bi];
+            scov[ai] = (int)had.size();
+            scov[bi] = P;
+            const int xs[2] = {ai, bi};
+            const int d = refresh(xs, 2) + site_cost(ai) + site_cost(bi) - before;
+            if (d <= 0 || U01(rng) < exp_basic(-d / temp)) { cost += d; continue; }
+            apply(bi, ai, false);
+            inC[bi] = 0; inC[ai] = 1;
+            scov[ai] = sa; scov[bi] = sb;
+            refresh(xs, 2);
+            continue;
+        }
+        const int p = rnd(P);
+        const int xi = rnd(free), x = S[p][xi];
+        int y = -1;
+        if (rnd(3) != 0) {
+            open_ends.clear();
+            for (int b = 0; b < B; b++)
+                if (bcov[b] == 0) {
+                    const int i = bonds[b].first, j = bonds[b].second;
+                    if (!in_tile(p, i)) open_ends.push_back(i);
+                    if (!in_tile(p, j)) open_ends.push_back(j);
+                }
+            for (int z = 0; z < N; z++) if (scov[z] == 0) open_ends.push_back(z);
+            if (!open_ends.empty()) y = open_ends[rnd((int)open_ends.size())];
+        }
+        if (y < 0) {
+            // a neighbour of the cluster
+            const int z = S[p][rnd(free)];
+            y = adj[z].empty() ? rnd(N) : adj[z][rnd((int)adj[z].size())];
+        }
+        if (inC[y] || inS[p][y]) continue;
+        const int before = (scov[x] == 0) + (scov[y] == 0);
+        inS[p][x] = 0; inS[p][y] = 1; S[p][xi] = y;
+        scov[x]--; scov[y]++;
+        const int xs[2] = {x, y};
+        const int d = refresh(xs, 2) + (scov[x] == 0) + (scov[y] == 0) - before;
+        if (d <= 0 || U01(rng) < exp_basic(-d / temp)) { cost += d; continue; }
+        inS[p][y] = 0; inS[p][x] = 1; S[p][xi] = x;
+        scov[x]++; scov[y]--;
+        refresh(xs, 2);
+    }
+    if (cost > 0) return {};
+    Cand r;
+    for (int x = 0; x < N; x++) if (inC[x]) r.C.push_back(x);
+    r.S = S;
+    return r;
+}
+
 }  // namespace
 
 Plan make_plan_reference_order(int N, const std::vector<std::pair<int, int>>& bonds, int T, int c, int restarts) {
@@ -164,6 +314,14 @@ Plan make_plan(int N, const std::vector<std::pair<int, int>>& bonds, int T, int 
         for (auto& s : cd.S) cost += s.size();
         if (cost < best_cost) { best_cost = cost; best = cd; }
     }
+    // fewer passes than the greedy covering: annealed coverings with one pass less at a time
+    if (!std::getenv("ESC_PLAN_GREEDY"))
+        for (int np = (int)best.S.size() - 1; np >= 1; np--) {
+            Cand a;
+            for (int t = 0; t < 8 && a.S.empty(); t++) a = anneal(N, T, c, np, bonds, adj, rng, 400000);
+            if (a.S.empty()) break;
+            best = a;
+        }
     // bit numbering: shared sites -> [0,c), first cluster -> [c, c+|S1|), later clusters' new sites next
     P.perm.assign(N, -1);
     int nextbit = 0;

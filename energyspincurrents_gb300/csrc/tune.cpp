@@ -82,8 +82,8 @@ bool load_tuning(esc_handle* h) {
     return true;
 }
 
-// Self-tuning of the complex64 H.v.  Plans: tile bits T in {11, 12, 13} (above 26 sites only 12:
-// the others never win there -- one more pass, or one CTA per SM) x first-fit / group-minimising
+// Self-tuning of the complex64 H.v.  Plans: tile bits T in {11, 12, 13} (above 26 sites 12 and 13:
+// 11 needs one pass more there) x first-fit / group-minimising
 // term-to-pass assignment (make_passes modes 0 and 2; the balanced mode 1 never won).  Kernel variants per plan: ahead-of-time vs run-time specialised;
 // 512, 256 or 128 threads per 4096-state tile (8, 16, 32 register states each); 2 or 3 tile buffers,
 // or 2 plus staged epilogue loads.  Every variant is timed pass by pass (CUDA events on the
@@ -126,7 +126,7 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
     std::vector<esc::DevPass> bpasses;
     try {
         for (int T : {11, 12, 13}) {
-            if (T > h->N || (h->N > 26 && T != 12)) continue;
+            if (T > h->N || (h->N > 26 && T == 11)) continue;
             const esc::Plan plan = esc::make_plan(h->N, bond_pairs(h), T, 3, 200);
             for (int balance : {0, 2}) {
                 std::vector<std::vector<esc::DevPass>> vars;
@@ -134,7 +134,7 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
                 for (int tb : {9, 8, 7})
                 for (int stages : {2, 3, 4})
                     for (int jit : {0, 1}) {
-                        if (T == 13 && (jit || tb != 9)) continue;   // 8192-state tiles: generic kernel only
+                        if (T == 13 && (tb == 7 || (tb == 8 && !jit))) continue;   // 8192-state tiles: 512 threads, or 256 specialised
                         install_plan(h, plan, balance, stages, tb);
                         if (jit) specialise(h, h->passes, 1);
                         bool spec = false;

@@ -155,3 +155,22 @@ def test_planner_covers_every_term(shape, J, tile):
     N = Lx * Ly
     T = tile[0]
     assert npass == 1 if N <= T else 2 <= npass <= 2 + 2 * (N - T)
+
+
+@pytest.mark.parametrize("shape,tile,most", [((3, 8), 12, 3), ((4, 8), 13, 4), ((4, 8), 12, 5), ((7, 4), 13, 3)])
+def test_planner_annealed_pass_counts(shape, tile, most):
+    """Pass counts of the annealed covering (Kitaev-Heisenberg, every bond off-diagonal): 3 passes
+    of 4096-state tiles at 24 sites and 4 of 8192-state tiles at 32, one fewer than the greedy
+    covering alone (ESC_PLAN_GREEDY)."""
+    Lx, Ly = shape
+    b = -0.02 / 3 ** 0.5
+    p = dict(Lx=Lx, Ly=Ly, Kxx=-1.0, Kyy=-1.0, Kzz=-1.0, Bxx=b, Byy=b, Bzz=b, jheis=0.05)
+    perm, npass = esc.plan(p, tile, 3)
+    assert sorted(perm.tolist()) == list(range(Lx * Ly))
+    assert npass <= most
+    if tile == 13 and Lx * Ly == 32 or tile == 12 and Lx * Ly == 24:
+        os.environ["ESC_PLAN_GREEDY"] = "1"
+        try:
+            assert esc.plan(p, tile, 3)[1] == npass + 1
+        finally:
+            del os.environ["ESC_PLAN_GREEDY"]
