@@ -22,6 +22,7 @@ constexpr int TPB = 512;
 struct PassTab {
     unsigned long long tabLo[64];
     unsigned long long tabHi[16];
+    unsigned long long rmask;   // the global bits of the tile number (tile_bits of all ones)
     unsigned char rest[40];
     int nrest, diag, accumulate, N;
     float fx, fy, fz, pad;   // Bx/2, By/2, Bz/2
@@ -39,6 +40,12 @@ __device__ __forceinline__ unsigned long long tile_bits(const PassTab& p, long l
     unsigned long long b = 0;
     for (int q = 0; q < p.nrest; q++) b |= (((unsigned long long)t >> q) & 1ull) << p.rest[q];
     return b;
+}
+// tile_bits(a + b) from x = tile_bits(a) and y = tile_bits(b): the bits outside the mask are set to
+// one so that carries run across them, then cleared (bits carried past the top are dropped, which
+// only happens for tile numbers past the last tile)
+__device__ __forceinline__ unsigned long long deposit_add(unsigned long long x, unsigned long long y, unsigned long long m) {
+    return ((x | ~m) + y) & m;
 }
 
 // Partners of a group: P[j] = state (t ^ lo) + TB j of the tile (TB threads per tile).
@@ -69,7 +76,9 @@ __device__ __forceinline__ void gfield(const float2 (&P)[E], float2 vfx, float f
         const float2 w = P[FB < 0 ? j : (j ^ (1 << FB))];
         const float sg = FB < 0 ? sf : (((j >> FB) & 1) ? fy : -fy);
         acc[j] = __ffma2_rn(vfx, w, acc[j]);
-        acc[j] = __ffma2_rn(make_float2(-sg, sg), make_float2(w.y, w.x), acc[j]);
+        // the i s part crosses the components: two scalar FMAs (no swapped register pair)
+        acc[j].x = fmaf(-sg, w.y, acc[j].x);
+        acc[j].y = fmaf(sg, w.x, acc[j].y);
     }
 }
 
@@ -95,10 +104,10 @@ __device__ __forceinline__ void tile_offsets(const PassTab& p, int tid, unsigned
     lo2[0] = p.tabLo[(tid >> 2) & 63] | (unsigned long long)((2 * tid) & 7);
     lo2[1] = p.tabLo[((tid >> 2) + 32) & 63] | (unsigned long long)((2 * tid) & 7);
 }
+// copies tile b (b = tile_bits of its number) into dst
 template <int E, int TB>
-__device__ __forceinline__ void issue_tile(const PassTab& p, const float2* __restrict__ in, float2* dst, long long tt,
-                                           int tid, const unsigned long long (&lo2)[2]) {
-    const unsigned long long b = tile_bits(p, tt);
+__device__ __forceinline__ void issue_tile(const PassTab& p, const float2* __restrict__ in, float2* dst,
+                                           unsigned long long b, int tid, const unsigned long long (&lo2)[2]) {
 #pragma unroll
     for (int i = 0; i < E / 2; i++) {
         const unsigned long long l = (TB == 128 && (i & 1)) ? lo2[1] : lo2[0];
@@ -124,10 +133,13 @@ __device__ __forceinline__ void pass_body_staged(const PassTab& p, const Terms& 
     __syncthreads();
     const long long g = gridDim.x;
     long long t = blockIdx.x;
-    if (t < ntiles) issue_tile<E, TB>(p, in, bufs, t, tid, lo2);
+    const unsigned long long dg = tile_bits(p, g);
+    unsigned long long bt = tile_bits(p, t);             // tile t
+    unsigned long long bn = deposit_add(bt, dg, p.rmask);   // tile t + g
+    if (t < ntiles) issue_tile<E, TB>(p, in, bufs, bt, tid, lo2);
     cp_async_commit();
-    for (int cur = 0; t < ntiles; t += g, cur ^= 1) {
-        const unsigned long long base = tile_bits(p, t) | lo;
+    for (int cur = 0; t < ntiles; t += g, cur ^= 1, bt = bn, bn = deposit_add(bn, dg, p.rmask)) {
+        const unsigned long long base = bt | lo;
         // [partials of tile t]: thread-private staging slots, read back by the same thread
 #pragma unroll
         for (int j = 0; j < E; j++) {
@@ -135,7 +147,7 @@ __device__ __forceinline__ void pass_body_staged(const PassTab& p, const Terms& 
             else if (p.accumulate) cp_async8(stage + tid + TB * j, out + (base | hi_off[j]));
         }
         cp_async_commit();
-        if (t + g < ntiles) issue_tile<E, TB>(p, in, bufs + (cur ^ 1) * (TB * E), t + g, tid, lo2);   // [tile t+g]
+        if (t + g < ntiles) issue_tile<E, TB>(p, in, bufs + (cur ^ 1) * (TB * E), bn, tid, lo2);   // [tile t+g]
         cp_async_commit();
         cp_async_wait<2>();         // tile t has landed
         __syncthreads();
@@ -195,19 +207,25 @@ __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, 
     const float fy = p.fy, fz = p.fz;
     __syncthreads();
     const long long g = gridDim.x;
-    auto issue = [&](long long tt, int slot) {
-        if (tt < ntiles) issue_tile<E, TB>(p, in, bufs + slot * (TB * E), tt, tid, lo2);
+    auto issue = [&](long long tt, unsigned long long bb, int slot) {
+        if (tt < ntiles) issue_tile<E, TB>(p, in, bufs + slot * (TB * E), bb, tid, lo2);
         cp_async_commit();
     };
     long long t = blockIdx.x;
+    const unsigned long long dg = tile_bits(p, g);
+    unsigned long long bt = tile_bits(p, t), bi = bt;   // tile t; the next tile to copy
 #pragma unroll
-    for (int s = 0; s < NS - 1; s++) issue(t + s * g, s);
-    for (int cur = 0; t < ntiles; t += g, cur = (cur + 1 == NS ? 0 : cur + 1)) {
-        issue(t + (NS - 1) * g, cur == 0 ? NS - 1 : cur - 1);
+    for (int s = 0; s < NS - 1; s++) {
+        issue(t + s * g, bi, s);
+        bi = deposit_add(bi, dg, p.rmask);
+    }
+    for (int cur = 0; t < ntiles; t += g, cur = (cur + 1 == NS ? 0 : cur + 1), bt = deposit_add(bt, dg, p.rmask)) {
+        issue(t + (NS - 1) * g, bi, cur == 0 ? NS - 1 : cur - 1);
+        bi = deposit_add(bi, dg, p.rmask);
         cp_async_wait<NS - 1>();
         __syncthreads();
         float2* tile = bufs + cur * (TB * E);
-        const unsigned long long base = tile_bits(p, t) | lo;
+        const unsigned long long base = bt | lo;
         float2 acc[E], pre[E];
         float dpre[E];
 #pragma unroll

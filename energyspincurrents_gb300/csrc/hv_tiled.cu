@@ -447,6 +447,8 @@ escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m) {
     std::memcpy(t.tabHi, p.tabHi, sizeof(t.tabHi));
     std::memcpy(t.rest, p.rest, sizeof(t.rest));
     t.nrest = p.nrest;
+    t.rmask = 0;
+    for (int q = 0; q < p.nrest; q++) t.rmask |= 1ull << p.rest[q];
     t.diag = p.diag;
     t.accumulate = p.accumulate;
     t.N = m.N;
