@@ -138,6 +138,16 @@ def cpu_baseline(params, sites, target_s=12.0, kind="port"):
                       f"oracle matrix-free gather (oracle/esc_oracle.cpp hv_matfree)"}
 
 
+def workload_config(sites, world):
+    """The `config` both arms report for the --sites workload."""
+    params = workload(sites)
+    D = 1 << sites
+    return {"workload": f"Kitaev-Heisenberg honeycomb N={sites} ({params['Lx']}x{params['Ly']//2} "
+                        f"unit cells, PBC), K=-1 J=0.05 h=0.02[111], one H.v per step (complex64)",
+            "states": D, "l2": "inputs larger than L2 (no flush needed)" if D * 8 > 129e6 else "inputs smaller than L2",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -146,7 +156,7 @@ def run_reference(args, rank):
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "GB/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-            "config": {"workload": f"Kitaev-Heisenberg honeycomb N={args.sites} H.v (CPU oracle port, bounded sample)"},
+            "config": workload_config(args.sites, args.gpus),
             "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "GB/s", "h2d_bytes_per_step": 0,
                                           "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -398,11 +408,7 @@ def main():
         line = {"metric": METRIC, "value": round(gbs_total, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-                "config": {"workload": f"Kitaev-Heisenberg honeycomb N={args.sites} ({params['Lx']}x{params['Ly']//2} "
-                                       f"unit cells, PBC), K=-1 J=0.05 h=0.02[111], one H.v per step (complex64)",
-                           "states": D, "l2": "inputs larger than L2 (no flush needed)" if D * 8 > 129e6 else
-                           "inputs smaller than L2", "parallelism": "replicas" if world > 1 else "single GPU",
-                           "tuning": tuning},
+                "config": dict(workload_config(args.sites, world), tuning=tuning),
                 "roofline": roof, "cpu_baseline": cb, "e2e": e2e, "time_to_S": tts, "clocks": clk.summary(),
                 "gpu_launches": args.steps * npasses}
         print(json.dumps(line), flush=True)
