@@ -492,6 +492,20 @@ def test_8192_state_tiles_match(tb, jit, stages, monkeypatch):
         assert np.array_equal(esc.Handle(p).hv(x), y)
 
 
+def test_8192_state_tiles_fp64_hv_and_energy(monkeypatch):
+    """The 8192-state plan on the FP64 paths: the complex128 H.v against the oracle to FP64
+    rounding, and the FP64 energy sweep (Rayleigh quotient) against the oracle's <x|H|x>."""
+    p = kitaev(Lx=3, Ly=8, J=0.1)
+    monkeypatch.setenv("ESC_TILE_BITS", "13")
+    h = esc.Handle(p)
+    m = O.Model("Kitaev", 3, 8, 1, 1, -1.0, -1.0, -1.0, p["Bxx"], p["Byy"], p["Bzz"], 0.1, 4, False)
+    x = O.random_start(13, h.D)
+    y = m.hv(x)
+    assert relerr(h.hv(x), y) < 1e-13
+    ref = np.vdot(x, y).real / np.vdot(x, x).real   # near 0 for a random vector: absolute bound
+    assert abs(h.rayleigh(x) - ref) < 1e-13
+
+
 def test_tuning_file_roundtrip(tmp_path, monkeypatch):
     """The self-tuner's choice is written to ESC_TUNE_FILE and a new handle for the same Hamiltonian
     applies it without timing: same H.v, bit for bit."""
