@@ -85,8 +85,9 @@ bool load_tuning(esc_handle* h) {
 // Self-tuning of the complex64 H.v.  Plans: tile bits T in {11, 12, 13} (above 26 sites 12 and 13:
 // 11 needs one pass more there) x first-fit / group-minimising
 // term-to-pass assignment (make_passes modes 0 and 2; the balanced mode 1 never won).  Kernel variants per plan: ahead-of-time vs run-time specialised;
-// 512, 256 or 128 threads per 4096-state tile (8, 16, 32 register states each); 2 or 3 tile buffers,
-// or 2 plus staged epilogue loads.  Every variant is timed pass by pass (CUDA events on the
+// 512, 256 or 128 threads per 4096-state tile (8, 16, 32 register states each), 512 or 256 (the
+// latter specialised only) per 8192-state tile (16, 32); 2 or 3 tile buffers, or 2 plus staged
+// epilogue loads.  Every variant is timed pass by pass (CUDA events on the
 // handle's stream, median of 3 after a warm-up); a plan's composite takes the fastest variant of
 // each pass (light and heavy passes prefer different variants) and is timed as a whole; the
 // fastest composite is installed.  All variants compute the same H.v up to complex64 rounding (the
