@@ -133,7 +133,7 @@ Cand anneal(int N, int T, int c, int P, const std::vector<std::pair<int, int>>& 
     std::vector<std::vector<char>> inS(P, std::vector<char>(N, 0));
     std::vector<std::vector<int>> S(P);
     // initial state: shared sites along a random path, clusters grown breadth-first from random seeds
-    {
+    if (c > 0) {
         int s0 = rnd(N);
         std::vector<int> C{s0};
         inC[s0] = 1;
@@ -143,19 +143,19 @@ Cand anneal(int N, int T, int c, int P, const std::vector<std::pair<int, int>>& 
             int y = nb.empty() ? rnd(N) : nb[rnd((int)nb.size())];
             if (!inC[y]) { inC[y] = 1; C.push_back(y); }
         }
-        for (int p = 0; p < P; p++) {
-            std::vector<int> q{rnd(N)};
-            for (size_t h = 0; h < q.size() && (int)S[p].size() < free; h++) {
-                const int x = q[h];
-                if (inC[x] || inS[p][x]) continue;
-                inS[p][x] = 1;
-                S[p].push_back(x);
-                for (int y : adj[x]) q.push_back(y);
-            }
-            while ((int)S[p].size() < free) {
-                const int x = rnd(N);
-                if (!inC[x] && !inS[p][x]) { inS[p][x] = 1; S[p].push_back(x); }
-            }
+    }
+    for (int p = 0; p < P; p++) {
+        std::vector<int> q{rnd(N)};
+        for (size_t h = 0; h < q.size() && (int)S[p].size() < free; h++) {
+            const int x = q[h];
+            if (inC[x] || inS[p][x]) continue;
+            inS[p][x] = 1;
+            S[p].push_back(x);
+            for (int y : adj[x]) q.push_back(y);
+        }
+        while ((int)S[p].size() < free) {
+            const int x = rnd(N);
+            if (!inC[x] && !inS[p][x]) { inS[p][x] = 1; S[p].push_back(x); }
         }
     }
     auto in_tile = [&](int p, int x) { return inC[x] || inS[p][x]; };
@@ -315,7 +315,8 @@ Plan make_plan(int N, const std::vector<std::pair<int, int>>& bonds, int T, int 
         if (cost < best_cost) { best_cost = cost; best = cd; }
     }
     // fewer passes than the greedy covering: annealed coverings with one pass less at a time
-    if (!std::getenv("ESC_PLAN_GREEDY"))
+    const char* greedy_only = std::getenv("ESC_PLAN_GREEDY");
+    if (!greedy_only || std::atoi(greedy_only) == 0)
         for (int np = (int)best.S.size() - 1; np >= 1; np--) {
             Cand a;
             for (int t = 0; t < 8 && a.S.empty(); t++) a = anneal(N, T, c, np, bonds, adj, rng, 400000);

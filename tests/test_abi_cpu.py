@@ -144,7 +144,7 @@ def test_device_entry_points_fail_loudly_without_gpu():
 
 @pytest.mark.parametrize("shape,J", [((3, 4), 0.0), ((4, 4), 0.1), ((3, 6), 0.1), ((3, 8), 0.1), ((7, 4), 0.05),
                                      ((4, 8), 0.05), ((5, 6), 0.05)])
-@pytest.mark.parametrize("tile", [(13, 3), (10, 3), (14, 4)])
+@pytest.mark.parametrize("tile", [(13, 3), (10, 3), (14, 4), (12, 1)])
 def test_planner_covers_every_term(shape, J, tile):
     """esc_plan builds the pass list (make_passes throws if any bond fits no tile) and a bijective
     site -> bit relabelling; pass counts stay small."""
