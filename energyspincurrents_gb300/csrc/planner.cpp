@@ -15,9 +15,12 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <numeric>
 #include <random>
 #include <set>
+#include <string>
 
 #include "esc_internal.h"
 
@@ -287,7 +290,37 @@ Plan make_plan_reference_order(int N, const std::vector<std::pair<int, int>>& bo
     return P;
 }
 
+namespace {
+Plan search_plan(int N, const std::vector<std::pair<int, int>>& bonds, int T, int c, int restarts, bool anneal_more);
+}
+
+// The search is deterministic (fixed seed) but takes seconds from 26 sites, and handle creation, the
+// self-tuner and the tuning file ask for the same plans again: results are kept per process, keyed
+// by everything the search reads.
 Plan make_plan(int N, const std::vector<std::pair<int, int>>& bonds, int T, int c, int restarts) {
+    if (N >= 26) restarts = std::max(restarts, 20000);   // large bases: fewer passes are worth ~3 s here
+    if (const char* e = std::getenv("ESC_PLAN_RESTARTS")) restarts = std::max(1, std::atoi(e));
+    const char* greedy_only = std::getenv("ESC_PLAN_GREEDY");
+    const bool anneal_more = !greedy_only || std::atoi(greedy_only) == 0;
+    std::string key = std::to_string(N) + "/" + std::to_string(T) + "/" + std::to_string(c) + "/" +
+                      std::to_string(restarts) + "/" + (anneal_more ? "a" : "g") + ":";
+    for (const auto& b : bonds) key += std::to_string(b.first) + "," + std::to_string(b.second) + ";";
+    static std::mutex mu;
+    static std::map<std::string, Plan> cache;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        const auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+    }
+    Plan P = search_plan(N, bonds, T, c, restarts, anneal_more);
+    std::lock_guard<std::mutex> lk(mu);
+    cache.emplace(key, P);
+    return P;
+}
+
+namespace {
+
+Plan search_plan(int N, const std::vector<std::pair<int, int>>& bonds, int T, int c, int restarts, bool anneal_more) {
     Plan P;
     P.N = N;
     if (N <= T) {
@@ -303,8 +336,6 @@ Plan make_plan(int N, const std::vector<std::pair<int, int>>& bonds, int T, int 
     P.T = T; P.c = c;
     std::vector<std::vector<int>> adj(N);
     for (auto& b : bonds) { adj[b.first].push_back(b.second); adj[b.second].push_back(b.first); }
-    if (N >= 26) restarts = std::max(restarts, 20000);   // large bases: fewer passes are worth ~3 s here
-    if (const char* e = std::getenv("ESC_PLAN_RESTARTS")) restarts = std::max(1, std::atoi(e));
     std::mt19937_64 rng(0x5eed1234u);
     Cand best;
     size_t best_cost = ~size_t(0);
@@ -315,8 +346,7 @@ Plan make_plan(int N, const std::vector<std::pair<int, int>>& bonds, int T, int 
         if (cost < best_cost) { best_cost = cost; best = cd; }
     }
     // fewer passes than the greedy covering: annealed coverings with one pass less at a time
-    const char* greedy_only = std::getenv("ESC_PLAN_GREEDY");
-    if (!greedy_only || std::atoi(greedy_only) == 0)
+    if (anneal_more)
         for (int np = (int)best.S.size() - 1; np >= 1; np--) {
             Cand a;
             for (int t = 0; t < 8 && a.S.empty(); t++) a = anneal(N, T, c, np, bonds, adj, rng, 400000);
@@ -340,5 +370,7 @@ Plan make_plan(int N, const std::vector<std::pair<int, int>>& bonds, int T, int 
     }
     return P;
 }
+
+}  // namespace
 
 }  // namespace esc
