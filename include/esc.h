@@ -254,9 +254,10 @@ esc_status esc_two_point(esc_handle* h, int opA, int opB, double* out);
 esc_status esc_measure_local(esc_handle* h, double* s_out, double* je_out);
 
 /* Self-tuning (extension, no reference counterpart): times the complex64 H.v of this Hamiltonian
- * on this device for each plan (tile bits 11/12/13 x first-fit / group-minimising term-to-pass assignment)
- * and each kernel variant (ahead-of-time vs run-time specialised, 2 vs 3 tile buffers) pass by
- * pass, composes the fastest variant of every pass and keeps the fastest composite.
+ * on this device for each plan (tile bits 11/12/13, only 12/13 above 26 sites, x first-fit /
+ * group-minimising term-to-pass assignment) and each kernel variant (ahead-of-time vs run-time
+ * specialised, threads per tile, 2 or 3 tile buffers or staged epilogue loads) pass by pass,
+ * composes the fastest variant of every pass and keeps the fastest composite.
  * All variants compute the same H.v.  Call before esc_lanczos_gs (it may change the internal
  * basis order; ESC_ERR_STATE otherwise).  Uses two complex64 vectors of scratch.  report (may be
  * NULL) receives one line per candidate and the choice.  ESC_AUTOTUNE=1 in the environment runs
