@@ -101,6 +101,7 @@ struct Staged {
 };
 Staged stage(esc_handle* h, const void* in, void* out, int cols, int64_t ld, esc_dtype dt, int flags);
 void unstage(esc_handle* h, const Staged& s, void* out, int cols, int64_t ld, esc_dtype dt, int flags);
+void release_staging(esc_handle* h, size_t keep);
 
 esc::DevModel model_with_field(const esc_handle* h, double bx, double by, double bz);
 std::vector<std::pair<int, int>> bond_pairs(const esc_handle* h);

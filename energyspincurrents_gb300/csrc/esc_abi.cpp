@@ -108,6 +108,15 @@ Staged stage(esc_handle* h, const void* in, void* out, int cols, int64_t ld, esc
     }
     return {in ? A : nullptr, B, n};
 }
+// A staging buffer larger than `keep` bytes (the 6 vectors a pipelined host batch leaves) is
+// released before a solver allocates its own vectors; cudaFree waits for work still using it.
+void release_staging(esc_handle* h, size_t keep) {
+    if (h->d_io && h->io_bytes > keep) {
+        cudaFree(h->d_io);
+        h->d_io = nullptr;
+        h->io_bytes = 0;
+    }
+}
 void unstage(esc_handle* h, const Staged& s, void* out, int cols, int64_t ld, esc_dtype dt, int flags) {
     const size_t es = esize(dt);
     const int64_t n = h->D;
@@ -465,6 +474,7 @@ esc_status esc_lanczos_gs(esc_handle* h, const esc_lanczos_cfg* cfg, const void*
     return guarded(h, [&]() {
         const int64_t D = h->D;
         const esc_dtype dt = cfg->dtype;
+        release_staging(h, 2 * (size_t)D * esize(dt));
         // start vector -> internal order in d_io[0]
         Staged s = stage(h, start, nullptr, 1, D, dt, flags);
         void* d_start = (void*)s.in;
@@ -512,6 +522,7 @@ esc_status esc_spectrum(esc_handle* h, const esc_dyn_cfg* cfg, double* out, int*
         return finish(h, ESC_OK, "");
     }
     return guarded(h, [&]() {
+        release_staging(h, 0);   // the spectra stage nothing through it
         std::vector<double> s;
         int nc = 0;
         // Ritz mode runs in the precision of the ground state and its Krylov basis.  CF mode runs
@@ -655,6 +666,7 @@ extern "C" esc_status esc_cf_batched(esc_handle* h, const esc_cf_batch_cfg* cfg,
         const int nc = cfg->ncols, K = cfg->max_steps;
         const esc_dtype dt = cfg->dtype;
         const size_t es = esize(dt), vb = (size_t)h->D * es;
+        release_staging(h, vb);
         ensure(h->d_cfb, h->cfb_bytes, std::max(h->cfb_bytes, 3 * (size_t)nc * vb));
         char* set1 = (char*)h->d_cfb + (size_t)nc * vb;
         for (int c = 0; c < nc; c++) {
