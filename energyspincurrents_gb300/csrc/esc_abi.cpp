@@ -216,9 +216,16 @@ esc_status esc_create(const esc_params* p, esc_handle** out) {
         h->N = h->L.N;
         h->D = int64_t(1) << h->N;
         int T = 12, c = 3;
-        if (const char* e = std::getenv("ESC_TILE_BITS")) T = std::atoi(e);
+        const char* te = std::getenv("ESC_TILE_BITS");
+        if (te) T = std::atoi(te);
         if (const char* e = std::getenv("ESC_TILE_LOW")) c = std::atoi(e);
-        install_plan(h.get(), esc::make_plan(h->N, bond_pairs(h.get()), T, c, 200), -1, 0);
+        esc::Plan plan = esc::make_plan(h->N, bond_pairs(h.get()), T, c, 200);
+        if (!te && h->N > 26) {
+            // large bases: 8192-state tiles when they need fewer passes (N=32: 4 instead of 5)
+            esc::Plan p13 = esc::make_plan(h->N, bond_pairs(h.get()), 13, c, 200);
+            if (p13.tiles.size() < plan.tiles.size()) plan = p13;
+        }
+        install_plan(h.get(), plan, -1, 0);
         int ndev = 0;
         cudaError_t e = cudaGetDeviceCount(&ndev);
         if (e != cudaSuccess || ndev == 0) {
@@ -621,7 +628,12 @@ extern "C" esc_status esc_plan(const esc_params* p, int tile_bits, int low_bits,
         std::vector<std::pair<int, int>> pairs;
         for (const auto& b : bonds)
             if (b.kx - b.ky != 0.0 || b.kx + b.ky != 0.0) pairs.push_back({b.i, b.j});
-        esc::Plan P = esc::make_plan(L.N, pairs, tile_bits > 0 ? tile_bits : 12, low_bits > 0 ? low_bits : 3, 200);
+        const int c = low_bits > 0 ? low_bits : 3;
+        esc::Plan P = esc::make_plan(L.N, pairs, tile_bits > 0 ? tile_bits : 12, c, 200);
+        if (tile_bits <= 0 && L.N > 26) {   // the default of esc_create
+            esc::Plan p13 = esc::make_plan(L.N, pairs, 13, c, 200);
+            if (p13.tiles.size() < P.tiles.size()) P = p13;
+        }
         std::vector<esc::Bond> rb(bonds);
         for (auto& b : rb) { b.i = P.perm[b.i]; b.j = P.perm[b.j]; }
         const esc::DevModel m = esc::make_dev_model(*p, L, rb, p->Bxx, p->Byy, p->Bzz);

@@ -152,7 +152,8 @@ esc_status esc_params_from_file(const char* path, esc_params* p, char* errbuf, s
 esc_status esc_lattice(const esc_params* p, int* neigh, int* nsites);
 
 /* Site relabelling and pass count of the tiled H.v for the model in `p` with tiles of 2^tile_bits
- * states (0 = default 12) whose lowest low_bits bits are shared (0 = default 3); host only.
+ * states whose lowest low_bits bits are shared (0 = default 3); host only.  tile_bits 0 = the
+ * default of esc_create: 12, or 13 above 26 sites when that needs fewer passes.
  * bit_of_site (N entries, may be NULL), npasses (may be NULL).  No reference counterpart. */
 esc_status esc_plan(const esc_params* p, int tile_bits, int low_bits, int* bit_of_site, int* npasses);
 

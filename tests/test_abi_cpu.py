@@ -174,3 +174,14 @@ def test_planner_annealed_pass_counts(shape, tile, most):
             assert esc.plan(p, tile, 3)[1] == npass + 1
         finally:
             del os.environ["ESC_PLAN_GREEDY"]
+
+
+def test_default_plan_takes_8192_state_tiles_above_26_sites_when_fewer_passes():
+    """Without ESC_TILE_BITS the plan uses 4096-state tiles, or 8192-state tiles above 26 sites when
+    they need fewer passes (N=32: 4 instead of 5; N=28: 3 instead of 4); esc_plan reports the same
+    default as esc_create."""
+    b = -0.02 / 3 ** 0.5
+    for (Lx, Ly), want, t12 in [((3, 8), 3, 3), ((7, 4), 3, 4), ((4, 8), 4, 5)]:
+        p = dict(Lx=Lx, Ly=Ly, Kxx=-1.0, Kyy=-1.0, Kzz=-1.0, Bxx=b, Byy=b, Bzz=b, jheis=0.05)
+        assert esc.plan(p)[1] == want
+        assert esc.plan(p, 12, 3)[1] == t12
