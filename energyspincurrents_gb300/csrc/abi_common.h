@@ -79,6 +79,7 @@ esc_status guarded(esc_handle* h, F&& f) {
 }
 
 size_t esize(esc_dtype dt);
+bool bad_dtype(int dt);   // not ESC_C128 / ESC_C64
 void ensure(void*& p, size_t& cap, size_t need);
 template <typename T>
 void ensure_t(T*& p, size_t& cap, size_t need) {

@@ -37,6 +37,7 @@ esc_status finish(esc_handle* h, esc_status st, const std::string& msg) {
 }
 
 size_t esize(esc_dtype dt) { return dt == ESC_C64 ? 8 : 16; }
+bool bad_dtype(int dt) { return dt != ESC_C128 && dt != ESC_C64; }
 
 void ensure(void*& p, size_t& cap, size_t need) {
     if (need <= cap && p) return;
@@ -112,9 +113,10 @@ Staged stage(esc_handle* h, const void* in, void* out, int cols, int64_t ld, esc
 // released before a solver allocates its own vectors; cudaFree waits for work still using it.
 void release_staging(esc_handle* h, size_t keep) {
     if (h->d_io && h->io_bytes > keep) {
-        cudaFree(h->d_io);
+        const cudaError_t e = cudaFree(h->d_io);
         h->d_io = nullptr;
         h->io_bytes = 0;
+        ESC_CUDA(e);   // a failed free reports its own cause (often a sticky error of earlier work)
     }
 }
 void unstage(esc_handle* h, const Staged& s, void* out, int cols, int64_t ld, esc_dtype dt, int flags) {
@@ -306,6 +308,7 @@ esc_status esc_basis_permutation(const esc_handle* h, int* bit_of_site) {
 esc_status esc_hv(esc_handle* h, const void* in, void* out, esc_dtype dt, int flags) {
     if (!h || !in || !out) return finish(h, ESC_ERR_PARAM, "null argument");
     if (in == out) return finish(h, ESC_ERR_PARAM, "esc_hv: in and out must differ");
+    if (bad_dtype(dt)) return finish(h, ESC_ERR_PARAM, "esc_hv: dt must be ESC_C128 or ESC_C64");
     return guarded(h, [&]() {
         Staged s = stage(h, in, out, 1, h->D, dt, flags);
         const void* dg = diag_for(h, dt);
@@ -392,6 +395,7 @@ esc_status esc_hv_batched(esc_handle* h, const void* in, void* out, int ncols, i
     if (!h || !in || !out) return finish(h, ESC_ERR_PARAM, "null argument");
     if (ncols < 1 || ncols > esc::MAX_COLS) return finish(h, ESC_ERR_PARAM, "ncols must be 1..16");
     if (ld < h->D) return finish(h, ESC_ERR_PARAM, "ld must be >= 2^N");
+    if (bad_dtype(dt)) return finish(h, ESC_ERR_PARAM, "esc_hv_batched: dt must be ESC_C128 or ESC_C64");
     return guarded(h, [&]() {
         esc::DevFields f;
         for (int c = 0; c < esc::MAX_COLS; c++) {
@@ -418,6 +422,7 @@ esc_status esc_hv_batched(esc_handle* h, const void* in, void* out, int ncols, i
 esc_status esc_apply_op(esc_handle* h, int op, int site, const void* in, void* out, esc_dtype dt, int flags) {
     if (!h || !in || !out) return finish(h, ESC_ERR_PARAM, "null argument");
     if (in == out) return finish(h, ESC_ERR_PARAM, "esc_apply_op: in and out must differ");
+    if (bad_dtype(dt)) return finish(h, ESC_ERR_PARAM, "esc_apply_op: dt must be ESC_C128 or ESC_C64");
     return guarded(h, [&]() {
         const esc::DevOp d = esc::make_dev_op(esc::operator_terms(op, site, h->p, h->L), &h->plan.perm);
         Staged s = stage(h, in, out, 1, h->D, dt, flags);
@@ -466,6 +471,7 @@ extern "C" {
 
 esc_status esc_start_vector(esc_handle* h, int kind, int seed, void* out, esc_dtype dt, int flags) {
     if (!h || !out) return finish(h, ESC_ERR_PARAM, "null argument");
+    if (bad_dtype(dt)) return finish(h, ESC_ERR_PARAM, "esc_start_vector: dt must be ESC_C128 or ESC_C64");
     return guarded(h, [&]() {
         Staged s = stage(h, nullptr, out, 1, h->D, dt, flags);
         start_vector_internal(h, kind, seed, s.out, dt);
@@ -478,6 +484,7 @@ esc_status esc_lanczos_gs(esc_handle* h, const esc_lanczos_cfg* cfg, const void*
     if (!h || !cfg) return finish(h, ESC_ERR_PARAM, "null argument");
     if (cfg->steps < 2) return finish(h, ESC_ERR_PARAM, "LanczosSteps must be >= 2");
     if (cfg->lanctype < 0 || cfg->lanctype > 2) return finish(h, ESC_ERR_PARAM, "DynLanczosSolver: Use PsiOrAll==GS or All");
+    if (bad_dtype(cfg->dtype)) return finish(h, ESC_ERR_PARAM, "esc_lanczos_gs: dtype must be ESC_C128 or ESC_C64");
     return guarded(h, [&]() {
         const int64_t D = h->D;
         const esc_dtype dt = cfg->dtype;
@@ -646,6 +653,7 @@ extern "C" esc_status esc_plan(const esc_params* p, int tile_bits, int low_bits,
 extern "C" esc_status esc_rayleigh(esc_handle* h, const void* v, esc_dtype dt, int flags, double* E) {
     if (!h || !E) return finish(h, ESC_ERR_PARAM, "null argument");
     if (!v && !h->have_gs) return finish(h, ESC_ERR_STATE, "no ground state: call esc_lanczos_gs first");
+    if (v && bad_dtype(dt)) return finish(h, ESC_ERR_PARAM, "esc_rayleigh: dt must be ESC_C128 or ESC_C64");
     return guarded(h, [&]() {
         // v == NULL: the handle's ground state, in place (no copy of the vector)
         if (!v) {
@@ -673,6 +681,7 @@ extern "C" esc_status esc_cf_batched(esc_handle* h, const esc_cf_batch_cfg* cfg,
     if (!h || !cfg || !starts) return finish(h, ESC_ERR_PARAM, "null argument");
     if (cfg->ncols < 1 || cfg->ncols > esc::MAX_COLS) return finish(h, ESC_ERR_PARAM, "ncols must be 1..16");
     if (cfg->max_steps < 1) return finish(h, ESC_ERR_PARAM, "max_steps must be >= 1");
+    if (bad_dtype(cfg->dtype)) return finish(h, ESC_ERR_PARAM, "esc_cf_batched: dtype must be ESC_C128 or ESC_C64");
     if (ld < h->D) return finish(h, ESC_ERR_PARAM, "ld must be >= 2^N");
     return guarded(h, [&]() {
         const int nc = cfg->ncols, K = cfg->max_steps;

@@ -11,7 +11,9 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <string>
 
 #include "esc_internal.h"
 #include "hv_pass_device.cuh"
@@ -930,7 +932,43 @@ constexpr int NOALLOC_SCRATCH = 2 * NOALLOC_MAX_TILES      // per-tile (re, im) 
                                 + 8;                       // reduction result
 constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+// Per device: the array's device address and the unique id of the CUDA context it was looked up
+// in.  A context rebuilt after cudaDeviceReset loads the module again, possibly at another
+// address; its new id triggers a fresh lookup.
+struct NoallocSlot {
+    unsigned long long ctx_id = 0;
+    void* ptr = nullptr;
+};
+NoallocSlot g_noalloc_slot[NOALLOC_MAX_DEVICES];
+
+// cuCtxGetCurrent / cuCtxGetId through the runtime (the library links no libcuda)
+typedef int (*PFN_ctx_current)(void**);
+typedef int (*PFN_ctx_id)(void*, unsigned long long*);
+bool current_context_id(unsigned long long& id) {
+    static PFN_ctx_current cur = nullptr;
+    static PFN_ctx_id gid = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+            qa == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+            qb == cudaDriverEntryPointSuccess) {
+            cur = (PFN_ctx_current)a;
+            gid = (PFN_ctx_id)b;
+        }
+        (void)cudaGetLastError();
+    }
+    void* ctx = nullptr;
+    return cur && gid && cur(&ctx) == 0 && ctx && gid(ctx, &id) == 0;
+}
+
+// Plans of the allocation-free path, kept per process (host memory only): a repeated call with the
+// same model does not repeat the covering search.
+std::map<std::string, Plan> g_noalloc_plans;
 }  // namespace
 
 static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH];
@@ -948,20 +986,27 @@ extern "C" esc_status esc_rayleigh_noalloc(const esc_params* p, const void* v, e
             (void)cudaGetLastError();
             return fail(ESC_ERR_CUDA, "no usable CUDA device");
         }
+        if (dt != ESC_C128 && dt != ESC_C64) return fail(ESC_ERR_PARAM, "esc_rayleigh_noalloc: dt must be ESC_C128 or ESC_C64");
         double* scratch = nullptr;
         {
-            // once per device, with that device current: the device address of the static array
+            // set-up once per device (and context), with that device current: the device address of
+            // the static array; host code must not pass the array's host-side name to a kernel
             std::lock_guard<std::mutex> lk(g_noalloc_mu);
-            if (!g_noalloc_ptr[dev]) {
+            unsigned long long id = 0;
+            const bool have_id = current_context_id(id);
+            NoallocSlot& slot = g_noalloc_slot[dev];
+            if (!slot.ptr || !have_id || slot.ctx_id != id) {
                 void* ptr = nullptr;
                 const cudaError_t rc = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
                 if (rc != cudaSuccess || !ptr) {
                     (void)cudaGetLastError();
+                    slot = NoallocSlot{};
                     return fail(ESC_ERR_CUDA, std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(rc));
                 }
-                g_noalloc_ptr[dev] = ptr;
+                slot.ptr = ptr;
+                slot.ctx_id = have_id ? id : 0;
             }
-            scratch = (double*)g_noalloc_ptr[dev];
+            scratch = (double*)slot.ptr;
         }
         Lattice L;
         std::vector<Bond> bonds;
@@ -975,7 +1020,16 @@ extern "C" esc_status esc_rayleigh_noalloc(const esc_params* p, const void* v, e
         std::vector<std::pair<int, int>> pairs;
         for (const auto& b : bonds)
             if (b.kx - b.ky != 0.0 || b.kx + b.ky != 0.0) pairs.push_back({b.i, b.j});
-        const Plan P = make_plan_reference_order(N, pairs, NOALLOC_TILE_BITS, 3, 200);
+        std::string key = std::to_string(N) + ":";
+        for (const auto& pr : pairs) key += std::to_string(pr.first) + "," + std::to_string(pr.second) + ";";
+        Plan P;
+        {
+            std::lock_guard<std::mutex> lk(g_noalloc_mu);
+            auto it = g_noalloc_plans.find(key);
+            if (it == g_noalloc_plans.end())
+                it = g_noalloc_plans.emplace(key, make_plan_reference_order(N, pairs, NOALLOC_TILE_BITS, 3, 200)).first;
+            P = it->second;
+        }
         const DevModel m = make_dev_model(*p, L, bonds, p->Bxx, p->Byy, p->Bzz);
         const std::vector<DevPass> passes = make_passes(P, m);
         double* part = scratch;                                // [2 * tiles]

@@ -212,8 +212,12 @@ esc_status esc_rayleigh(esc_handle* h, const void* v, esc_dtype dt, int flags, d
  *     which loads the library holds until the process exits.  The array holds one partial per
  *     tile of 2^12 states, so at most 25 sites (2^25 states) are accepted; larger models fail with
  *     ESC_ERR_PARAM and a message in esc_last_error(NULL).
- *   - The first call on a device looks up the array's device address there (with that device
- *     current); make that first call before any CUDA stream capture.
+ *   - The first call on a device (and the first after its context was rebuilt, e.g. by
+ *     cudaDeviceReset) looks up the array's device address there, with that device current.
+ *   - Every call synchronises `stream` and reads partial sums back to the host, so it must not be
+ *     called while `stream` (or, in global capture mode, the legacy default stream) is being
+ *     captured into a CUDA graph.
+ *   - dt other than ESC_C128 / ESC_C64 fails with ESC_ERR_PARAM.
  *   - All calls share the one array: calls whose work overlaps on the GPU (other streams, other
  *     host threads, same device) race and may return wrong results.  Every value read back is
  *     written by the same call, so nothing has to be cleared between calls. */

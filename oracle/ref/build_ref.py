@@ -17,7 +17,15 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 OUT = os.path.join(REPO, "oracle", "_ref")
-REF = os.environ.get("ESC_REFERENCE_DIR", "/root/reference")
+# The reference source tree: ESC_REFERENCE_DIR, else the read-only mount of the build container
+# (absent on GPU hosts, which use the prebuilt outputs and never call this recipe).
+DEFAULT_REFERENCE_DIR = "/root/reference"
+
+
+def reference_dir():
+    """Directory holding the reference's main.cpp and src/, or None when it is not present."""
+    d = os.environ.get("ESC_REFERENCE_DIR") or DEFAULT_REFERENCE_DIR
+    return d if os.path.isdir(os.path.join(d, "src")) else None
 
 
 def _openblas():
@@ -29,8 +37,10 @@ def _openblas():
 
 
 def build(force=False):
-    if not os.path.isdir(os.path.join(REF, "src")):
-        raise RuntimeError("reference source tree not present")
+    REF = reference_dir()
+    if REF is None:
+        raise RuntimeError("reference source tree not present: set ESC_REFERENCE_DIR to the directory holding "
+                           "the reference's main.cpp and src/")
     os.makedirs(OUT, exist_ok=True)
     blas = _openblas()
     common = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-w", "-I", os.path.join(HERE, "shim"),

@@ -115,6 +115,11 @@ int main(int argc, char** argv) {
         std::vector<std::complex<double>> loc;
         for (int s = 0; s < N; s++) { loc.push_back(Sxi[s]); loc.push_back(Syi[s]); loc.push_back(Szi[s]); }
         dump("localS.bin", loc.data(), loc.size() * 16);
+        // Observables::measureLocalJe (src/Observables.h:88-104) only prints: its lines (site,
+        // <Je_x>, <Je_y>, total) are captured between markers at precision 17
+        std::cout << "@@LOCALJE_BEGIN" << std::endl;
+        Obs.measureLocalJe(Psi);
+        std::cout << "@@LOCALJE_END" << std::endl;
         // Observables::TwoPointCorr (src/Observables.h:131-158), its commented drivers in main.cpp:118-183
         const char* pairs[][2] = {{"Sz", "Sz"}, {"Sx", "Sy"}, {"Sp", "Sm"}, {"Jsx", "Jsy"}, {"Jex", "Jey"}};
         for (auto& pr : pairs) {

@@ -197,6 +197,21 @@ def project(vecs, D):
 CORR_PAIRS = [("Sz", "Sz"), ("Sx", "Sy"), ("Sp", "Sm"), ("Jsx", "Jsy"), ("Jex", "Jey")]
 
 
+def parse_local_je(log, N):
+    """<Je_x,i>, <Je_y,i> per site from the lines the reference's measureLocalJe prints
+    (src/Observables.h:88-104: 'site \\t (re,im) \\t (re,im) \\t  \\t (re,im)'), N x 2 complex."""
+    seg = log.split("@@LOCALJE_BEGIN")[1].split("@@LOCALJE_END")[0]
+    rows = {}
+    for line in seg.splitlines():
+        vals = re.findall(r"\(([-+0-9.eE]+),([-+0-9.eE]+)\)", line)
+        head = line.strip().split()
+        if len(vals) == 3 and head and head[0].isdigit():
+            rows[int(head[0])] = [complex(float(a), float(b)) for a, b in vals[:2]]
+    if sorted(rows) != list(range(N)):
+        raise RuntimeError("measureLocalJe output incomplete")
+    return np.array([rows[s] for s in range(N)], dtype=np.complex128)
+
+
 def run_case(name, text, full_ops, exe):
     p = parse_params(text)
     N = int(p["NumberofSitesLx"]) * int(p["NumberofSitesLy"])
@@ -245,6 +260,7 @@ def run_case(name, text, full_ops, exe):
                 res[f"full_{k}"] = v
             if p.get("LancType") == "All":
                 res["localS"] = rd("localS.bin", np.complex128).reshape(N, 3)
+                res["localJe"] = parse_local_je(log, N)
                 for a, b in CORR_PAIRS:
                     res[f"corr_{a}_{b}"] = rd(f"corr_{a}_{b}.bin", np.complex128).reshape(N, N)
                 for fn, key in (("JeJe_outSpectrum.real", "JeJe"), ("JsJs_outSpectrum.real", "JsJs"),

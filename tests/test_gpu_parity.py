@@ -104,6 +104,9 @@ def test_measure_local(name, tmp_path):
     s, je = h.measure_local()
     tol = 1e-9 if name != "midinput" else 1e-4       # midinput: 2-fold degenerate |gs> (start-vector dependent)
     assert np.abs(s - g["localS"]).max() < tol
+    # Observables::measureLocalJe (src/Observables.h:88-104): <Je_x,i>, <Je_y,i> as the reference prints them
+    assert je.shape == g["localJe"].shape
+    assert np.abs(je - g["localJe"]).max() < tol
 
 
 S3 = 3 ** 0.5

@@ -96,3 +96,16 @@ def test_two_point_corr(name):
     for a, b in CORR_PAIRS:
         c = m.two_point(a, b, g["psi"])
         np.testing.assert_allclose(c, g[f"corr_{a}_{b}"], rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names() if "localJe" in np.load(f"{GOLDEN}/{n}.npz").files])
+def test_measure_local_je(name):
+    """Observables::measureLocalJe (src/Observables.h:88-104): <gs|Je_x,i|gs>, <gs|Je_y,i|gs> per site,
+    evaluated by the oracle's operators on the reference's own ground state (printed by the reference
+    at 17 digits)."""
+    g, p, m = load(name)
+    if "psi" not in g.files:
+        pytest.skip("ground state not stored for this case")
+    psi = g["psi"]
+    je = np.array([[np.vdot(psi, m.apply(op, s, psi)) for op in ("Jex", "Jey")] for s in range(m.N)])
+    np.testing.assert_allclose(je, g["localJe"], rtol=0, atol=1e-15)

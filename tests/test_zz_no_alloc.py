@@ -55,3 +55,11 @@ def test_noalloc_rejects_too_many_sites():
     dummy = torch.zeros(2, dtype=torch.complex128, device="cuda")
     with pytest.raises(esc.EscError, match="at most 25 sites"):
         noalloc(P, dummy, esc.C128, torch.cuda.current_stream().cuda_stream)
+
+
+def test_noalloc_rejects_bad_dtype():
+    """A dtype value other than complex128 / complex64 is refused before any kernel reads the vector."""
+    P = esc.ConstVariables(**params(2, 4))
+    dummy = torch.zeros(256, dtype=torch.complex64, device="cuda")
+    with pytest.raises(esc.EscError, match="dt must be"):
+        noalloc(P, dummy, 7, torch.cuda.current_stream().cuda_stream)
