@@ -213,6 +213,44 @@ def ground_state_report(esc, sites, steps=200):
             "tuning": tune, "vectors": "complex64, 3 resident + ground state"}
 
 
+def lanczos_step_report(esc, sites, steps=24):
+    """Cost of one ground-state Lanczos step (complex64, no reorthogonalisation: the H.v passes with
+    alpha from the last pass's epilogue, then one update sweep fused with |u|^2) against one H.v,
+    both on the self-tuned passes.  The run is LancType=OnlyEgs, so nothing else is timed."""
+    import numpy as np
+    import torch
+    h = esc.Handle(workload(sites))
+    tune = h.autotune().strip().splitlines()[-1]
+    D = h.D
+    v = torch.empty(D, dtype=torch.complex64, device="cuda")
+    out = torch.empty_like(v)
+    flags = esc.DEVICE_PTR | esc.ASYNC | esc.INTERNAL_ORDER
+    esc.lib().esc_start_vector(h.h, 1, 1, esc.ctypes.c_void_p(v.data_ptr()), esc.C64, flags)
+    stream = torch.cuda.ExternalStream(h.stream())
+    for _ in range(2):
+        h.hv_device(v.data_ptr(), out.data_ptr(), esc.C64, flags)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(5):
+        h.hv_device(v.data_ptr(), out.data_ptr(), esc.C64, flags)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    hv_ms = ev0.elapsed_time(ev1) / 5
+    del v, out
+    torch.cuda.empty_cache()
+    t = []
+    for n in (steps // 2, steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h.lanczos_gs(steps=n, lanctype="OnlyEgs", reortho=0, dtype=np.complex64, want_gs=False)
+        t.append(time.perf_counter() - t0)
+    step_ms = (t[1] - t[0]) / (steps - steps // 2) * 1e3     # set-up and start vector cancel
+    h.close()
+    return {"sites": sites, "hv_ms": round(hv_ms, 3), "lanczos_step_ms": round(step_ms, 3),
+            "step_over_hv": round(step_ms / hv_ms, 3), "tuning": tune}
+
+
 def reduce_max(x, dist, device):
     """Max over the ranks of a per-rank time (the slowest replica sets the job's time)."""
     import torch
@@ -269,6 +307,8 @@ def main():
     ap.add_argument("--gs-report", action="store_true",
                     help="time a mixed-precision ground state of the --sites cluster (Lanczos on complex64 vectors, "
                          "FP64 Rayleigh refinement) and print one JSON line, then exit")
+    ap.add_argument("--step-report", action="store_true",
+                    help="time one complex64 Lanczos step of the --sites cluster against one H.v and print one JSON line")
     ap.add_argument("--autotune-report", action="store_true",
                     help="print the self-tuner's timing of every H.v variant for --sites and exit (no JSON line)")
     args = ap.parse_args()
@@ -290,6 +330,9 @@ def main():
         return
     if args.gs_report:
         print(json.dumps(ground_state_report(esc, args.sites)), flush=True)
+        return
+    if args.step_report:
+        print(json.dumps(lanczos_step_report(esc, args.sites)), flush=True)
         return
     if args.tts_report:
         print(json.dumps(mixed_spectrum_report(esc, args.sites)), flush=True)

@@ -9,6 +9,10 @@
 // iterations (one per rotation), so every kernel parameter is fixed and the iteration counter is
 // read from device memory.
 //
+// One iteration: the tiled H.V passes over all active columns (one launch per pass; the last pass
+// also leaves the partial sums of <cur|H cur> per column, so alpha needs no extra sweep over the
+// vectors), alpha, the update u_{k+1} (fused with its squared norm), beta and the stop test.
+//
 // The Lanczos vectors are kept unnormalised: u_k = beta_k v_k with beta_0 = |phi| and beta_k the
 // usual off-diagonal, so no pass over the vectors only rescales them.  With w = H u_k:
 //   alpha_k   = <u_k|w> / beta_k^2
@@ -72,42 +76,6 @@ __device__ __forceinline__ void stream_loop(long long D, F&& f) {
     for (; i < D; i += stride) f(i, stride, 1);
 }
 
-// alpha partials: blockIdx.y = column; partial (re, im) of <cur|w>
-template <typename R>
-__global__ void __launch_bounds__(BTPB) kb_dot(const typename V2B<R>::T* __restrict__ cur,
-                                               const typename V2B<R>::T* __restrict__ w, long long D,
-                                               const int* __restrict__ active, double* __restrict__ part) {
-    typedef typename V2B<R>::T C;
-    const int c = blockIdx.y;
-    if (!active[c]) return;
-    const C* x = cur + (size_t)c * D;
-    const C* y = w + (size_t)c * D;
-    double re = 0.0, im = 0.0;
-    float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-    stream_loop(D, [&](long long i, long long st, int n) {
-        C a[UNR], b[UNR];
-#pragma unroll
-        for (int u = 0; u < UNR; u++)
-            if (u < n) { a[u] = x[i + u * st]; b[u] = y[i + u * st]; }
-#pragma unroll
-        for (int u = 0; u < UNR; u++) {
-            if (u >= n) break;
-            if constexpr (sizeof(R) == 4) {
-                bff_addprod(rh, rl, a[u].x, b[u].x); bff_addprod(rh, rl, a[u].y, b[u].y);
-                bff_addprod(ih, il, a[u].x, b[u].y); bff_addprod(ih, il, -a[u].y, b[u].x);
-            } else {
-                re += a[u].x * b[u].x + a[u].y * b[u].y;
-                im += a[u].x * b[u].y - a[u].y * b[u].x;
-            }
-        }
-    });
-    if constexpr (sizeof(R) == 4) {
-        re = (double)rh + (double)rl;
-        im = (double)ih + (double)il;
-    }
-    block_sum2(re, im, part + ((size_t)c * gridDim.x + blockIdx.x) * 2);
-}
-
 // alpha_c[it] = (sum of partials) / |u_it|^2 (one block per column)
 __global__ void __launch_bounds__(BTPB) kb_alpha(const double* __restrict__ part, int G, const int* __restrict__ it_p,
                                                  const int* __restrict__ active, double* __restrict__ alpha,
@@ -123,7 +91,7 @@ __global__ void __launch_bounds__(BTPB) kb_alpha(const double* __restrict__ part
     block_sum2(re, im, out);
     if (threadIdx.x == 0) {
         const int it = *it_p;
-        const double nb2 = b2[(size_t)c * (kmax + 1) + it];   // |u_it|^2
+        const double nb2 = b2[(size_t)c * (kmax + 1) + it];   // |u_it|^2 (> 0 while the column is active)
         alpha[((size_t)c * kmax + it) * 2] = out[0] / nb2;
         alpha[((size_t)c * kmax + it) * 2 + 1] = out[1] / nb2;
     }
@@ -233,6 +201,51 @@ __global__ void __launch_bounds__(BTPB) kb_norm0_final(const double* __restrict_
     }
 }
 
+// Helpers for the ground-state Lanczos on this recurrence (one column; iteration counter on the
+// device, so they can sit inside the captured iterations):
+// L[it + 1] = w  (Krylov basis kept for Ritz-mode spectra)
+template <typename R>
+__global__ void __launch_bounds__(BTPB) kb_store(const typename V2B<R>::T* __restrict__ w, typename V2B<R>::T* __restrict__ L,
+                                                 long long D, const int* __restrict__ it_p, const int* __restrict__ active) {
+    if (!active[0]) return;
+    typename V2B<R>::T* dst = L + (size_t)(*it_p + 1) * D;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) dst[i] = w[i];
+}
+// gs += zc[it + 1] w  (ground state rebuilt from the regenerated vectors)
+template <typename R>
+__global__ void __launch_bounds__(BTPB) kb_accum(const typename V2B<R>::T* __restrict__ w, typename V2B<R>::T* __restrict__ gs,
+                                                 long long D, const int* __restrict__ it_p, const double* __restrict__ zc,
+                                                 const int* __restrict__ active) {
+    if (!active[0]) return;
+    const R z = (R)zc[*it_p + 1];
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) {
+        typename V2B<R>::T a = gs[i];
+        const typename V2B<R>::T b = w[i];
+        a.x = fma(z, b.x, a.x);
+        a.y = fma(z, b.y, a.y);
+        gs[i] = a;
+    }
+}
+template <typename R>
+void launch_store_iter(const void* w, void* L, int64_t D, const int* d_it, const int* d_active, cudaStream_t s) {
+    typedef typename V2B<R>::T C;
+    kb_store<R><<<BGRID, BTPB, 0, s>>>((const C*)w, (C*)L, D, d_it, d_active);
+    ESC_CUDA(cudaGetLastError());
+}
+template <typename R>
+void launch_accum_iter(const void* w, void* gs, int64_t D, const int* d_it, const double* zc, const int* d_active,
+                       cudaStream_t s) {
+    typedef typename V2B<R>::T C;
+    kb_accum<R><<<BGRID, BTPB, 0, s>>>((const C*)w, (C*)gs, D, d_it, zc, d_active);
+    ESC_CUDA(cudaGetLastError());
+}
+template void launch_store_iter<float>(const void*, void*, int64_t, const int*, const int*, cudaStream_t);
+template void launch_store_iter<double>(const void*, void*, int64_t, const int*, const int*, cudaStream_t);
+template void launch_accum_iter<float>(const void*, void*, int64_t, const int*, const double*, const int*, cudaStream_t);
+template void launch_accum_iter<double>(const void*, void*, int64_t, const int*, const double*, const int*, cudaStream_t);
+
 template <typename R>
 void CFBatch<R>::run(cudaStream_t s) {
     typedef typename V2B<R>::T C;
@@ -253,10 +266,10 @@ void CFBatch<R>::run(cudaStream_t s) {
         C* prev = V[r % 3];
         C* cur = V[(r + 1) % 3];
         C* w = V[(r + 2) % 3];
-        for (int c = 0; c < ncols; c++) hv_column(c, cur + (size_t)c * D, w + (size_t)c * D, d_active + c, s);
-        kb_dot<R><<<gcol, BTPB, 0, s>>>(cur, w, D, d_active, d_part);
-        kb_alpha<<<ncols, BTPB, 0, s>>>(d_part, BGRID, d_it, d_active, d_alpha, d_b2, kmax);
+        const int G = hv_all(cur, w, d_active, d_part, s);   // w = H cur; alpha partials per column
+        kb_alpha<<<ncols, BTPB, 0, s>>>(d_part, G, d_it, d_active, d_alpha, d_b2, kmax);
         kb_update<R><<<gcol, BTPB, 0, s>>>(w, cur, prev, D, d_it, d_active, d_alpha, d_b2, kmax, d_part);
+        if (after_update) after_update(w, s);
         kb_beta<<<ncols, BTPB, 0, s>>>(d_part, BGRID, d_it, d_active, d_b2, kmax, d_steps, tol);
         kb_advance<<<1, 1, 0, s>>>(d_it, d_active, ncols);
         ESC_CUDA(cudaGetLastError());

@@ -412,9 +412,16 @@ esc_status esc_hv_batched(esc_handle* h, const void* in, void* out, int ncols, i
                                   : hv_host_pipelined<double>(h, (const char*)in, (char*)out, ncols, ld, fields, dt, internal);
             if (done) return;
         }
+        // device pointers (or a host batch that did not fit the pipeline): the tiled passes over
+        // all columns at once (tile offsets and term groups decoded once per tile for every column)
         Staged s = stage(h, in, out, ncols, ld, dt, flags);
-        if (dt == ESC_C64) esc::launch_hv_batched<float>(h->dm, f, s.in, s.out, ncols, s.ld, h->D, h->stream);
-        else esc::launch_hv_batched<double>(h->dm, f, s.in, s.out, ncols, s.ld, h->D, h->stream);
+        esc::DevCols cols = esc::single_column(h->dm);
+        cols.ncols = ncols;
+        cols.ld = s.ld;
+        cols.f = f;
+        const void* dg = diag_for(h, dt);
+        if (dt == ESC_C64) esc::launch_hv_cols<float>(h->dm, cols, h->passes, s.in, s.out, h->D, dg, h->stream, nullptr);
+        else esc::launch_hv_cols<double>(h->dm, cols, h->passes, s.in, s.out, h->D, dg, h->stream, nullptr);
         unstage(h, s, out, ncols, ld, dt, flags);
     });
 }

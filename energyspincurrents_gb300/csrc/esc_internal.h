@@ -60,6 +60,18 @@ struct DevFields {
     double fx[MAX_COLS], fy[MAX_COLS], fz[MAX_COLS];
     float fxf[MAX_COLS], fyf[MAX_COLS], fzf[MAX_COLS];
 };
+// Columns of one tiled H.V launch sequence: column c reads in + c ld and writes out + c ld with the
+// field f[c]; dotp (may be NULL) receives the alpha partials sum conj(in) out of every column from
+// the last pass, (re, im) at dotp[(c * G + b) * 2] for b < G (G returned by the launcher).
+struct DevCols {
+    long long ld = 0;
+    int ncols = 1;
+    int pad = 0;
+    DevFields f{};
+    double* dotp = nullptr;
+};
+DevCols single_column(const DevModel& m);
+DevCols with_field(DevCols c, int col, double bx, double by, double bz);   // Bx/2 ... from full fields
 
 // Operator = sum of terms; term t = coef * f_{n-1} ... f_0 (f_0 applied first), each factor a
 // single-site S^x/S^y/S^z.  Gather form: out[k] += coef * phi_t(k0) * in[k0], k0 = k ^ flip.
@@ -147,9 +159,10 @@ bool jit_compile(std::vector<DevPass>& passes, std::string& err);
 // The CUDA source jit_compile hands to NVRTC; which (optional) receives the pass index of each
 // kernel esc_jit_pass<k>.
 std::string jit_source(const std::vector<DevPass>& passes, std::vector<int>* which);
-void jit_launch(const DevPass& p, const escdev::PassTab& pt, const void* diag, const void* in, void* out, int64_t D,
-                int sms, cudaStream_t s, const int* active);
-escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m);
+// Launches the specialised kernel of pass p; returns its grid size.
+int jit_launch(const DevPass& p, const escdev::PassTab& pt, const void* diag, const void* in, void* out, int64_t D,
+               int sms, cudaStream_t s, const int* active);
+escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m, const DevCols* cols = nullptr, double* dotp = nullptr);
 // Default tile buffers per CTA of the complex64 passes (2; ESC_STAGES=3 for three).
 int pass_stages();
 // diag: precomputed diagonal of the bond terms (no field), R per state (launch_diag); may be NULL,
@@ -158,6 +171,11 @@ int pass_stages();
 template <typename R> void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in,
                                            void* out, int64_t D, const void* diag, cudaStream_t s,
                                            const int* active = nullptr);
+// Multi-column form: all active columns (device flags active[c], may be NULL) in one launch per
+// pass; returns the number G of alpha partials per column written to cols.dotp (0 without dotp).
+template <typename R> int launch_hv_cols(const DevModel& m, const DevCols& cols, const std::vector<DevPass>& passes,
+                                         const void* in, void* out, int64_t D, const void* diag, cudaStream_t s,
+                                         const int* active);
 template <typename R> void launch_diag(const DevModel& m, void* diag, int64_t D, cudaStream_t s);
 // host_sum = <v|H|v> (re, im) computed in FP64 pass by pass; S = storage precision of v.
 template <typename S> void launch_energy(const DevModel& m, const std::vector<DevPass>& passes, const void* in,
@@ -193,8 +211,6 @@ int red_blocks(int64_t n);
 constexpr int RED_MAX_BLOCKS = 1216;   // 8 x 152 SMs
 
 template <typename R> void launch_hv(const DevModel& m, const void* in, void* out, int64_t D, cudaStream_t s);
-template <typename R> void launch_hv_batched(const DevModel& m, const DevFields& f, const void* in, void* out,
-                                             int ncols, int64_t ld, int64_t D, cudaStream_t s);
 template <typename R> void launch_apply(const DevOp& op, const void* in, void* out, int64_t D, cudaStream_t s);
 
 // dst (double2) = sum conj(a) b
@@ -244,10 +260,21 @@ struct CFBatch {
     // start_it > 0 continues a recurrence at iteration start_it: prev = set start_it % 3, cur =
     // set (start_it + 1) % 3, alpha / b2 filled below start_it, active flags set by the caller
     int start_it = 0;
-    std::function<void(int, const void*, void*, const int*, cudaStream_t)> hv_column;
+    // w = H cur for every active column; writes the alpha partials sum conj(cur) w of column c at
+    // part[(c * G + b) * 2] and returns G (launch_hv_cols)
+    std::function<int(const void* cur, void* w, const int* active, double* part, cudaStream_t)> hv_all;
+    // optional, run (and captured) after the update of every iteration: w holds u_{it+1} of every
+    // column, the iteration counter is at d_it
+    std::function<void(const void* w, cudaStream_t)> after_update;
     void run(cudaStream_t s);
 };
 constexpr int CFB_GRID = 1216;   // blocks per column of the batched CF kernels (8 x 152 SMs)
+// One-column helpers for the ground-state Lanczos on the CFBatch recurrence (device iteration
+// counter d_it, column flag d_active[0]): L[it+1] = w, and gs += zc[it+1] w.
+template <typename R> void launch_store_iter(const void* w, void* L, int64_t D, const int* d_it, const int* d_active,
+                                             cudaStream_t s);
+template <typename R> void launch_accum_iter(const void* w, void* gs, int64_t D, const int* d_it, const double* zc,
+                                             const int* d_active, cudaStream_t s);
 
 // ---------------------------------------------------------------------------------------------
 // Host numerics

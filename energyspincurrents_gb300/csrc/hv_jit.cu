@@ -226,8 +226,8 @@ bool jit_compile(std::vector<DevPass>& passes, std::string& err) {
     return true;
 }
 
-void jit_launch(const DevPass& p, const escdev::PassTab& pt, const void* diag, const void* in, void* out, int64_t D,
-                int sms, cudaStream_t s, const int* active) {
+int jit_launch(const DevPass& p, const escdev::PassTab& pt, const void* diag, const void* in, void* out, int64_t D,
+               int sms, cudaStream_t s, const int* active) {
     JitEntry e;
     {
         std::lock_guard<std::mutex> lk(g_mu);
@@ -236,7 +236,7 @@ void jit_launch(const DevPass& p, const escdev::PassTab& pt, const void* diag, c
     }
     const long long ntiles = (long long)(D >> p.Tp);
     const long long g = std::min<long long>(ntiles, (long long)sms * std::max(e.per_sm, 1));
-    if (g <= 0) return;
+    if (g <= 0) return 0;
     escdev::PassTab tab = pt;
     const float* dg = (const float*)diag;
     const float2* vin = (const float2*)in;
@@ -248,6 +248,7 @@ void jit_launch(const DevPass& p, const escdev::PassTab& pt, const void* diag, c
     if (!drv(driver().launchKernel(e.fn, (unsigned)g, 1, 1, (unsigned)e.TB, 1, 1, (unsigned)e.smem, (CUstream)s, args, nullptr),
              "cuLaunchKernel", err))
         throw CudaError(err);
+    return (int)g;
 }
 
 }  // namespace esc

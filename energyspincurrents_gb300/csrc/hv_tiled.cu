@@ -135,92 +135,159 @@ __global__ void __launch_bounds__(256) k_diag(const __grid_constant__ DevModel m
 // tile-local index splits into thread bits (< 9) and j bits (>= 9).  Term parameters are read once
 // per thread per term; the parity of a term's mask over the j bits is a host-precomputed bit mask
 // (bjpar / fjbit), the thread-bit part one POPC.  Diagonal read from the precomputed vector.
+// Columns: per tile, every active column of `cols` (own vectors at in + c ld, own field); with
+// cols.dotp, the alpha partials sum conj(in) out per column and CTA (accumulated in double).
 template <typename R, int E>
 __global__ void __launch_bounds__(TILE_THREADS) k_hv_pass_fast(const __grid_constant__ DevModel m,
                                                                 const __grid_constant__ DevPass p,
+                                                                const __grid_constant__ DevCols cols,
                                                                 const R* __restrict__ diag,
                                                                 const typename V2T<R>::T* __restrict__ in,
                                                                 typename V2T<R>::T* __restrict__ out,
                                                                 long long ntiles, const int* __restrict__ active) {
     typedef typename V2T<R>::T C;
-    if (active && *active == 0) return;
+    unsigned cmask = 0;
+    for (int c = 0; c < cols.ncols; c++)
+        if (!active || active[c]) cmask |= 1u << c;
+    if (!cmask) return;
     constexpr bool F32 = sizeof(R) == 4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* tile = reinterpret_cast<C*>(smem_raw);
     __shared__ unsigned long long hi_off[E];
+    __shared__ double dsm[MAX_COLS][TILE_THREADS / 32][2];
     const int tid = threadIdx.x;
     if (tid < E) hi_off[tid] = p.tabHi[tid];
+    if (cols.dotp)
+        for (int i = tid; i < MAX_COLS * (TILE_THREADS / 32) * 2; i += TILE_THREADS) (&dsm[0][0][0])[i] = 0.0;
     const unsigned long long lo = p.tabLo[tid >> 3] | (unsigned long long)(tid & 7);
-    const R fx = F32 ? (R)m.fxf : (R)m.fx, fy = F32 ? (R)m.fyf : (R)m.fy;
-    const R fz = F32 ? (R)m.fzf : (R)m.fz;
     __syncthreads();
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
         unsigned long long base = lo;
         for (int q = 0; q < p.nrest; q++) base |= (((unsigned long long)t >> q) & 1ull) << p.rest[q];
+        for (unsigned cm = cmask; cm; cm &= cm - 1) {
+            const int c = __ffs((int)cm) - 1;
+            const C* inc = in + c * cols.ld;
+            C* outc = out + c * cols.ld;
+            const R fx = F32 ? (R)cols.f.fxf[c] : (R)cols.f.fx[c], fy = F32 ? (R)cols.f.fyf[c] : (R)cols.f.fy[c];
+            const R fz = F32 ? (R)cols.f.fzf[c] : (R)cols.f.fz[c];
 #pragma unroll
-        for (int j = 0; j < E; j++) tile[tid + TILE_THREADS * j] = in[base | hi_off[j]];
+            for (int j = 0; j < E; j++) tile[tid + TILE_THREADS * j] = inc[base | hi_off[j]];
+            __syncthreads();
+            R ar[E], ai[E];
+            if (p.diag) {
+#pragma unroll
+                for (int j = 0; j < E; j++) {
+                    const unsigned long long k = base | hi_off[j];
+                    const R d = diag[k];
+                    const R nz = (R)(m.N - 2 * __popcll(k));
+                    R dg;
+                    if constexpr (F32) dg = fmaf(fz, nz, d);
+                    else dg = __dadd_rn(d, __dmul_rn(fz, nz));    // HDiag += Bzz*SzT (src/Hamiltonian.h:374)
+                    const C v = tile[tid + TILE_THREADS * j];
+                    ar[j] = dg * v.x;
+                    ai[j] = dg * v.y;
+                }
+            } else if (p.accumulate) {
+#pragma unroll
+                for (int j = 0; j < E; j++) {
+                    const C o = outc[base | hi_off[j]];
+                    ar[j] = o.x;
+                    ai[j] = o.y;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < E; j++) ar[j] = ai[j] = (R)0;
+            }
+            for (int b = 0; b < p.nbond; b++) {
+                const unsigned int lm = p.blm[b];
+                const unsigned int jp = p.bjpar[b];
+                const unsigned int pb = __popc((unsigned)tid & lm) & 1u;
+                R c0, c1;
+                if constexpr (F32) { c0 = p.ceqf[b]; c1 = p.cdifff[b]; }
+                else { c0 = p.ceq[b]; c1 = p.cdiff[b]; }
+#pragma unroll
+                for (int j = 0; j < E; j++) {
+                    const R cc = (pb ^ ((jp >> j) & 1u)) ? c1 : c0;
+                    const C w = tile[(tid + TILE_THREADS * j) ^ lm];
+                    ar[j] = fma(cc, w.x, ar[j]);
+                    ai[j] = fma(cc, w.y, ai[j]);
+                }
+            }
+            for (int f = 0; f < p.nfield; f++) {
+                const unsigned int lm = p.flm[f];
+                const unsigned int jb = p.fjbit[f];
+                const bool tb = ((unsigned)tid & lm) != 0u;
+#pragma unroll
+                for (int j = 0; j < E; j++) {
+                    // (Bx/2 + i By/2 (bit ? +1 : -1)) v[k ^ 2^s]
+                    const R sfy = (tb || ((jb >> j) & 1u)) ? fy : -fy;
+                    const C w = tile[(tid + TILE_THREADS * j) ^ lm];
+                    ar[j] = fma(fx, w.x, ar[j]); ar[j] = fma(-sfy, w.y, ar[j]);
+                    ai[j] = fma(fx, w.y, ai[j]); ai[j] = fma(sfy, w.x, ai[j]);
+                }
+            }
+            double dre = 0.0, dim = 0.0;
+#pragma unroll
+            for (int j = 0; j < E; j++) {
+                C o;
+                o.x = ar[j];
+                o.y = ai[j];
+                outc[base | hi_off[j]] = o;
+                if (cols.dotp) {
+                    const C v = tile[tid + TILE_THREADS * j];
+                    dre += (double)v.x * (double)o.x + (double)v.y * (double)o.y;
+                    dim += (double)v.x * (double)o.y - (double)v.y * (double)o.x;
+                }
+            }
+            if (cols.dotp) {
+                for (int o = 16; o > 0; o >>= 1) {
+                    dre += __shfl_xor_sync(0xffffffffu, dre, o);
+                    dim += __shfl_xor_sync(0xffffffffu, dim, o);
+                }
+                if ((tid & 31) == 0) { dsm[c][tid >> 5][0] += dre; dsm[c][tid >> 5][1] += dim; }
+            }
+            __syncthreads();
+        }
+    }
+    if (cols.dotp) {
         __syncthreads();
-        R ar[E], ai[E];
-        if (p.diag) {
-#pragma unroll
-            for (int j = 0; j < E; j++) {
-                const unsigned long long k = base | hi_off[j];
-                const R d = diag[k];
-                const R nz = (R)(m.N - 2 * __popcll(k));
-                R dg;
-                if constexpr (F32) dg = fmaf(fz, nz, d);
-                else dg = __dadd_rn(d, __dmul_rn(fz, nz));    // HDiag += Bzz*SzT (src/Hamiltonian.h:374)
-                const C v = tile[tid + TILE_THREADS * j];
-                ar[j] = dg * v.x;
-                ai[j] = dg * v.y;
-            }
-        } else if (p.accumulate) {
-#pragma unroll
-            for (int j = 0; j < E; j++) {
-                const C o = out[base | hi_off[j]];
-                ar[j] = o.x;
-                ai[j] = o.y;
-            }
-        } else {
-#pragma unroll
-            for (int j = 0; j < E; j++) ar[j] = ai[j] = (R)0;
+        if (tid < MAX_COLS && ((cmask >> tid) & 1u)) {
+            double re = 0.0, im = 0.0;
+            for (int w = 0; w < TILE_THREADS / 32; w++) { re += dsm[tid][w][0]; im += dsm[tid][w][1]; }
+            cols.dotp[((size_t)tid * gridDim.x + blockIdx.x) * 2] = re;
+            cols.dotp[((size_t)tid * gridDim.x + blockIdx.x) * 2 + 1] = im;
         }
-        for (int b = 0; b < p.nbond; b++) {
-            const unsigned int lm = p.blm[b];
-            const unsigned int jp = p.bjpar[b];
-            const unsigned int pb = __popc((unsigned)tid & lm) & 1u;
-            R c0, c1;
-            if constexpr (F32) { c0 = p.ceqf[b]; c1 = p.cdifff[b]; }
-            else { c0 = p.ceq[b]; c1 = p.cdiff[b]; }
-#pragma unroll
-            for (int j = 0; j < E; j++) {
-                const R c = (pb ^ ((jp >> j) & 1u)) ? c1 : c0;
-                const C w = tile[(tid + TILE_THREADS * j) ^ lm];
-                ar[j] = fma(c, w.x, ar[j]);
-                ai[j] = fma(c, w.y, ai[j]);
-            }
-        }
-        for (int f = 0; f < p.nfield; f++) {
-            const unsigned int lm = p.flm[f];
-            const unsigned int jb = p.fjbit[f];
-            const bool tb = ((unsigned)tid & lm) != 0u;
-#pragma unroll
-            for (int j = 0; j < E; j++) {
-                // (Bx/2 + i By/2 (bit ? +1 : -1)) v[k ^ 2^s]
-                const R sfy = (tb || ((jb >> j) & 1u)) ? fy : -fy;
-                const C w = tile[(tid + TILE_THREADS * j) ^ lm];
-                ar[j] = fma(fx, w.x, ar[j]); ar[j] = fma(-sfy, w.y, ar[j]);
-                ai[j] = fma(fx, w.y, ai[j]); ai[j] = fma(sfy, w.x, ai[j]);
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < E; j++) {
-            C o;
-            o.x = ar[j];
-            o.y = ai[j];
-            out[base | hi_off[j]] = o;
-        }
-        __syncthreads();
+    }
+}
+
+// Alpha partials of launches without an epilogue of their own: sum conj(in) out per column over a
+// fixed grid of DOT_GRID blocks (layout of DevCols::dotp).
+constexpr int DOT_GRID = 608;
+template <typename R>
+__global__ void __launch_bounds__(256) k_dot_cols(const typename V2T<R>::T* __restrict__ in,
+                                                  const typename V2T<R>::T* __restrict__ out, long long ld, long long D,
+                                                  const int* __restrict__ active, double* __restrict__ dotp) {
+    const int c = blockIdx.y;
+    if (active && !active[c]) return;
+    double re = 0.0, im = 0.0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += stride) {
+        const typename V2T<R>::T v = in[c * ld + i], o = out[c * ld + i];
+        re += (double)v.x * (double)o.x + (double)v.y * (double)o.y;
+        im += (double)v.x * (double)o.y - (double)v.y * (double)o.x;
+    }
+    __shared__ double sm[2][8];
+    for (int o = 16; o > 0; o >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, o);
+        im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    if ((threadIdx.x & 31) == 0) { sm[0][threadIdx.x >> 5] = re; sm[1][threadIdx.x >> 5] = im; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < 8; w++) { a += sm[0][w]; b += sm[1][w]; }
+        dotp[((size_t)c * gridDim.x + blockIdx.x) * 2] = a;
+        dotp[((size_t)c * gridDim.x + blockIdx.x) * 2 + 1] = b;
     }
 }
 
@@ -442,7 +509,7 @@ __global__ void __launch_bounds__(TB, TB * E >= 8192 ? 1 : 2) k_hv_pass_f32g(con
     escdev::pass_body<E, NS, RuntimeTerms<E, TB>, TB>(pt, RuntimeTerms<E, TB>{p}, diag, in, out, ntiles, active);
 }
 
-escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m) {
+escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m, const DevCols* cols, double* dotp) {
     escdev::PassTab t;
     std::memset(&t, 0, sizeof(t));
     std::memcpy(t.tabLo, p.tabLo, sizeof(t.tabLo));
@@ -454,10 +521,36 @@ escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m) {
     t.diag = p.diag;
     t.accumulate = p.accumulate;
     t.N = m.N;
-    t.fx = m.fxf;
-    t.fy = m.fyf;
-    t.fz = m.fzf;
+    if (cols) {
+        t.ld = cols->ld;
+        t.ncols = cols->ncols;
+        for (int c = 0; c < cols->ncols; c++) {
+            t.fx[c] = cols->f.fxf[c];
+            t.fy[c] = cols->f.fyf[c];
+            t.fz[c] = cols->f.fzf[c];
+        }
+    } else {
+        t.ncols = 1;
+        t.fx[0] = m.fxf;
+        t.fy[0] = m.fyf;
+        t.fz[0] = m.fzf;
+    }
+    t.dotp = dotp;
     return t;
+}
+
+DevCols single_column(const DevModel& m) {
+    DevCols c;
+    c.ncols = 1;
+    c.f.fx[0] = m.fx; c.f.fy[0] = m.fy; c.f.fz[0] = m.fz;
+    c.f.fxf[0] = m.fxf; c.f.fyf[0] = m.fyf; c.f.fzf[0] = m.fzf;
+    return c;
+}
+
+DevCols with_field(DevCols c, int col, double bx, double by, double bz) {
+    c.f.fx[col] = 0.5 * bx; c.f.fy[col] = 0.5 * by; c.f.fz[col] = 0.5 * bz;
+    c.f.fxf[col] = (float)c.f.fx[col]; c.f.fyf[col] = (float)c.f.fy[col]; c.f.fzf[col] = (float)c.f.fz[col];
+    return c;
 }
 
 // FP64 energy sweep: sum over one pass of conj(v[k]) (H_pass v)[k], computed in FP64 from a
@@ -783,8 +876,8 @@ void launch_diag(const DevModel& m, void* diag, int64_t D, cudaStream_t s) {
 }
 
 template <typename R, int E>
-static void run_fast(const DevModel& m, const DevPass& p, const void* diag, const void* in, void* out, int64_t D,
-                     int sms, cudaStream_t s, const int* active) {
+static int run_fast(const DevModel& m, const DevPass& p, const DevCols& cols, const void* diag, const void* in, void* out,
+                    int64_t D, int sms, cudaStream_t s, const int* active) {
     typedef typename V2T<R>::T C;
     const size_t smem = (size_t)TILE_THREADS * E * sizeof(C);
     if (smem > 48 * 1024)
@@ -793,9 +886,10 @@ static void run_fast(const DevModel& m, const DevPass& p, const void* diag, cons
     ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass_fast<R, E>, TILE_THREADS, smem));
     const long long ntiles = (long long)(D >> p.Tp);
     const long long g = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
-    k_hv_pass_fast<R, E><<<(unsigned)g, TILE_THREADS, smem, s>>>(m, p, (const R*)diag, (const C*)in, (C*)out, ntiles,
-                                                                 active);
+    k_hv_pass_fast<R, E><<<(unsigned)g, TILE_THREADS, smem, s>>>(m, p, cols, (const R*)diag, (const C*)in, (C*)out,
+                                                                 ntiles, active);
     ESC_CUDA(cudaGetLastError());
+    return (int)g;
 }
 
 template <int E>
@@ -814,8 +908,8 @@ static void run_f32(const DevModel& m, const DevPass& p, const void* diag, const
 }
 
 template <int E, int NS, int TB = TILE_THREADS>
-static void run_f32g(const DevModel& m, const DevPass& p, const void* diag, const void* in, void* out, int64_t D, int sms,
-                     cudaStream_t s, const int* active) {
+static int run_f32g(const escdev::PassTab& pt, const DevPass& p, const void* diag, const void* in, void* out, int64_t D,
+                    int sms, cudaStream_t s, const int* active) {
     // NS-stage ring of tiles (NS = 4: 2 tiles + staging of the epilogue loads)
     const size_t smem = (size_t)(NS == 4 ? 3 : NS) * TB * E * sizeof(float2);
     // always raised: dynamic + static shared memory may pass 48 KB even when the ring alone does not
@@ -824,9 +918,10 @@ static void run_f32g(const DevModel& m, const DevPass& p, const void* diag, cons
     ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass_f32g<E, NS, TB>, TB, smem));
     const long long ntiles = (long long)(D >> p.Tp);
     const long long g = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
-    k_hv_pass_f32g<E, NS, TB><<<(unsigned)g, TB, smem, s>>>(make_pass_tab(p, m), p, (const float*)diag,
-                                                            (const float2*)in, (float2*)out, ntiles, active);
+    k_hv_pass_f32g<E, NS, TB><<<(unsigned)g, TB, smem, s>>>(pt, p, (const float*)diag, (const float2*)in, (float2*)out,
+                                                            ntiles, active);
     ESC_CUDA(cudaGetLastError());
+    return (int)g;
 }
 
 int pass_stages() {
@@ -835,76 +930,116 @@ int pass_stages() {
     return x >= 2 && x <= 4 ? x : 2;
 }
 
+// Grouped complex64 pass (ahead of time): E = 2^(Tp - tb_bits) states per thread; returns the grid,
+// or 0 when no instance fits the pass's shape.
+static int run_grouped(const escdev::PassTab& pt, const DevPass& p, const void* diag, const void* in, void* out, int64_t D,
+                       int sms, cudaStream_t s, const int* active) {
+    if (!(p.c == 3 && ((p.Tp == 11 || p.Tp == 12) ? p.tb_bits >= 7 && p.tb_bits <= 9 : p.Tp == 13 && p.tb_bits == 9)))
+        return 0;
+    switch ((p.tb_bits == 8 ? 100 : p.tb_bits == 7 ? 200 : 0) + (p.Tp == 11 ? 10 : p.Tp == 12 ? 20 : 30) + p.stages) {
+        case 32: return run_f32g<16, 2, 512>(pt, p, diag, in, out, D, sms, s, active);
+        case 33: return run_f32g<16, 3, 512>(pt, p, diag, in, out, D, sms, s, active);
+        case 34: return run_f32g<16, 4, 512>(pt, p, diag, in, out, D, sms, s, active);
+        case 212: return run_f32g<16, 2, 128>(pt, p, diag, in, out, D, sms, s, active);
+        case 213: return run_f32g<16, 3, 128>(pt, p, diag, in, out, D, sms, s, active);
+        case 214: return run_f32g<16, 4, 128>(pt, p, diag, in, out, D, sms, s, active);
+        case 222: return run_f32g<32, 2, 128>(pt, p, diag, in, out, D, sms, s, active);
+        case 223: return run_f32g<32, 3, 128>(pt, p, diag, in, out, D, sms, s, active);
+        case 224: return run_f32g<32, 4, 128>(pt, p, diag, in, out, D, sms, s, active);
+        case 12: return run_f32g<4, 2>(pt, p, diag, in, out, D, sms, s, active);
+        case 13: return run_f32g<4, 3>(pt, p, diag, in, out, D, sms, s, active);
+        case 14: return run_f32g<4, 4>(pt, p, diag, in, out, D, sms, s, active);
+        case 23: return run_f32g<8, 3>(pt, p, diag, in, out, D, sms, s, active);
+        case 24: return run_f32g<8, 4>(pt, p, diag, in, out, D, sms, s, active);
+        case 112: return run_f32g<8, 2, 256>(pt, p, diag, in, out, D, sms, s, active);
+        case 113: return run_f32g<8, 3, 256>(pt, p, diag, in, out, D, sms, s, active);
+        case 114: return run_f32g<8, 4, 256>(pt, p, diag, in, out, D, sms, s, active);
+        case 122: return run_f32g<16, 2, 256>(pt, p, diag, in, out, D, sms, s, active);
+        case 123: return run_f32g<16, 3, 256>(pt, p, diag, in, out, D, sms, s, active);
+        case 124: return run_f32g<16, 4, 256>(pt, p, diag, in, out, D, sms, s, active);
+        default: return run_f32g<8, 2>(pt, p, diag, in, out, D, sms, s, active);
+    }
+}
+
 template <typename R>
-void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in, void* out, int64_t D,
-                     const void* diag, cudaStream_t s, const int* active) {
+int launch_hv_cols(const DevModel& m, const DevCols& cols, const std::vector<DevPass>& passes, const void* in, void* out,
+                   int64_t D, const void* diag, cudaStream_t s, const int* active) {
     typedef typename V2T<R>::T C;
     int dev = 0, sms = 0;
     ESC_CUDA(cudaGetDevice(&dev));
     ESC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    for (const DevPass& p : passes) {
+    if (cols.ncols < 1 || cols.ncols > MAX_COLS) throw std::invalid_argument("1..16 columns per H.V launch");
+    int G = 0;
+    for (size_t pi = 0; pi < passes.size(); pi++) {
+        const DevPass& p = passes[pi];
+        double* dotp = pi + 1 == passes.size() ? cols.dotp : nullptr;
+        int g = 0;   // grid of a launch that handled every column (and the alpha epilogue)
         if constexpr (sizeof(R) == 4) {
-            if (diag && p.jit >= 0) {
-                jit_launch(p, make_pass_tab(p, m), diag, in, out, D, sms, s, active);
-                continue;
-            }
-            if (diag && p.c == 3 && ((p.Tp == 11 || p.Tp == 12) ? p.tb_bits >= 7 && p.tb_bits <= 9 : p.Tp == 13 && p.tb_bits == 9)) {
-                // E = 2^(Tp - tb_bits) states per thread
-                switch ((p.tb_bits == 8 ? 100 : p.tb_bits == 7 ? 200 : 0) + (p.Tp == 11 ? 10 : p.Tp == 12 ? 20 : 30) + p.stages) {
-                    case 32: run_f32g<16, 2, 512>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 33: run_f32g<16, 3, 512>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 34: run_f32g<16, 4, 512>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 212: run_f32g<16, 2, 128>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 213: run_f32g<16, 3, 128>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 214: run_f32g<16, 4, 128>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 222: run_f32g<32, 2, 128>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 223: run_f32g<32, 3, 128>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 224: run_f32g<32, 4, 128>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 12: run_f32g<4, 2>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 13: run_f32g<4, 3>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 14: run_f32g<4, 4>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 23: run_f32g<8, 3>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 24: run_f32g<8, 4>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 112: run_f32g<8, 2, 256>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 113: run_f32g<8, 3, 256>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 114: run_f32g<8, 4, 256>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 122: run_f32g<16, 2, 256>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 123: run_f32g<16, 3, 256>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 124: run_f32g<16, 4, 256>(m, p, diag, in, out, D, sms, s, active); break;
-                    default: run_f32g<8, 2>(m, p, diag, in, out, D, sms, s, active); break;
-                }
-                continue;
-            }
-            if (diag && p.c == 3 && p.Tp >= 11 && p.Tp <= 13) {
-                switch (p.Tp) {
-                    case 11: run_f32<4>(m, p, diag, in, out, D, sms, s, active); break;
-                    case 12: run_f32<8>(m, p, diag, in, out, D, sms, s, active); break;
-                    default: run_f32<16>(m, p, diag, in, out, D, sms, s, active); break;
-                }
-                continue;
+            if (diag) {
+                const escdev::PassTab pt = make_pass_tab(p, m, &cols, dotp);
+                if (p.jit >= 0) g = jit_launch(p, pt, diag, in, out, D, sms, s, active);
+                else g = run_grouped(pt, p, diag, in, out, D, sms, s, active);
             }
         }
-        if (diag && p.c == 3 && p.Tp >= 10 && p.Tp <= 13) {
+        if (!g && diag && p.c == 3 && p.Tp >= 10 && p.Tp <= 13 && (sizeof(R) == 8 || !(p.Tp >= 11))) {
+            DevCols cc = cols;
+            cc.dotp = dotp;
             switch (p.Tp) {
-                case 10: run_fast<R, 2>(m, p, diag, in, out, D, sms, s, active); break;
-                case 11: run_fast<R, 4>(m, p, diag, in, out, D, sms, s, active); break;
-                case 12: run_fast<R, 8>(m, p, diag, in, out, D, sms, s, active); break;
-                default: run_fast<R, 16>(m, p, diag, in, out, D, sms, s, active); break;
+                case 10: g = run_fast<R, 2>(m, p, cc, diag, in, out, D, sms, s, active); break;
+                case 11: g = run_fast<R, 4>(m, p, cc, diag, in, out, D, sms, s, active); break;
+                case 12: g = run_fast<R, 8>(m, p, cc, diag, in, out, D, sms, s, active); break;
+                default: g = run_fast<R, 16>(m, p, cc, diag, in, out, D, sms, s, active); break;
             }
+        }
+        if (g) {
+            if (dotp) G = g;
             continue;
         }
-        const size_t smem = (size_t(1) << p.Tp) * sizeof(C);
-        if (smem > 48 * 1024)
-            ESC_CUDA(cudaFuncSetAttribute(k_hv_pass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        int per_sm = 0;
-        ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass<R>, TILE_THREADS, smem));
-        const long long ntiles = (long long)(D >> p.Tp);
-        const long long g = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
-        k_hv_pass<R><<<(unsigned)g, TILE_THREADS, smem, s>>>(m, p, (const C*)in, (C*)out, ntiles, active);
-        ESC_CUDA(cudaGetLastError());
+        // single-column kernels: one launch per column with that column's field
+        for (int c = 0; c < cols.ncols; c++) {
+            DevModel mc = m;
+            mc.fx = cols.f.fx[c]; mc.fy = cols.f.fy[c]; mc.fz = cols.f.fz[c];
+            mc.fxf = cols.f.fxf[c]; mc.fyf = cols.f.fyf[c]; mc.fzf = cols.f.fzf[c];
+            const C* inc = (const C*)in + c * cols.ld;
+            C* outc = (C*)out + c * cols.ld;
+            const int* act = active ? active + c : nullptr;
+            if (sizeof(R) == 4 && diag && p.c == 3 && p.Tp >= 11 && p.Tp <= 13) {
+                switch (p.Tp) {
+                    case 11: run_f32<4>(mc, p, diag, inc, outc, D, sms, s, act); break;
+                    case 12: run_f32<8>(mc, p, diag, inc, outc, D, sms, s, act); break;
+                    default: run_f32<16>(mc, p, diag, inc, outc, D, sms, s, act); break;
+                }
+                continue;
+            }
+            const size_t smem = (size_t(1) << p.Tp) * sizeof(C);
+            if (smem > 48 * 1024)
+                ESC_CUDA(cudaFuncSetAttribute(k_hv_pass<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            int per_sm = 0;
+            ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pass<R>, TILE_THREADS, smem));
+            const long long ntiles = (long long)(D >> p.Tp);
+            const long long gg = std::min<long long>(ntiles, (long long)sms * std::max(per_sm, 1));
+            k_hv_pass<R><<<(unsigned)gg, TILE_THREADS, smem, s>>>(mc, p, inc, outc, ntiles, act);
+            ESC_CUDA(cudaGetLastError());
+        }
+        if (dotp) {
+            k_dot_cols<R><<<dim3(DOT_GRID, cols.ncols), 256, 0, s>>>((const C*)in, (const C*)out, cols.ld, D, active, dotp);
+            ESC_CUDA(cudaGetLastError());
+            G = DOT_GRID;
+        }
     }
+    return G;
 }
 
+template <typename R>
+void launch_hv_tiled(const DevModel& m, const std::vector<DevPass>& passes, const void* in, void* out, int64_t D,
+                     const void* diag, cudaStream_t s, const int* active) {
+    launch_hv_cols<R>(m, single_column(m), passes, in, out, D, diag, s, active);
+}
+
+template int launch_hv_cols<double>(const DevModel&, const DevCols&, const std::vector<DevPass>&, const void*, void*,
+                                    int64_t, const void*, cudaStream_t, const int*);
+template int launch_hv_cols<float>(const DevModel&, const DevCols&, const std::vector<DevPass>&, const void*, void*,
+                                   int64_t, const void*, cudaStream_t, const int*);
 template void launch_hv_tiled<double>(const DevModel&, const std::vector<DevPass>&, const void*, void*, int64_t,
                                       const void*, cudaStream_t, const int*);
 template void launch_hv_tiled<float>(const DevModel&, const std::vector<DevPass>&, const void*, void*, int64_t,

@@ -97,93 +97,10 @@ __global__ void __launch_bounds__(256) k_hv(const __grid_constant__ DevModel m,
     }
 }
 
-// Batched H.V: NC columns (leading dimension ld), one field per column, index decoded once.
-template <typename R, int NC>
-__global__ void __launch_bounds__(256) k_hv_batched(const __grid_constant__ DevModel m,
-                                                    const __grid_constant__ DevFields f,
-                                                    const typename V2<R>::T* __restrict__ in,
-                                                    typename V2<R>::T* __restrict__ out, long long D,
-                                                    long long ld, int ncols) {
-    typedef typename V2<R>::T C;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < D; k += stride) {
-        const unsigned long long uk = (unsigned long long)k;
-        constexpr bool F32 = sizeof(R) == 4;
-        R dgb = 0;
-        for (int b = 0; b < m.nd; b++) {
-            const R q = F32 ? (R)m.dqf[b] : (R)(0.25 * m.d[b].dz);
-            dgb += (__popcll(uk & m.d[b].mask) == 1) ? -q : q;
-        }
-        const R nz = (R)(m.N - 2 * __popcll(uk));
-        R ar[NC], ai[NC], Fr[NC], Fi[NC], Gr[NC], Gi[NC];
-#pragma unroll
-        for (int c = 0; c < NC; c++) {
-            ar[c] = ai[c] = Fr[c] = Fi[c] = Gr[c] = Gi[c] = (R)0;
-            if (c < ncols) {
-                R dg;
-                if constexpr (F32) dg = fmaf(f.fzf[c], nz, dgb);
-                else dg = __dadd_rn(dgb, __dmul_rn(f.fz[c], nz));
-                const C v = in[c * ld + k];
-                ar[c] = dg * v.x; ai[c] = dg * v.y;
-            }
-        }
-        for (int b = 0; b < m.nb; b++) {
-            const unsigned long long mk = m.b[b].mask;
-            const bool df = __popcll(uk & mk) == 1;
-            R cc;
-            if constexpr (F32) cc = df ? m.cdifff[b] : m.ceqf[b];
-            else cc = df ? m.b[b].cdiff : m.b[b].ceq;
-            const unsigned long long kp = uk ^ mk;
-#pragma unroll
-            for (int c = 0; c < NC; c++)
-                if (c < ncols) {
-                    const C w = in[c * ld + kp];
-                    ar[c] = fma(cc, w.x, ar[c]);
-                    ai[c] = fma(cc, w.y, ai[c]);
-                }
-        }
-        for (int s = 0; s < m.N; s++) {
-            const unsigned long long kp = uk ^ (1ull << s);
-            const R sg = ((uk >> s) & 1ull) ? (R)1 : (R)-1;
-#pragma unroll
-            for (int c = 0; c < NC; c++)
-                if (c < ncols) {
-                    const C w = in[c * ld + kp];
-                    Fr[c] += w.x; Fi[c] += w.y;
-                    Gr[c] = fma(sg, w.x, Gr[c]); Gi[c] = fma(sg, w.y, Gi[c]);
-                }
-        }
-#pragma unroll
-        for (int c = 0; c < NC; c++)
-            if (c < ncols) {
-                const R fx = F32 ? (R)f.fxf[c] : (R)f.fx[c], fy = F32 ? (R)f.fyf[c] : (R)f.fy[c];
-                C o;
-                o.x = fma(-fy, Gi[c], fma(fx, Fr[c], ar[c]));
-                o.y = fma(fy, Gr[c], fma(fx, Fi[c], ai[c]));
-                out[c * ld + k] = o;
-            }
-    }
-}
-
 template <typename R>
 void launch_hv(const DevModel& m, const void* in, void* out, int64_t D, cudaStream_t s) {
     typedef typename V2<R>::T C;
     k_hv<R><<<grid_for(D, 256, SMS * 16), 256, 0, s>>>(m, (const C*)in, (C*)out, (long long)D);
-    ESC_CUDA(cudaGetLastError());
-}
-
-template <typename R>
-void launch_hv_batched(const DevModel& m, const DevFields& f, const void* in, void* out, int ncols, int64_t ld,
-                       int64_t D, cudaStream_t s) {
-    typedef typename V2<R>::T C;
-    const int g = grid_for(D, 256, SMS * 16);
-    const C* pi = (const C*)in;
-    C* po = (C*)out;
-    if (ncols <= 1) k_hv_batched<R, 1><<<g, 256, 0, s>>>(m, f, pi, po, D, ld, ncols);
-    else if (ncols <= 2) k_hv_batched<R, 2><<<g, 256, 0, s>>>(m, f, pi, po, D, ld, ncols);
-    else if (ncols <= 4) k_hv_batched<R, 4><<<g, 256, 0, s>>>(m, f, pi, po, D, ld, ncols);
-    else if (ncols <= 8) k_hv_batched<R, 8><<<g, 256, 0, s>>>(m, f, pi, po, D, ld, ncols);
-    else k_hv_batched<R, 16><<<g, 256, 0, s>>>(m, f, pi, po, D, ld, ncols);
     ESC_CUDA(cudaGetLastError());
 }
 
@@ -676,8 +593,6 @@ void launch_start_normal(uint64_t seed, void* out, int64_t n, cudaStream_t s) {
 // explicit instantiations
 #define ESC_INST(R)                                                                                        \
     template void launch_hv<R>(const DevModel&, const void*, void*, int64_t, cudaStream_t);                \
-    template void launch_hv_batched<R>(const DevModel&, const DevFields&, const void*, void*, int, int64_t, \
-                                       int64_t, cudaStream_t);                                             \
     template void launch_apply<R>(const DevOp&, const void*, void*, int64_t, cudaStream_t);                \
     template void launch_dot<R>(const void*, const void*, int64_t, double*, double*, cudaStream_t);        \
     template void launch_nrm2<R>(const void*, int64_t, double*, double*, cudaStream_t);                    \

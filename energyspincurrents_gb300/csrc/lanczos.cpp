@@ -1,26 +1,193 @@
 // lanczos.cpp -- the ground-state Lanczos (DynLanczosSolver::Lanczos_Nirav) and the batched
 // continued-fraction recurrences on the device; the host keeps only scalars and the tridiagonal.
+#include <functional>
 #include <type_traits>
 
 #include "abi_common.h"
 
 namespace escabi {
 
+// Columns of a CFBatch for the model list ms (one field per column) on the handle's passes.
+template <typename RR>
+std::function<int(const void*, void*, const int*, double*, cudaStream_t)> hv_all_columns(
+        esc_handle* h, const std::vector<esc::DevModel>& ms, const void* dg) {
+    esc::DevCols cols = esc::single_column(ms[0]);
+    cols.ncols = (int)ms.size();
+    cols.ld = h->D;
+    for (size_t c = 0; c < ms.size(); c++) {
+        cols.f.fx[c] = ms[c].fx; cols.f.fy[c] = ms[c].fy; cols.f.fz[c] = ms[c].fz;
+        cols.f.fxf[c] = ms[c].fxf; cols.f.fyf[c] = ms[c].fyf; cols.f.fzf[c] = ms[c].fzf;
+    }
+    const esc::DevModel m0 = ms[0];
+    return [h, cols, m0, dg](const void* in, void* out, const int* active, double* part, cudaStream_t s) {
+        esc::DevCols c = cols;
+        c.dotp = part;
+        return esc::launch_hv_cols<RR>(m0, c, h->passes, in, out, h->D, dg, s, active);
+    };
+}
+
+// Exit step of a run with LanczosEps > 0: the first iteration whose lowest Ritz value moved by
+// less than eps (src/DynLanczosSolver.h:125-151), from the recorded coefficients.
+static int exit_iteration(const std::vector<double>& a, const std::vector<double>& b, double eps) {
+    const int M = (int)a.size();
+    double E0 = 1.0;
+    for (int iter = 1; iter < M; iter++) {
+        std::vector<double> d(a.begin(), a.begin() + iter + 1), e(iter + 1, 0.0);
+        for (int i = 0; i < iter; i++) e[i] = b[i + 1];
+        if (!esc::tridiag_eig(iter + 1, d, e, nullptr)) throw Fail(ESC_ERR_NUMERIC, "diag: tridiagonal eigensolver failed");
+        const double diff = std::fabs(E0 - d[0]);
+        E0 = d[0];
+        if (diff < eps) return iter;
+    }
+    return M - 1;
+}
+
 // Ground-state Lanczos, DynLanczosSolver::Lanczos_Nirav (src/DynLanczosSolver.h:38-239).
+//
+// Without reorthogonalisation (OnlyEgs, and GS / All with Reortho=0) the recurrence runs on the
+// batched engine (batched.cu) with one column: unnormalised vectors u_k = beta_k v_k, alpha from
+// the epilogue of the last H.v pass, the update fused with its norm, every iteration captured in a
+// CUDA graph -- per step the H.v passes plus one streaming update, no separate dot or rescale
+// sweeps.  Same alpha, beta and Ritz values as the normalised recurrence (mathematically; the
+// rounding differs).  The run stops early only on beta = 0 or NaN, which are reported.
+//   GS: three vectors; |gs> = sum_m Z(m,0) v_m rebuilt in a second sweep that regenerates the
+//   vectors bit for bit (same kernels, same inputs) and accumulates them.
+//   All: every u_k kept, rescaled to v_k afterwards (Ritz-mode spectra need the basis).
+// With reorthogonalisation (the reference's mode) the normalised recurrence below runs as the
+// reference does, with full Gram-Schmidt against every stored vector.
 template <typename R>
 void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) {
     Pipe<R> P(h);
     const int64_t D = h->D;
     const size_t ES = Pipe<R>::ES;
     const int M = cfg.steps;
-    // GS without reorthogonalisation keeps three vectors and rebuilds |gs> in a second pass
-    // (the Lanczos vectors are recomputed from the recorded alpha/beta, not stored): the mode for
-    // bases too large to hold M+1 vectors (N = 28..32).
     const bool recompute = cfg.lanctype == 1 && !cfg.reortho;
     const bool store = cfg.lanctype != 0 && !recompute;  // OnlyEgs keeps no basis (returns a zero vector)
     const bool reo = store && cfg.reortho;
-    const int nvec = store ? M + 1 : 3;
     h->have_gs = h->have_basis = false;
+    if (!reo) {
+        // ---- unnormalised recurrence on the batched engine --------------------------------------
+        const size_t nd = (size_t)esc::CFB_GRID * 2 + (size_t)M * 2 + (size_t)(M + 1) + (size_t)(M + 2);
+        ensure_t(h->d_cfs, h->cfs_bytes, std::max(h->cfs_bytes, nd * sizeof(double)));
+        ensure_t(h->d_cfi, h->cfi_bytes, std::max(h->cfi_bytes, (size_t)4 * sizeof(int)));
+        ensure(h->d_L, h->L_bytes, (size_t)(store ? M + 1 + 3 : 3) * D * ES);
+        ensure_partials(h, 4);
+        ensure_t(h->d_sc, h->sc_bytes, std::max(h->sc_bytes, (size_t)16 * sizeof(double)));
+        char* ring = (char*)h->d_L + (store ? (size_t)(M + 1) * D * ES : 0);   // 3 rotating vectors
+        char* basis = (char*)h->d_L;                                             // All: u_0 .. u_M
+        const void* dg = diag_for(h, sizeof(R) == 4 ? ESC_C64 : ESC_C128);
+        const std::vector<esc::DevModel> ms{h->dm};
+        double* zc = nullptr;
+        auto make = [&](esc::CFBatch<R>& cb) {
+            cb.ncols = 1; cb.kmax = M; cb.D = D; cb.tol = 0.0; cb.use_graph = true;
+            cb.bufs = ring;
+            cb.d_part = h->d_cfs;
+            cb.d_alpha = cb.d_part + (size_t)esc::CFB_GRID * 2;
+            cb.d_b2 = cb.d_alpha + (size_t)M * 2;
+            zc = cb.d_b2 + (M + 1);
+            cb.d_active = h->d_cfi;
+            cb.d_steps = h->d_cfi + 1;
+            cb.d_it = h->d_cfi + 2;
+            cb.hv_all = hv_all_columns<R>(h, ms, dg);
+        };
+        // u_0 = normalised start, in the ring's set 1 (the engine's first "cur")
+        auto load_start = [&]() {
+            P.nrm2(d_start, h->d_sc);
+            P.scale(d_start, ring + D * ES, h->d_sc);
+        };
+        ESC_CUDA(cudaMemsetAsync(h->d_cfs, 0, nd * sizeof(double), h->stream));
+        ESC_CUDA(cudaMemcpyAsync(h->d_cfi + 1, &M, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+        esc::CFBatch<R> cb;
+        make(cb);
+        load_start();
+        if (store) {
+            ESC_CUDA(cudaMemcpyAsync(basis, ring + D * ES, D * ES, cudaMemcpyDeviceToDevice, h->stream));
+            cb.after_update = [&](const void* w, cudaStream_t s) {
+                esc::launch_store_iter<R>(w, basis, D, cb.d_it, cb.d_active, s);
+            };
+        }
+        cb.run(h->stream);   // synchronises
+        std::vector<double> al((size_t)M * 2), b2(M + 1);
+        ESC_CUDA(cudaMemcpy(al.data(), cb.d_alpha, al.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        ESC_CUDA(cudaMemcpy(b2.data(), cb.d_b2, b2.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        std::vector<double> a, b{0.0};
+        int n = 0;
+        for (; n < M; n++) {
+            a.push_back(al[2 * (size_t)n]);
+            b.push_back(std::sqrt(b2[n + 1]));
+            if (!std::isfinite(a.back()) || !std::isfinite(b.back()))
+                throw Fail(ESC_ERR_NUMERIC, "NaN/Inf in Lanczos coefficients at step " + std::to_string(n));
+            if (n + 1 < M && !(b.back() > 0.0))
+                throw Fail(ESC_ERR_NUMERIC, "Lanczos breakdown: beta=0 at step " + std::to_string(n + 1) +
+                                                " (Krylov space exhausted; use fewer LanczosSteps)");
+        }
+        const int nx = cfg.eps > 0.0 ? exit_iteration(a, b, cfg.eps) + 1 : M;   // EXITiter (:164)
+        h->alpha.assign(a.begin(), a.begin() + nx);
+        h->beta.assign(b.begin(), b.begin() + nx + 1);
+        std::vector<double> d(h->alpha), e(nx, 0.0);
+        for (int i = 0; i < nx - 1; i++) e[i] = h->beta[i + 1];
+        h->Z.clear();
+        if (!esc::tridiag_eig(nx, d, e, (store || recompute) ? &h->Z : nullptr))
+            throw Fail(ESC_ERR_NUMERIC, "diag: tridiagonal eigensolver failed");
+        h->ritz = d;
+        h->nsteps = nx;
+        ensure(h->d_gs, h->gs_bytes, (size_t)D * ES);
+        if (recompute) {
+            // second sweep: the same kernels on the same inputs regenerate u_0 .. u_{nx-1}; gs
+            // accumulates Z(m,0) v_m = Z(m,0) / beta_m u_m  (beta_0 = |u_0| after normalisation)
+            std::vector<double> z(nx);
+            for (int m = 0; m < nx; m++) z[m] = h->Z[m] / std::sqrt(b2[m]);
+            ESC_CUDA(cudaMemsetAsync(h->d_cfs, 0, nd * sizeof(double), h->stream));
+            ESC_CUDA(cudaMemcpyAsync(zc, z.data(), nx * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+            const int steps = nx - 1;
+            esc::CFBatch<R> cb2;
+            make(cb2);
+            if (steps > 0) {
+                ESC_CUDA(cudaMemcpyAsync(cb2.d_steps, &steps, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+                cb2.kmax = M;
+            }
+            load_start();
+            ESC_CUDA(cudaMemsetAsync(h->d_gs, 0, (size_t)D * ES, h->stream));
+            esc::launch_axpy_dev<R>(ring + D * ES, h->d_gs, zc, D, h->stream);
+            if (steps > 0) {
+                cb2.after_update = [&](const void* w, cudaStream_t s) {
+                    esc::launch_accum_iter<R>(w, h->d_gs, D, cb2.d_it, zc, cb2.d_active, s);
+                };
+                cb2.run(h->stream);
+            }
+        } else if (store) {
+            // v_m = u_m / beta_m (beta_m^2 = b2[m], on the device), then PsiAll[0] = sum_m v_m Z(m,0)
+            for (int m = 0; m < nx; m++) {
+                char* L = basis + (size_t)m * D * ES;
+                P.scale(L, L, cb.d_b2 + m);
+            }
+            ensure_t(h->d_sc, h->sc_bytes, std::max(h->sc_bytes, (size_t)(nx + 8) * sizeof(double)));
+            double* d_z = h->d_sc;
+            ESC_CUDA(cudaMemcpyAsync(d_z, h->Z.data(), nx * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+            esc::launch_lincomb<R>(basis, D, nx, d_z, h->d_gs, D, h->stream);
+            h->have_basis = cfg.lanctype == 2;
+        } else {
+            ESC_CUDA(cudaMemsetAsync(h->d_gs, 0, (size_t)D * ES, h->stream));   // OnlyEgs returns zeros (:178-180)
+        }
+        if (recompute || store) {
+            // the Lanczos vectors lose orthogonality once the ground state has converged, so the
+            // sum is not a unit vector: normalise it
+            P.nrm2(h->d_gs, h->d_sc + 3);
+            P.scale(h->d_gs, h->d_gs, h->d_sc + 3);
+        }
+        if (!store && h->d_L) {   // the three recurrence vectors are not needed any more: free them for the dynamics
+            cudaFree(h->d_L);
+            h->d_L = nullptr;
+            h->L_bytes = 0;
+        }
+        h->basis_dt = sizeof(R) == 8 ? ESC_C128 : ESC_C64;
+        h->L_ld = D;
+        h->have_gs = true;
+        sync(h);
+        return;
+    }
+    // ---- normalised recurrence with full reorthogonalisation (the reference's mode) ---------------
+    const int nvec = M + 1;
     ensure(h->d_L, h->L_bytes, (size_t)nvec * D * ES);
     ensure(h->d_work, h->work_bytes, (size_t)D * ES);
     // scalars: alpha[2M] | b2[M+2] | tmp[8] | r[2(M+2)] | z[M+2]
@@ -31,9 +198,9 @@ void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) 
     double* d_tmp = d_b2 + (M + 2);
     double* d_r = d_tmp + 8;
     double* d_z = d_r + 2 * (M + 2);
-    ensure_partials(h, reo ? M + 2 : 4);
+    ensure_partials(h, M + 2);
     ESC_CUDA(cudaMemsetAsync(h->d_sc, 0, n_sc * sizeof(double), h->stream));
-    auto Lv = [&](int i) -> char* { return (char*)h->d_L + (size_t)(store ? i : i % 3) * D * ES; };
+    auto Lv = [&](int i) -> char* { return (char*)h->d_L + (size_t)i * D * ES; };
     void* w = h->d_work;
 
     // Vorig.normalize(); V0 = Vorig (:58-66)
@@ -52,18 +219,16 @@ void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) 
         esc::launch_lanczos_update<R>(w, Lv(iter), Lv(iter - 1), d_alpha + 2 * iter, d_b2 + iter, D, h->d_part,
                                       d_b2 + iter + 1, h->stream);
         P.scale(w, Lv(iter + 1), d_b2 + iter + 1);
-        if (reo) {
-            // Full reorthogonalisation against L_0..L_iter (:105-119).  The reference does one
-            // modified Gram-Schmidt sweep; here two classical sweeps (CGS2) as two GEMV pairs,
-            // which orthogonalise to the same working precision.
-            for (int pass = 0; pass < 2; pass++) {
-                esc::launch_gemv_h<R>(h->d_L, D, iter + 1, Lv(iter + 1), D, h->d_part, part_cap_doubles(h), d_r,
-                                      h->stream);
-                esc::launch_gemv_sub<R>(h->d_L, D, iter + 1, d_r, Lv(iter + 1), D, h->stream);
-            }
-            P.nrm2(Lv(iter + 1), d_tmp + 1);
-            P.scale(Lv(iter + 1), Lv(iter + 1), d_tmp + 1);
+        // Full reorthogonalisation against L_0..L_iter (:105-119).  The reference does one
+        // modified Gram-Schmidt sweep; here two classical sweeps (CGS2) as two GEMV pairs,
+        // which orthogonalise to the same working precision.
+        for (int pass = 0; pass < 2; pass++) {
+            esc::launch_gemv_h<R>(h->d_L, D, iter + 1, Lv(iter + 1), D, h->d_part, part_cap_doubles(h), d_r,
+                                  h->stream);
+            esc::launch_gemv_sub<R>(h->d_L, D, iter + 1, d_r, Lv(iter + 1), D, h->stream);
         }
+        P.nrm2(Lv(iter + 1), d_tmp + 1);
+        P.scale(Lv(iter + 1), Lv(iter + 1), d_tmp + 1);
         if (cfg.eps > 0.0) {                                 // :125-151 (convergence test)
             std::vector<double> a(2 * (iter + 1)), b2(iter + 2);
             ESC_CUDA(cudaMemcpyAsync(a.data(), d_alpha, a.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -97,44 +262,14 @@ void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) 
     std::vector<double> d(h->alpha), e(n, 0.0);
     for (int i = 0; i < n - 1; i++) e[i] = h->beta[i + 1];
     h->Z.clear();
-    if (!esc::tridiag_eig(n, d, e, (store || recompute) ? &h->Z : nullptr)) throw Fail(ESC_ERR_NUMERIC, "diag: tridiagonal eigensolver failed");
+    if (!esc::tridiag_eig(n, d, e, &h->Z)) throw Fail(ESC_ERR_NUMERIC, "diag: tridiagonal eigensolver failed");
     h->ritz = d;
     h->nsteps = n;
     ensure(h->d_gs, h->gs_bytes, (size_t)D * ES);
-    if (recompute) {
-        // second pass: identical kernels on identical inputs regenerate L_0..L_{n-1} bit for bit
-        ESC_CUDA(cudaMemcpyAsync(d_z, h->Z.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-        ESC_CUDA(cudaMemsetAsync(h->d_gs, 0, (size_t)D * ES, h->stream));
-        P.nrm2(d_start, d_tmp);
-        P.scale(d_start, Lv(0), d_tmp);
-        esc::launch_axpy_dev<R>(Lv(0), h->d_gs, d_z, D, h->stream);
-        for (int it = 0; it + 1 < n; it++) {
-            P.hv(Lv(it), w);
-            esc::launch_lanczos_update<R>(w, Lv(it), it ? Lv(it - 1) : nullptr, d_alpha + 2 * it, it ? d_b2 + it : nullptr,
-                                          D, h->d_part, d_tmp + 2, h->stream);
-            P.scale(w, Lv(it + 1), d_b2 + it + 1);
-            esc::launch_axpy_dev<R>(Lv(it + 1), h->d_gs, d_z + it + 1, D, h->stream);
-        }
-    } else if (store) {
-        // PsiAll[0] = sum_m L_m Z(m,0) (:208-234), without forming the other Ritz vectors
-        ESC_CUDA(cudaMemcpyAsync(d_z, h->Z.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-        esc::launch_lincomb<R>(h->d_L, D, n, d_z, h->d_gs, D, h->stream);
-        h->have_basis = cfg.lanctype == 2;
-    } else {
-        ESC_CUDA(cudaMemsetAsync(h->d_gs, 0, (size_t)D * ES, h->stream));   // OnlyEgs returns zeros (:178-180)
-    }
-    if ((recompute || store) && !reo) {
-        // Without reorthogonalisation the Lanczos vectors lose orthogonality once the ground state
-        // has converged, and sum_m Z(m,0) L_m is then not a unit vector: normalise it.  (With full
-        // reorthogonalisation, the reference's mode, the sum is kept exactly as the reference forms it.)
-        P.nrm2(h->d_gs, d_tmp + 3);
-        P.scale(h->d_gs, h->d_gs, d_tmp + 3);
-    }
-    if (!store && h->d_L) {   // the three recurrence vectors are not needed any more: free them for the dynamics
-        cudaFree(h->d_L);
-        h->d_L = nullptr;
-        h->L_bytes = 0;
-    }
+    // PsiAll[0] = sum_m L_m Z(m,0) (:208-234), without forming the other Ritz vectors
+    ESC_CUDA(cudaMemcpyAsync(d_z, h->Z.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    esc::launch_lincomb<R>(h->d_L, D, n, d_z, h->d_gs, D, h->stream);
+    h->have_basis = cfg.lanctype == 2;
     h->basis_dt = sizeof(R) == 8 ? ESC_C128 : ESC_C64;
     h->L_ld = D;
     h->have_gs = true;
@@ -180,9 +315,7 @@ void cf_batch_run(esc_handle* h, int ncols, int kmax, const std::vector<int>& st
         cb.d_steps = h->d_cfi + ncols;
         cb.d_it = h->d_cfi + 2 * ncols;
         typedef typename std::conditional<std::is_same<CB, esc::CFBatch<float>>::value, float, double>::type RR;
-        cb.hv_column = [h, &ms, dg](int c, const void* in, void* out, const int* active, cudaStream_t s) {
-            esc::launch_hv_tiled<RR>(ms[c], h->passes, in, out, h->D, dg, s, active);
-        };
+        cb.hv_all = hv_all_columns<RR>(h, ms, dg);
     };
     ESC_CUDA(cudaMemsetAsync(h->d_cfs, 0, nd * sizeof(double), h->stream));
     esc::CFBatch<R> cb;

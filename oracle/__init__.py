@@ -41,6 +41,7 @@ def lib():
         L.or_tridiag.argtypes = [c_int, c_void_p, c_void_p, c_void_p, c_void_p]
         L.or_lanczos.argtypes = [c_void_p, c_void_p, c_int, c_double, c_char_p, c_void_p, c_void_p, c_void_p, P(c_int)]
         L.or_get_psi.argtypes = [c_void_p, c_void_p]
+        L.or_lanczos3.argtypes = [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p]
         L.or_set_ritz.argtypes = [c_void_p, c_int, c_void_p, c_void_p]
         L.or_apply.argtypes = [c_void_p, c_char_p, c_int, c_void_p, c_void_p]
         L.or_dynamics.argtypes = [c_void_p, c_char_p, c_int, c_double, c_double, c_void_p]
@@ -168,6 +169,16 @@ class Model:
             raise RuntimeError(lib().or_last_error().decode())
         n = n.value
         return dict(alpha=a[:n], beta=b[: n + 1], ritz=r[:n], steps=n)
+
+    def lanczos3(self, start, M, want_gs=True):
+        """Three-vector FP64 Lanczos without reorthogonalisation on the matrix-free H.v (bases whose
+        COO lists or M+1 vectors do not fit); |gs> rebuilt in a second sweep and normalised."""
+        start = np.ascontiguousarray(start, dtype=np.complex128)
+        a = np.zeros(M); b = np.zeros(M + 1); r = np.zeros(M)
+        gs = np.empty(self.D, dtype=np.complex128) if want_gs else None
+        if lib().or_lanczos3(self.h, _p(start), M, _p(a), _p(b), _p(r), _p(gs) if want_gs else None):
+            raise RuntimeError(lib().or_last_error().decode())
+        return dict(alpha=a, beta=b, ritz=r, E0=r[0], gs=gs)
 
     def psi(self):
         out = np.empty(self.D, dtype=np.complex128)

@@ -18,7 +18,7 @@ def build(force: bool = False) -> str:
     if (not force and os.path.exists(SO)
             and os.path.getmtime(SO) >= max(os.path.getmtime(SRC), os.path.getmtime(__file__))):
         return SO
-    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-shared", "-fPIC", "-o", SO + ".tmp", SRC]
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fcx-limited-range", "-fopenmp", "-shared", "-fPIC", "-o", SO + ".tmp", SRC]
     subprocess.run(cmd, check=True)
     os.replace(SO + ".tmp", SO)
     return SO

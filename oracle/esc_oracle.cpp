@@ -265,27 +265,64 @@ static void hv_matfree(const OrModel& m, const std::complex<R>* vin, std::comple
                        int64_t r0, int64_t r1, int threads) {
     typedef std::complex<R> C;
     const int N = m.N;
-#pragma omp parallel for num_threads(threads) schedule(static)
-    for (int64_t k = r0; k < r1; k++) {
-        double dg = 0.0;
-        for (const Bond& b : m.zb) dg += b.k * ((findBit(k, b.i) == findBit(k, b.j)) ? 0.25 : -0.25);
-        for (int s = 0; s < N; s++) dg += m.Bzz * (findBit(k, s) ? -0.5 : 0.5);
-        for (const Bond& b : m.nn) if (m.J != 0.0) dg += m.J * ((findBit(k, b.i) == findBit(k, b.j)) ? 0.25 : -0.25);
-        C acc = C(R(dg), 0) * vin[k];
-        for (const Bond& b : m.xb) acc += C(R(0.25 * b.k), 0) * vin[k ^ ((int64_t(1) << b.i) | (int64_t(1) << b.j))];
-        for (const Bond& b : m.yb) {
-            double c = (findBit(k, b.i) == findBit(k, b.j)) ? -0.25 * b.k : 0.25 * b.k;
-            acc += C(R(c), 0) * vin[k ^ ((int64_t(1) << b.i) | (int64_t(1) << b.j))];
+    // Rows in blocks of 2^16; within a block the terms are applied one after another, so every term
+    // streams through one contiguous source block (k ^ mask for k in an aligned block) instead of
+    // gathering 2.5N scattered partners per row, and terms that read the same source block (same
+    // mask bits above the block) run back to back while it is in cache.
+    struct Term { int64_t mask; int kind, i, j; double c; };   // kind: 0 x bond, 1 y bond, 2 J bond, 3 field
+    std::vector<Term> terms;
+    for (const Bond& b : m.xb) terms.push_back({(int64_t(1) << b.i) | (int64_t(1) << b.j), 0, b.i, b.j, 0.25 * b.k});
+    for (const Bond& b : m.yb) terms.push_back({(int64_t(1) << b.i) | (int64_t(1) << b.j), 1, b.i, b.j, 0.25 * b.k});
+    if (m.J != 0.0)
+        for (const Bond& b : m.nn) terms.push_back({(int64_t(1) << b.i) | (int64_t(1) << b.j), 2, b.i, b.j, 0.5 * m.J});
+    for (int s = 0; s < N; s++) terms.push_back({int64_t(1) << s, 3, s, s, 0.0});
+    const int SB = 16;
+    const int64_t B = int64_t(1) << SB;
+    std::stable_sort(terms.begin(), terms.end(), [&](const Term& a, const Term& b) { return (a.mask >> SB) < (b.mask >> SB); });
+    const int64_t nblk = (r1 - r0 + B - 1) / B;
+#pragma omp parallel num_threads(threads)
+    {
+        std::vector<C> acc(B);
+#pragma omp for schedule(static)
+        for (int64_t q = 0; q < nblk; q++) {
+            const int64_t k0 = r0 + q * B, k1 = std::min(r1, k0 + B);
+            for (int64_t k = k0; k < k1; k++) {
+                double dg = 0.0;
+                for (const Bond& b : m.zb) dg += b.k * ((findBit(k, b.i) == findBit(k, b.j)) ? 0.25 : -0.25);
+                for (int s = 0; s < N; s++) dg += m.Bzz * (findBit(k, s) ? -0.5 : 0.5);
+                for (const Bond& b : m.nn) if (m.J != 0.0) dg += m.J * ((findBit(k, b.i) == findBit(k, b.j)) ? 0.25 : -0.25);
+                acc[k - k0] = C(R(dg), 0) * vin[k];
+            }
+            for (const Term& t : terms) {
+                const std::complex<R>* src = vin;
+                const int64_t mk = t.mask;
+                switch (t.kind) {
+                    case 0: {
+                        const C c(R(t.c), 0);
+                        for (int64_t k = k0; k < k1; k++) acc[k - k0] += c * src[k ^ mk];
+                        break;
+                    }
+                    case 1:
+                        for (int64_t k = k0; k < k1; k++) {
+                            const double c = (findBit(k, t.i) == findBit(k, t.j)) ? -t.c : t.c;
+                            acc[k - k0] += C(R(c), 0) * src[k ^ mk];
+                        }
+                        break;
+                    case 2: {
+                        const C c(R(t.c), 0);
+                        for (int64_t k = k0; k < k1; k++)
+                            if (findBit(k, t.i) != findBit(k, t.j)) acc[k - k0] += c * src[k ^ mk];
+                        break;
+                    }
+                    default:
+                        for (int64_t k = k0; k < k1; k++) {
+                            const C f(R(0.5 * m.Bxx), R(findBit(k, t.i) ? 0.5 * m.Byy : -0.5 * m.Byy));
+                            acc[k - k0] += f * src[k ^ mk];
+                        }
+                }
+            }
+            for (int64_t k = k0; k < k1; k++) vout[k - r0] = acc[k - k0];
         }
-        if (m.J != 0.0)
-            for (const Bond& b : m.nn)
-                if (findBit(k, b.i) != findBit(k, b.j))
-                    acc += C(R(0.5 * m.J), 0) * vin[k ^ ((int64_t(1) << b.i) | (int64_t(1) << b.j))];
-        for (int s = 0; s < N; s++) {
-            C f(R(0.5 * m.Bxx), R(findBit(k, s) ? 0.5 * m.Byy : -0.5 * m.Byy));
-            acc += f * vin[k ^ (int64_t(1) << s)];
-        }
-        vout[k - r0] = acc;
     }
 }
 
@@ -456,6 +493,51 @@ static int lanczos_nirav(OrModel& m, const cplx* start, int MAXiter, double Lanc
     }
     std::copy(m.PsiAll.begin(), m.PsiAll.begin() + N, m.Psi.begin());
     return 0;
+}
+
+// EXTENSION: the same three-term recurrence without reorthogonalisation (src/DynLanczosSolver.h:
+// 73-101 with the reortho block :105-119 skipped, as LancType=OnlyEgs does) on three vectors and
+// the matrix-free H.v, for bases whose M+1 vectors or COO lists do not fit (N >= 22).  E0 and the
+// tridiagonal come from the first sweep; a second sweep regenerates the Lanczos vectors (same
+// operations, so bit-identical) and forms |gs> = sum_m Z(m,0) L_m (:208-234 for k = 0), then
+// normalises it (the vectors are not orthogonal without reorthogonalisation).
+static void lanczos3(OrModel& m, const cplx* start, int M, std::vector<double>& a, std::vector<double>& b,
+                     std::vector<double>& ritz, std::vector<cplx>* gs) {
+    const int64_t D = m.D;
+    std::vector<cplx> V0(D), V1(start, start + D), V2(D);
+    auto sweep = [&](const std::vector<double>* z, std::vector<cplx>* acc) {
+        std::fill(V0.begin(), V0.end(), cplx(0, 0));
+        std::copy(start, start + D, V1.begin());
+        vnormalize(V1.data(), D);
+        if (acc) for (int64_t h = 0; h < D; h++) (*acc)[h] = V1[h] * (*z)[0];
+        for (int it = 0; it < M; it++) {
+            hv_matfree<double>(m, V1.data(), V2.data(), 0, D, m.threads);
+            const double al = vdot(V1.data(), V2.data(), D).real();
+            const double be = it ? b[it] : 0.0;
+            if (!acc) a[it] = al;
+            for (int64_t h = 0; h < D; h++) V2[h] = V2[h] - (acc ? a[it] : al) * V1[h] - be * V0[h];
+            if (it + 1 == M) break;
+            const double bn = vnorm(V2.data(), D);
+            if (!acc) b[it + 1] = bn;
+            for (int64_t h = 0; h < D; h++) V2[h] /= (acc ? b[it + 1] : bn);
+            std::swap(V0, V1);
+            std::swap(V1, V2);
+            if (acc) for (int64_t h = 0; h < D; h++) (*acc)[h] += V1[h] * (*z)[it + 1];
+        }
+    };
+    a.assign(M, 0.0);
+    b.assign(M + 1, 0.0);
+    sweep(nullptr, nullptr);
+    std::vector<double> d(a), e(M, 0.0), Z;
+    for (int i = 0; i + 1 < M; i++) e[i] = b[i + 1];
+    if (tridiag_ql(M, d, e, gs ? &Z : nullptr) != 0) throw std::runtime_error("tridiagonal eigensolver failed");
+    ritz = d;
+    if (gs) {
+        std::vector<double> z0(Z.begin(), Z.begin() + M);   // column 0: eigenvector of the lowest Ritz value
+        gs->assign(D, cplx(0, 0));
+        sweep(&z0, gs);
+        vnormalize(gs->data(), D);
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -833,6 +915,20 @@ int or_lanczos(void* h, const double* start, int M, double eps, const char* lanc
         for (int i = 0; i < ex; i++) alpha[i] = m->alpha[i].real();
         for (int i = 0; i <= ex && i < (int)m->beta.size(); i++) beta[i] = m->beta[i].real();
         for (int i = 0; i < ex; i++) ritz[i] = m->TriDeval[i];
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
+int or_lanczos3(void* h, const double* start, int M, double* alpha, double* beta, double* ritz, double* gs_out) {
+    OrModel* m = (OrModel*)h;
+    try {
+        std::vector<double> a, b, r;
+        std::vector<cplx> gs;
+        lanczos3(*m, (const cplx*)start, M, a, b, r, gs_out ? &gs : nullptr);
+        std::copy(a.begin(), a.end(), alpha);
+        std::copy(b.begin(), b.end(), beta);
+        std::copy(r.begin(), r.end(), ritz);
+        if (gs_out) std::memcpy(gs_out, gs.data(), gs.size() * sizeof(cplx));
         return 0;
     } catch (std::exception& e) { g_err = e.what(); return 1; }
 }

@@ -555,3 +555,65 @@ def test_cf_spectra_all_kinds_vs_exact_eigenpairs(kind):
     s = h.spectrum(kind, "CF", omega_steps=nw - 1, domega=dw, eta=eta, cf_steps=256)
     assert s.shape == ref.shape
     assert np.abs(s - ref).max() < 1e-8 * max(1.0, np.abs(ref).max())
+
+
+@pytest.mark.parametrize("shape,dt", [((3, 4), np.complex128), ((3, 6), np.complex64), ((4, 4), np.complex64),
+                                      ((2, 4), np.complex128), ((3, 6), np.complex128)])
+def test_hv_batched_device_columns_match_single(shape, dt):
+    """esc_hv_batched on device pointers: the tiled passes run over all columns at once (tile
+    offsets and term groups decoded once per tile, one field per column) and give, bit for bit, the
+    single-column H.v of a handle with that column's field."""
+    torch = pytest.importorskip("torch")
+    p = kitaev(Lx=shape[0], Ly=shape[1], J=0.1)
+    h = esc.Handle(p)
+    rng = np.random.default_rng(7)
+    nc = 5
+    V = (rng.standard_normal((nc, h.D)) + 1j * rng.standard_normal((nc, h.D))).astype(dt)
+    fields = np.array([[p["Bxx"]] * 3, [0.0] * 3, [-0.02] * 3, [0.1, -0.2, 0.3], [-0.1] * 3])
+    din = torch.from_numpy(V).cuda()
+    dout = torch.empty_like(din)
+    torch.cuda.synchronize()
+    st = esc.lib().esc_hv_batched(h.h, esc.ctypes.c_void_p(din.data_ptr()), esc.ctypes.c_void_p(dout.data_ptr()), nc, h.D,
+                                  esc._ptr(np.ascontiguousarray(fields)), esc.C64 if dt == np.complex64 else esc.C128,
+                                  esc.DEVICE_PTR)
+    assert st == esc.ESC_OK, esc.lib().esc_last_error(h.h)
+    out = dout.cpu().numpy()
+    for c in range(nc):
+        hc = esc.Handle(dict(p, Bxx=fields[c, 0], Byy=fields[c, 1], Bzz=fields[c, 2]))
+        assert np.array_equal(out[c], hc.hv(V[c])), c
+
+
+@pytest.mark.parametrize("dt", [np.complex128, np.complex64])
+def test_lanczos_without_reortho_matches_oracle(dt):
+    """Ground-state Lanczos without reorthogonalisation (unnormalised vectors, alpha from the last
+    H.v pass, one update sweep per step, iterations in a CUDA graph) against the oracle's
+    three-vector FP64 recurrence on the same start vector (18 sites)."""
+    p = kitaev(Lx=3, Ly=6, J=0.1, seed=0)
+    h = esc.Handle(p)
+    m = O.Model("Kitaev", 3, 6, 1, 1, -1.0, -1.0, -1.0, p["Bxx"], p["Byy"], p["Bzz"], 0.1, 8, False)
+    v0 = O.random_start(0, h.D)
+    r = h.lanczos_gs(start=v0, steps=120, lanctype="GS", reortho=0, dtype=dt)
+    ro = m.lanczos3(v0, 120)
+    c128 = dt == np.complex128
+    tol = 1e-12 if c128 else 3e-6
+    np.testing.assert_allclose(r["alpha"][:30], ro["alpha"][:30], atol=tol)
+    np.testing.assert_allclose(r["beta"][1:31], ro["beta"][1:31], atol=tol)
+    assert abs(r["E0"] - ro["E0"]) <= (1e-10 if c128 else 1e-5) * abs(ro["E0"])
+    gs = r["gs"].astype(np.complex128)
+    assert abs(abs(np.vdot(ro["gs"], gs)) / np.linalg.norm(gs) - 1) < (1e-10 if c128 else 1e-5)
+
+
+def test_lanczos_eps_exit_matches_reference_rule():
+    """LanczosEps > 0 without reorthogonalisation: the run stops at the first step whose lowest Ritz
+    value moved by less than eps (src/DynLanczosSolver.h:125-151); the coefficients are those of the
+    full run up to that step."""
+    p = kitaev(J=0.1, seed=0)
+    h = esc.Handle(p)
+    v0 = O.random_start(0, h.D)
+    full = h.lanczos_gs(start=v0, steps=150, lanctype="GS", reortho=0)
+    r = h.lanczos_gs(start=v0, steps=150, eps=1e-9, lanctype="GS", reortho=0)
+    n = r["steps"]
+    assert 2 < n < 150
+    assert np.array_equal(r["alpha"], full["alpha"][:n])
+    w = [O.tridiag_eig(full["alpha"][:k + 1], full["beta"][1:k + 1], vectors=False)[0] for k in range(n)]
+    assert abs(w[n - 1] - w[n - 2]) < 1e-9 and all(abs(w[k] - w[k - 1]) >= 1e-9 for k in range(1, n - 1))
