@@ -138,12 +138,13 @@ def cpu_baseline(params, sites, target_s=12.0, kind="port"):
                       f"oracle matrix-free gather (oracle/esc_oracle.cpp hv_matfree)"}
 
 
-def workload_config(sites, world):
+def workload_config(sites, world, dtype="c64"):
     """The `config` both arms report for the --sites workload."""
     params = workload(sites)
     D = 1 << sites
+    cname = "complex128" if dtype == "c128" else "complex64"
     return {"workload": f"Kitaev-Heisenberg honeycomb N={sites} ({params['Lx']}x{params['Ly']//2} "
-                        f"unit cells, PBC), K=-1 J=0.05 h=0.02[111], one H.v per step (complex64)",
+                        f"unit cells, PBC), K=-1 J=0.05 h=0.02[111], one H.v per step ({cname})",
             "states": D, "l2": "inputs larger than L2 (no flush needed)" if D * 8 > 129e6 else "inputs smaller than L2",
             "parallelism": "replicas" if world > 1 else "single GPU"}
 
@@ -239,6 +240,8 @@ def lanczos_step_report(esc, sites, steps=24):
     hv_ms = ev0.elapsed_time(ev1) / 5
     del v, out
     torch.cuda.empty_cache()
+    # warm-up run: allocates the recurrence vectors and the scalars once
+    h.lanczos_gs(steps=steps // 2, lanctype="OnlyEgs", reortho=0, dtype=np.complex64, want_gs=False)
     t = []
     for n in (steps // 2, steps):
         torch.cuda.synchronize()
@@ -297,6 +300,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--sites", type=int, default=32)
+    ap.add_argument("--dtype", default="c64", choices=["c64", "c128"],
+                    help="c128: the step is the plain FP64 H.v (complex128 vectors; no self-tuner, e2e or spectrum legs)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-spectrum", action="store_true")
@@ -307,6 +312,8 @@ def main():
     ap.add_argument("--gs-report", action="store_true",
                     help="time a mixed-precision ground state of the --sites cluster (Lanczos on complex64 vectors, "
                          "FP64 Rayleigh refinement) and print one JSON line, then exit")
+    ap.add_argument("--alu-report", action="store_true",
+                    help="measure the FP32 / packed FP32 / FP64 FMA ceilings of the GPU (clocks sampled) and print one JSON line")
     ap.add_argument("--step-report", action="store_true",
                     help="time one complex64 Lanczos step of the --sites cluster against one H.v and print one JSON line")
     ap.add_argument("--autotune-report", action="store_true",
@@ -331,6 +338,17 @@ def main():
     if args.gs_report:
         print(json.dumps(ground_state_report(esc, args.sites)), flush=True)
         return
+    if args.alu_report:
+        with Clocks(local) as clk:
+            r = esc.alu_peaks()
+        r["clocks"] = clk.summary()
+        mhz = r["clocks"].get("sm_mhz")
+        if mhz:   # per SM and clock: flops / (SMs x cycles)
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
+            for k in ("ffma", "ffma2", "dfma"):
+                r[k + "_flops_per_sm_clock"] = round(r[k + "_tflops"] * 1e12 / (sms * mhz * 1e6), 2)
+        print(json.dumps(r), flush=True)
+        return
     if args.step_report:
         print(json.dumps(lanczos_step_report(esc, args.sites)), flush=True)
         return
@@ -344,17 +362,21 @@ def main():
     params = workload(args.sites)
     h = esc.Handle(params)
     D = h.D
+    c128 = args.dtype == "c128"
+    if c128:
+        args.no_autotune = args.no_e2e = args.no_spectrum = True
     tuning = None
     if not args.no_autotune:
         # the library's self-tuner: per-pass choice of kernel variant for this Hamiltonian (untimed)
         tuning = h.autotune().strip().splitlines()[-1]
     stream = torch.cuda.ExternalStream(h.stream())
-    v = torch.empty(D, dtype=torch.complex64, device="cuda")
+    edt = esc.C128 if c128 else esc.C64
+    v = torch.empty(D, dtype=torch.complex128 if c128 else torch.complex64, device="cuda")
     out = torch.empty_like(v)
     # vectors stay resident in the library's internal basis order (a fixed relabelling of the sites;
     # inner products and spectra do not depend on it), so a step is exactly the H.v kernels
     flags = esc.DEVICE_PTR | esc.ASYNC | esc.INTERNAL_ORDER
-    st = esc.lib().esc_start_vector(h.h, 1, 1, esc.ctypes.c_void_p(v.data_ptr()), esc.C64, flags)
+    st = esc.lib().esc_start_vector(h.h, 1, 1, esc.ctypes.c_void_p(v.data_ptr()), edt, flags)
     assert st == 0, esc.lib().esc_last_error(h.h)
     npasses = esc.plan(esc.ConstVariables(**params))[1]
     if tuning:
@@ -362,7 +384,7 @@ def main():
     torch.cuda.synchronize()
 
     def step():
-        h.hv_device(v.data_ptr(), out.data_ptr(), esc.C64, flags)
+        h.hv_device(v.data_ptr(), out.data_ptr(), edt, flags)
 
     for _ in range(args.warmup):
         step()
@@ -380,14 +402,16 @@ def main():
     ms = ev0.elapsed_time(ev1) / args.steps
     if dist:
         ms = reduce_max(ms, dist, "cuda")
-    algo_bytes = D * 16                              # read v + write out, complex64
+    algo_bytes = D * (32 if c128 else 16)            # read v + write out
     gbs_total = replicas_gbs(algo_bytes, world, ms)
     kernel_gbs = algo_bytes / (ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
     prof = traffic_from_profile() or {}
     traffic, tsrc = None, None
     meas = prof.get("measured_bytes_per_hv", {})
-    if str(args.sites) in meas:
+    if c128:
+        pass   # the committed traffic figures are for the complex64 passes
+    elif str(args.sites) in meas:
         traffic, tsrc = int(meas[str(args.sites)]), prof.get("source")
     elif prof.get("first_pass_bytes_per_state"):
         # per-pass DRAM bytes per state measured on a smaller cluster, scaled by the states and
@@ -396,7 +420,8 @@ def main():
         tsrc = prof.get("source") + f", scaled to 2^{args.sites} states and {npasses} passes"
     roof = {"bound": "hbm", "achieved": round(kernel_gbs, 1), "peak": peak, "unit": "GB/s",
             "frac": round(kernel_gbs / peak, 4), "peak_source": peak_kind, "traffic": traffic,
-            "kernel": "complex64 tiled H.v passes (esc_jit_pass*, k_hv_pass_f32g; per-pass choice of the self-tuner)",
+            "kernel": ("complex128 tiled H.v passes (k_hv_pass_fast<double>)" if c128 else
+                       "complex64 tiled H.v passes (esc_jit_pass*, k_hv_pass_f32g; per-pass choice of the self-tuner)"),
             "passes": npasses,
             "algorithmic_bytes_per_launch": algo_bytes, "traffic_source": tsrc}
     del v, out
@@ -450,8 +475,8 @@ def main():
     if rank == 0:
         line = {"metric": METRIC, "value": round(gbs_total, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-                "config": dict(workload_config(args.sites, world), tuning=tuning),
+                "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
+                "config": dict(workload_config(args.sites, world, args.dtype), tuning=tuning),
                 "roofline": roof, "cpu_baseline": cb, "e2e": e2e, "time_to_S": tts, "clocks": clk.summary(),
                 "gpu_launches": args.steps * npasses}
         print(json.dumps(line), flush=True)

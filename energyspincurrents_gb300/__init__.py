@@ -61,7 +61,7 @@ class LanczosCfg(ctypes.Structure):
 class CFBatchCfg(ctypes.Structure):
     _fields_ = [("ncols", ctypes.c_int), ("max_steps", ctypes.c_int), ("steps", ctypes.c_void_p),
                 ("fields", ctypes.c_void_p), ("tol", ctypes.c_double), ("dtype", ctypes.c_int),
-                ("use_graph", ctypes.c_int)]
+                ("use_graph", ctypes.c_int), ("fp64_head", ctypes.c_int)]
 
 
 class DynCfg(ctypes.Structure):
@@ -75,7 +75,7 @@ _lib = None
 # every symbol declared in include/esc.h
 EXPORTS = ["esc_params_default", "esc_params_from_file", "esc_lattice", "esc_plan", "esc_create", "esc_destroy", "esc_last_error",
            "esc_num_sites", "esc_dim", "esc_neighbors", "esc_basis_permutation", "esc_stream", "esc_hv", "esc_hv_batched", "esc_apply_op",
-           "esc_start_vector", "esc_rayleigh", "esc_rayleigh_noalloc", "esc_lanczos_gs", "esc_cf_batched", "esc_spectrum", "esc_measure_local", "esc_grad", "esc_autotune", "esc_two_point"]
+           "esc_start_vector", "esc_rayleigh", "esc_rayleigh_noalloc", "esc_refine_gs", "esc_lanczos_gs", "esc_cf_batched", "esc_spectrum", "esc_measure_local", "esc_grad", "esc_autotune", "esc_two_point", "esc_alu_peaks"]
 
 
 def lib_path():
@@ -112,6 +112,7 @@ def lib():
     L.esc_start_vector.argtypes = [vp, ci, ci, vp, ci, ci]
     L.esc_rayleigh.argtypes = [vp, vp, ci, ci, P(cd)]
     L.esc_rayleigh_noalloc.argtypes = [P(Params), vp, ci, vp, P(cd)]
+    L.esc_refine_gs.argtypes = [vp, ci, P(cd), vp]
     L.esc_lanczos_gs.argtypes = [vp, P(LanczosCfg), vp, ci, P(cd), vp, vp, vp, P(ci), vp]
     L.esc_spectrum.argtypes = [vp, P(DynCfg), vp, P(ci), P(ci)]
     L.esc_cf_batched.argtypes = [vp, P(CFBatchCfg), vp, i64, ci, vp, vp, vp]
@@ -119,6 +120,7 @@ def lib():
     L.esc_grad.argtypes = [vp, P(DynCfg), vp, vp]
     L.esc_autotune.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     L.esc_two_point.argtypes = [vp, ci, ci, vp]
+    L.esc_alu_peaks.argtypes = [vp]
     _lib = L
     return L
 
@@ -308,14 +310,23 @@ class Handle:
         _check(self.h, lib().esc_rayleigh(self.h, _ptr(v), _dt(v), flags, ctypes.byref(E)))
         return E.value
 
-    def cf_batched(self, starts, max_steps, steps=None, fields=None, tol=1e-10, use_graph=True, flags=0):
-        """Batched continued-fraction Lanczos; starts (ncols, D).  Returns [(a, b)] per column."""
+    def refine_gs(self, steps=4):
+        """FP64 residual refinement of the ground state; returns (E, |H psi - E psi| before each
+        step and after the last)."""
+        E = ctypes.c_double()
+        rn = np.zeros(steps + 1)
+        _check(self.h, lib().esc_refine_gs(self.h, int(steps), ctypes.byref(E), _ptr(rn)))
+        return E.value, rn
+
+    def cf_batched(self, starts, max_steps, steps=None, fields=None, tol=1e-10, use_graph=True, flags=0, fp64_head=0):
+        """Batched continued-fraction Lanczos; starts (ncols, D).  Returns [(a, b)] per column.
+        fp64_head (complex64 starts only): leading steps run on complex128 copies of the columns."""
         V = np.ascontiguousarray(starts)
         nc = V.shape[0]
         st = None if steps is None else np.ascontiguousarray(steps, dtype=np.int32)
         fl = None if fields is None else np.ascontiguousarray(fields, dtype=np.float64)
         cfg = CFBatchCfg(nc, max_steps, _ptr(st).value if st is not None else None,
-                         _ptr(fl).value if fl is not None else None, tol, _dt(V), 1 if use_graph else 0)
+                         _ptr(fl).value if fl is not None else None, tol, _dt(V), 1 if use_graph else 0, int(fp64_head))
         a = np.zeros((nc, max_steps)); b = np.zeros((nc, max_steps + 1)); lens = np.zeros(nc, dtype=np.int32)
         _check(self.h, lib().esc_cf_batched(self.h, ctypes.byref(cfg), _ptr(V), V.shape[1], flags, _ptr(a), _ptr(b),
                                             _ptr(lens)))
@@ -367,6 +378,16 @@ class Handle:
         dS = np.zeros((omega_steps + 1, 3))
         _check(self.h, lib().esc_grad(self.h, ctypes.byref(cfg), _ptr(d), _ptr(dS)))
         return d, dS
+
+
+def alu_peaks():
+    """FP32 FMA, packed f32x2 FMA and FP64 FMA throughput of the current device (TFLOP/s) and the
+    timed kernels' durations (ms)."""
+    out = np.zeros(6)
+    st = lib().esc_alu_peaks(_ptr(out))
+    if st != ESC_OK:
+        raise EscError(st, lib().esc_last_error(None).decode())
+    return dict(ffma_tflops=out[0], ffma2_tflops=out[1], dfma_tflops=out[2], ms=out[3:].tolist())
 
 
 # ------------------------------------------------------------------------------------------------

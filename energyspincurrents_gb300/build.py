@@ -23,7 +23,7 @@ LIB = os.path.join(OUT, "libesc.so")
 EXE = os.path.join(OUT, "LanczosCond")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kernels.cu", "hv_tiled.cu", "batched.cu", "hv_jit.cu", "permute.cu"]
+CU_SOURCES = ["kernels.cu", "hv_tiled.cu", "batched.cu", "hv_jit.cu", "permute.cu", "alu_bench.cu"]
 CPP_SOURCES = ["esc_abi.cpp", "lanczos.cpp", "spectra.cpp", "grad.cpp", "tune.cpp", "params.cpp", "model.cpp", "numerics.cpp",
                "planner.cpp"]
 

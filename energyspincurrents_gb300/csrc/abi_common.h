@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -20,6 +21,7 @@ struct esc_handle {
     int N = 0;
     int64_t D = 0;
     int device = 0;
+    int cols_per_launch = esc::MAX_COLS;   // columns per multi-column H.V launch (self-tuner's choice)
     cudaStream_t stream = nullptr;
     // copy streams and per-slot events of the pipelined host-buffer batches (created on first use)
     cudaStream_t s_in = nullptr, s_out = nullptr;
@@ -132,6 +134,10 @@ struct Pipe {
 
 // lanczos.cpp
 template <typename R> void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start);
+void refine_gs(esc_handle* h, int steps, double* E, double* rnorm);
+template <typename RR>
+std::function<int(const void*, void*, const int*, double*, cudaStream_t)> hv_all_columns(
+        esc_handle* h, const std::vector<esc::DevModel>& ms, const void* dg);
 int cf_batch_width(esc_handle* h, size_t es, int want);
 template <typename R>
 void cf_batch_run(esc_handle* h, int ncols, int kmax, const std::vector<int>& steps, const std::vector<esc::DevModel>& ms,

@@ -683,6 +683,13 @@ extern "C" esc_status esc_rayleigh(esc_handle* h, const void* v, esc_dtype dt, i
     });
 }
 
+extern "C" esc_status esc_refine_gs(esc_handle* h, int steps, double* E, double* rnorm) {
+    if (!h) return finish(h, ESC_ERR_PARAM, "null argument");
+    if (!h->have_gs) return finish(h, ESC_ERR_STATE, "no ground state: call esc_lanczos_gs first");
+    if (steps < 0) return finish(h, ESC_ERR_PARAM, "steps must be >= 0");
+    return guarded(h, [&]() { refine_gs(h, steps, E, rnorm); });
+}
+
 extern "C" esc_status esc_cf_batched(esc_handle* h, const esc_cf_batch_cfg* cfg, const void* starts, int64_t ld,
                                      int flags, double* a, double* b, int* lens) {
     if (!h || !cfg || !starts) return finish(h, ESC_ERR_PARAM, "null argument");
@@ -718,7 +725,7 @@ extern "C" esc_status esc_cf_batched(esc_handle* h, const esc_cf_batch_cfg* cfg,
             for (int c = 0; c < nc; c++) ms[c] = model_with_field(h, cfg->fields[3 * c], cfg->fields[3 * c + 1], cfg->fields[3 * c + 2]);
         const double tol = cfg->tol > 0 ? cfg->tol : 1e-10;
         std::vector<std::vector<double>> A, B;
-        if (dt == ESC_C64) cf_batch_run<float>(h, nc, K, steps, ms, tol, cfg->use_graph != 0, A, B);
+        if (dt == ESC_C64) cf_batch_run<float>(h, nc, K, steps, ms, tol, cfg->use_graph != 0, A, B, std::max(0, cfg->fp64_head));
         else cf_batch_run<double>(h, nc, K, steps, ms, tol, cfg->use_graph != 0, A, B);
         for (int c = 0; c < nc; c++) {
             if (lens) lens[c] = (int)A[c].size();

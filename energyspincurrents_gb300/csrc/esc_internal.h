@@ -66,7 +66,7 @@ struct DevFields {
 struct DevCols {
     long long ld = 0;
     int ncols = 1;
-    int pad = 0;
+    int col0 = 0;            // global index of column 0 in the layout of dotp (launches over a column range)
     DevFields f{};
     double* dotp = nullptr;
 };
@@ -210,7 +210,6 @@ DevOp make_dev_op(const std::vector<OpTerm>& terms, const std::vector<int>* perm
 int red_blocks(int64_t n);
 constexpr int RED_MAX_BLOCKS = 1216;   // 8 x 152 SMs
 
-template <typename R> void launch_hv(const DevModel& m, const void* in, void* out, int64_t D, cudaStream_t s);
 template <typename R> void launch_apply(const DevOp& op, const void* in, void* out, int64_t D, cudaStream_t s);
 
 // dst (double2) = sum conj(a) b

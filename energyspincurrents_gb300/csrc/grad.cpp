@@ -21,6 +21,33 @@ void derivative_models(const esc_handle* h, esc::DevModel ms[3]) {
     }
 }
 
+// dH/dq on the tiled passes: the derivative model's terms assigned to the handle's plan (same
+// site relabelling and tiles), with its own bond diagonal.
+struct DerivOps {
+    esc_handle* h;
+    std::vector<esc::DevPass> passes[3];
+    void* diag = nullptr;       // 3 x D entries of R
+    size_t rsize = 8;
+    DerivOps(esc_handle* hh, const esc::DevModel (&dm)[3], size_t r) : h(hh), rsize(r) {
+        for (int q = 0; q < 3; q++) passes[q] = esc::make_passes(h->plan, dm[q], 0, 2, 9);
+        if (cudaMalloc(&diag, 3 * (size_t)h->D * rsize) != cudaSuccess) {
+            (void)cudaGetLastError();
+            diag = nullptr;
+            throw Fail(ESC_ERR_MEMORY, "derivative diagonals do not fit on the device");
+        }
+        for (int q = 0; q < 3; q++) {
+            if (rsize == 8) esc::launch_diag<double>(dm[q], dq(q), h->D, h->stream);
+            else esc::launch_diag<float>(dm[q], dq(q), h->D, h->stream);
+        }
+    }
+    ~DerivOps() { if (diag) cudaFree(diag); }
+    void* dq(int q) const { return (char*)diag + (size_t)q * h->D * rsize; }
+    template <typename R>
+    void hv(const esc::DevModel& m, int q, const void* in, void* out) const {
+        esc::launch_hv_tiled<R>(m, passes[q], in, out, h->D, dq(q), h->stream);
+    }
+};
+
 struct GradVecs {
     esc_handle* h;
     int64_t D;
@@ -91,9 +118,10 @@ void grad_impl(esc_handle* h, const esc_dyn_cfg* cfg, double* dE0, double* dS) {
         auto run = [&](auto tag) {
             typedef decltype(tag) R;
             ensure(h->d_work, h->work_bytes, std::max(h->work_bytes, (size_t)D * Pipe<R>::ES));
+            const DerivOps ops(h, dm, sizeof(R));
             esc::launch_dot<R>(h->d_gs, h->d_gs, D, h->d_part, h->d_sc + 8, h->stream);
             for (int q = 0; q < 3; q++) {
-                esc::launch_hv<R>(dm[q], h->d_gs, h->d_work, D, h->stream);
+                ops.hv<R>(dm[q], q, h->d_gs, h->d_work);
                 esc::launch_dot<R>(h->d_gs, h->d_work, D, h->d_part, h->d_sc + 2 * q, h->stream);
             }
             double r[10];
@@ -115,6 +143,7 @@ void grad_impl(esc_handle* h, const esc_dyn_cfg* cfg, double* dE0, double* dS) {
     // vectors: 0 gs(normalised) 1 tmp 2..4 dH_q gs -> later dgs_q, 5..7 dphi_q, CG (8..11), Lanczos
     // q_prev 12, q 13, w 14, tangents dq_prev 15..17, dq 18..20, dw 21..23
     GradVecs V(h, 24);
+    const DerivOps ops(h, dm, 8);
     void* gs = V[0];
     copyv(h, h->d_gs, gs);
     const double ngs = std::sqrt(dotc(h, gs, gs).real());
@@ -122,7 +151,7 @@ void grad_impl(esc_handle* h, const esc_dyn_cfg* cfg, double* dE0, double* dS) {
     const double E0 = h->ritz[0];
     double dE[3];
     for (int q = 0; q < 3; q++) {
-        esc::launch_hv<double>(dm[q], gs, V[2 + q], D, h->stream);
+        ops.hv<double>(dm[q], q, gs, V[2 + q]);
         dE[q] = dotc(h, gs, V[2 + q]).real();
         dE0[q] = dE[q];
     }
@@ -194,7 +223,7 @@ void grad_impl(esc_handle* h, const esc_dyn_cfg* cfg, double* dE0, double* dS) {
         double dak[3];
         for (int q = 0; q < 3; q++) {
             Hv(dqc[q], dw[q]);                       // dw = H dq + dH q
-            esc::launch_hv<double>(dm[q], qc, tmp, D, h->stream);
+            ops.hv<double>(dm[q], q, qc, tmp);
             axpby(h, dw[q], tmp, dw[q], cplx(1, 0), cplx(1, 0));
             dak[q] = (dotc(h, dqc[q], w) + dotc(h, qc, dw[q])).real();
         }

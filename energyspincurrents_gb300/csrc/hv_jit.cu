@@ -44,9 +44,9 @@ std::mutex g_mu;
 std::vector<JitEntry> g_entries;
 std::map<std::string, std::vector<int>> g_cache;   // device + source -> entry per kernel
 
-// 4096-state tiles (and 2048): 512, 256 or 128 threads; 8192-state tiles: 512 or 256 threads
+// 4096-state tiles (and 2048): 512, 256 or 128 threads; 8192-state tiles: 1024, 512 or 256 threads
 bool eligible(const DevPass& p) {
-    const bool shape = (p.Tp == 11 || p.Tp == 12) ? p.tb_bits >= 7 && p.tb_bits <= 9 : p.Tp == 13 && (p.tb_bits == 8 || p.tb_bits == 9);
+    const bool shape = (p.Tp == 11 || p.Tp == 12) ? p.tb_bits >= 7 && p.tb_bits <= 9 : p.Tp == 13 && p.tb_bits >= 8 && p.tb_bits <= 10;
     return p.c == 3 && shape && p.nterm > 0;
 }
 

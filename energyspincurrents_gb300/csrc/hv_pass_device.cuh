@@ -4,7 +4,7 @@
 // and by the kernels specialised per Hamiltonian at run time in hv_jit.cu (terms compiled in as
 // straight-line code).  It includes nothing, because it is also handed verbatim to NVRTC.
 //
-// A CTA of TB threads (512, 256 or 128: more register states per thread) owns one tile of TB E
+// A CTA of TB threads (1024, 512, 256 or 128: more register states per thread) owns one tile of TB E
 // basis states at a time: thread t holds the states t + TB j (j < E), i.e. tile-local bits
 // 0..log2(TB)-1 are thread bits and the bits above are register bits.
 // Tiles are copied global -> shared with cp.async (16 B per copy, runs of 8 consecutive states),
@@ -37,9 +37,10 @@ struct PassTab {
     unsigned char rest[40];
     int nrest, diag, accumulate, N;
     long long ld;               // column stride (states)
-    int ncols, pad;
+    int ncols;
+    int dcol0;                  // global index of column 0 in the alpha partials (launches over a column range)
     float fx[MAXC], fy[MAXC], fz[MAXC];   // Bx/2, By/2, Bz/2 per column
-    double* dotp;               // alpha partials: (re, im) at dotp[(c * gridDim.x + blockIdx.x) * 2]; NULL: none
+    double* dotp;               // alpha partials: (re, im) at dotp[((dcol0 + c) * gridDim.x + blockIdx.x) * 2]; NULL: none
 };
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -84,9 +85,9 @@ __device__ __forceinline__ int next_column(unsigned m, int c) {
 
 // Alpha epilogue accumulators: one float-float (re, im) per column and warp in shared memory.
 struct DotAcc {
-    float (*s)[16][4];   // [MAXC][warp (at most 16 of 512 threads)][hi re, lo re, hi im, lo im]
+    float (*s)[32][4];   // [MAXC][warp (at most 32 of 1024 threads)][hi re, lo re, hi im, lo im]
     __device__ __forceinline__ void clear(int tid, int nthreads) {
-        for (int i = tid; i < MAXC * 16 * 4; i += nthreads) (&s[0][0][0])[i] = 0.f;
+        for (int i = tid; i < MAXC * 32 * 4; i += nthreads) (&s[0][0][0])[i] = 0.f;
     }
     // adds the thread's (re, im) float-float sums of one column: warp butterfly, lane 0 accumulates
     __device__ __forceinline__ void add(int c, int tid, float rh, float rl, float ih, float il) {
@@ -112,8 +113,8 @@ struct DotAcc {
                 re += (double)s[tid][w][0] + (double)s[tid][w][1];
                 im += (double)s[tid][w][2] + (double)s[tid][w][3];
             }
-            p.dotp[((unsigned long long)tid * gridDim.x + blockIdx.x) * 2] = re;
-            p.dotp[((unsigned long long)tid * gridDim.x + blockIdx.x) * 2 + 1] = im;
+            p.dotp[((unsigned long long)(p.dcol0 + tid) * gridDim.x + blockIdx.x) * 2] = re;
+            p.dotp[((unsigned long long)(p.dcol0 + tid) * gridDim.x + blockIdx.x) * 2 + 1] = im;
         }
     }
 };
@@ -180,7 +181,7 @@ template <int E, int TB>
 __device__ __forceinline__ void tile_offsets(const PassTab& p, int tid, unsigned long long* hi_off,
                                              unsigned long long& lo, unsigned long long (&lo2)[2]) {
     if (tid < E) hi_off[tid] = p.tabLo[((TB * tid) >> 3) & 63] | p.tabHi[(TB * tid) >> 9];
-    lo = p.tabLo[(tid >> 3) & 63] | (unsigned long long)(tid & 7);
+    lo = p.tabLo[(tid >> 3) & 63] | p.tabHi[tid >> 9] | (unsigned long long)(tid & 7);   // tabHi: 1024 threads
     // 16-byte copies: copy c = tid + TB i moves tile states 2c and 2c+1 (runs of 8 never split);
     // (c >> 2) & 63 depends on i only for TB = 128 (through bit 5: i odd)
     lo2[0] = p.tabLo[(tid >> 2) & 63] | (unsigned long long)((2 * tid) & 7);
@@ -224,7 +225,7 @@ __device__ __forceinline__ void pass_body_staged(const PassTab& p, const Terms& 
     float2* bufs = reinterpret_cast<float2*>(smem_raw);   // 2 x (TB E) states
     float2* stage = bufs + 2 * TB * E;                     // TB E partials (or diagonal entries)
     __shared__ unsigned long long hi_off[E];
-    __shared__ float dsm[MAXC][16][4];
+    __shared__ float dsm[MAXC][32][4];
     DotAcc da{dsm};
     const int tid = threadIdx.x;
     unsigned long long lo, lo2[2];
@@ -326,7 +327,7 @@ __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* bufs = reinterpret_cast<float2*>(smem_raw);   // NS x (TB E) states
     __shared__ unsigned long long hi_off[E];
-    __shared__ float dsm[MAXC][16][4];
+    __shared__ float dsm[MAXC][32][4];
     DotAcc da{dsm};
     const int tid = threadIdx.x;
     unsigned long long lo, lo2[2];

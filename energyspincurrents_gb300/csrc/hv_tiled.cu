@@ -254,8 +254,8 @@ __global__ void __launch_bounds__(TILE_THREADS) k_hv_pass_fast(const __grid_cons
         if (tid < MAX_COLS && ((cmask >> tid) & 1u)) {
             double re = 0.0, im = 0.0;
             for (int w = 0; w < TILE_THREADS / 32; w++) { re += dsm[tid][w][0]; im += dsm[tid][w][1]; }
-            cols.dotp[((size_t)tid * gridDim.x + blockIdx.x) * 2] = re;
-            cols.dotp[((size_t)tid * gridDim.x + blockIdx.x) * 2 + 1] = im;
+            cols.dotp[((size_t)(cols.col0 + tid) * gridDim.x + blockIdx.x) * 2] = re;
+            cols.dotp[((size_t)(cols.col0 + tid) * gridDim.x + blockIdx.x) * 2 + 1] = im;
         }
     }
 }
@@ -266,7 +266,7 @@ constexpr int DOT_GRID = 608;
 template <typename R>
 __global__ void __launch_bounds__(256) k_dot_cols(const typename V2T<R>::T* __restrict__ in,
                                                   const typename V2T<R>::T* __restrict__ out, long long ld, long long D,
-                                                  const int* __restrict__ active, double* __restrict__ dotp) {
+                                                  const int* __restrict__ active, double* __restrict__ dotp, int col0) {
     const int c = blockIdx.y;
     if (active && !active[c]) return;
     double re = 0.0, im = 0.0;
@@ -286,8 +286,8 @@ __global__ void __launch_bounds__(256) k_dot_cols(const typename V2T<R>::T* __re
     if (threadIdx.x == 0) {
         double a = 0.0, b = 0.0;
         for (int w = 0; w < 8; w++) { a += sm[0][w]; b += sm[1][w]; }
-        dotp[((size_t)c * gridDim.x + blockIdx.x) * 2] = a;
-        dotp[((size_t)c * gridDim.x + blockIdx.x) * 2 + 1] = b;
+        dotp[((size_t)(col0 + c) * gridDim.x + blockIdx.x) * 2] = a;
+        dotp[((size_t)(col0 + c) * gridDim.x + blockIdx.x) * 2 + 1] = b;
     }
 }
 
@@ -524,6 +524,7 @@ escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m, const DevCols
     if (cols) {
         t.ld = cols->ld;
         t.ncols = cols->ncols;
+        t.dcol0 = cols->col0;
         for (int c = 0; c < cols->ncols; c++) {
             t.fx[c] = cols->f.fxf[c];
             t.fy[c] = cols->f.fyf[c];
@@ -650,9 +651,9 @@ template void launch_energy<double>(const DevModel&, const std::vector<DevPass>&
                                     std::vector<double>&, cudaStream_t);
 
 std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_opt, int stages, int tb_bits) {
-    if (tb_bits < 5 || tb_bits > 9) {
+    if (tb_bits < 5 || tb_bits > 10) {
         const char* e = std::getenv("ESC_TB_BITS");
-        tb_bits = e && std::atoi(e) >= 7 && std::atoi(e) <= 9 ? std::atoi(e) : 9;
+        tb_bits = e && std::atoi(e) >= 7 && std::atoi(e) <= 10 ? std::atoi(e) : 9;
     }
     const int np = (int)P.tiles.size();
     std::vector<DevPass> out(np);
@@ -934,9 +935,14 @@ int pass_stages() {
 // or 0 when no instance fits the pass's shape.
 static int run_grouped(const escdev::PassTab& pt, const DevPass& p, const void* diag, const void* in, void* out, int64_t D,
                        int sms, cudaStream_t s, const int* active) {
-    if (!(p.c == 3 && ((p.Tp == 11 || p.Tp == 12) ? p.tb_bits >= 7 && p.tb_bits <= 9 : p.Tp == 13 && p.tb_bits == 9)))
+    if (!(p.c == 3 && ((p.Tp == 11 || p.Tp == 12) ? p.tb_bits >= 7 && p.tb_bits <= 9
+                                                   : p.Tp == 13 && (p.tb_bits == 9 || p.tb_bits == 10))))
         return 0;
-    switch ((p.tb_bits == 8 ? 100 : p.tb_bits == 7 ? 200 : 0) + (p.Tp == 11 ? 10 : p.Tp == 12 ? 20 : 30) + p.stages) {
+    switch ((p.tb_bits == 8 ? 100 : p.tb_bits == 7 ? 200 : p.tb_bits == 10 ? 300 : 0) + (p.Tp == 11 ? 10 : p.Tp == 12 ? 20 : 30) +
+            p.stages) {
+        case 332: return run_f32g<8, 2, 1024>(pt, p, diag, in, out, D, sms, s, active);
+        case 333: return run_f32g<8, 3, 1024>(pt, p, diag, in, out, D, sms, s, active);
+        case 334: return run_f32g<8, 4, 1024>(pt, p, diag, in, out, D, sms, s, active);
         case 32: return run_f32g<16, 2, 512>(pt, p, diag, in, out, D, sms, s, active);
         case 33: return run_f32g<16, 3, 512>(pt, p, diag, in, out, D, sms, s, active);
         case 34: return run_f32g<16, 4, 512>(pt, p, diag, in, out, D, sms, s, active);
@@ -1022,7 +1028,8 @@ int launch_hv_cols(const DevModel& m, const DevCols& cols, const std::vector<Dev
             ESC_CUDA(cudaGetLastError());
         }
         if (dotp) {
-            k_dot_cols<R><<<dim3(DOT_GRID, cols.ncols), 256, 0, s>>>((const C*)in, (const C*)out, cols.ld, D, active, dotp);
+            k_dot_cols<R><<<dim3(DOT_GRID, cols.ncols), 256, 0, s>>>((const C*)in, (const C*)out, cols.ld, D, active, dotp,
+                                                                    cols.col0);
             ESC_CUDA(cudaGetLastError());
             G = DOT_GRID;
         }

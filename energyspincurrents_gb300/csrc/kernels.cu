@@ -45,66 +45,6 @@ int red_blocks(int64_t n) {
 }
 
 // =============================================================================================
-// H.v  (src/Hamiltonian.h:480-557 restated as a gather, coefficients computed from the bits)
-// =============================================================================================
-template <typename R>
-__global__ void __launch_bounds__(256) k_hv(const __grid_constant__ DevModel m,
-                                            const typename V2<R>::T* __restrict__ in,
-                                            typename V2<R>::T* __restrict__ out, long long D) {
-    typedef typename V2<R>::T C;
-    constexpr bool F32 = sizeof(R) == 4;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < D; k += stride) {
-        const unsigned long long uk = (unsigned long long)k;
-        R dg;
-        if constexpr (F32) {
-            float d = 0.0f;
-            for (int b = 0; b < m.nd; b++) d += (__popcll(uk & m.d[b].mask) == 1) ? -m.dqf[b] : m.dqf[b];
-            dg = fmaf(m.fzf, (float)(m.N - 2 * __popcll(uk)), d);
-        } else {
-            double d = 0.0;
-            for (int b = 0; b < m.nd; b++) {
-                const double q = 0.25 * m.d[b].dz;
-                d += (__popcll(uk & m.d[b].mask) == 1) ? -q : q;
-            }
-            // product rounded before the sum (no FMA contraction), as HDiag += Bzz*SzT does
-            dg = __dadd_rn(d, __dmul_rn(m.fz, (double)(m.N - 2 * __popcll(uk))));
-        }
-        const C v = in[k];
-        R ar = dg * v.x, ai = dg * v.y;
-        for (int b = 0; b < m.nb; b++) {
-            const unsigned long long mk = m.b[b].mask;
-            const bool df = __popcll(uk & mk) == 1;
-            R c;
-            if constexpr (F32) c = df ? m.cdifff[b] : m.ceqf[b];
-            else c = df ? m.b[b].cdiff : m.b[b].ceq;
-            const C w = in[uk ^ mk];
-            ar = fma(c, w.x, ar);
-            ai = fma(c, w.y, ai);
-        }
-        // field partners: F = sum v[k^2^s], G = sum (bit_s(k) ? +1 : -1) v[k^2^s]
-        R Fr = 0, Fi = 0, Gr = 0, Gi = 0;
-        for (int s = 0; s < m.N; s++) {
-            const C w = in[uk ^ (1ull << s)];
-            Fr += w.x; Fi += w.y;
-            if ((uk >> s) & 1ull) { Gr += w.x; Gi += w.y; } else { Gr -= w.x; Gi -= w.y; }
-        }
-        const R fx = F32 ? (R)m.fxf : (R)m.fx, fy = F32 ? (R)m.fyf : (R)m.fy;
-        ar = fma(fx, Fr, ar); ar = fma(-fy, Gi, ar);
-        ai = fma(fx, Fi, ai); ai = fma(fy, Gr, ai);
-        C o; o.x = ar; o.y = ai;
-        out[k] = o;
-    }
-}
-
-template <typename R>
-void launch_hv(const DevModel& m, const void* in, void* out, int64_t D, cudaStream_t s) {
-    typedef typename V2<R>::T C;
-    k_hv<R><<<grid_for(D, 256, SMS * 16), 256, 0, s>>>(m, (const C*)in, (C*)out, (long long)D);
-    ESC_CUDA(cudaGetLastError());
-}
-
-// =============================================================================================
 // Operator strings (src/Observables.h: single-site ops :429-521, currents :161-470, totals)
 // =============================================================================================
 template <typename R>
@@ -592,7 +532,6 @@ void launch_start_normal(uint64_t seed, void* out, int64_t n, cudaStream_t s) {
 
 // explicit instantiations
 #define ESC_INST(R)                                                                                        \
-    template void launch_hv<R>(const DevModel&, const void*, void*, int64_t, cudaStream_t);                \
     template void launch_apply<R>(const DevOp&, const void*, void*, int64_t, cudaStream_t);                \
     template void launch_dot<R>(const void*, const void*, int64_t, double*, double*, cudaStream_t);        \
     template void launch_nrm2<R>(const void*, int64_t, double*, double*, cudaStream_t);                    \

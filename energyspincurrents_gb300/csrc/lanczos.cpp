@@ -7,7 +7,8 @@
 
 namespace escabi {
 
-// Columns of a CFBatch for the model list ms (one field per column) on the handle's passes.
+// Columns of a CFBatch for the model list ms (one field per column) on the handle's passes, in
+// launches of at most h->cols_per_launch columns (the self-tuner's choice; all by default).
 template <typename RR>
 std::function<int(const void*, void*, const int*, double*, cudaStream_t)> hv_all_columns(
         esc_handle* h, const std::vector<esc::DevModel>& ms, const void* dg) {
@@ -19,10 +20,23 @@ std::function<int(const void*, void*, const int*, double*, cudaStream_t)> hv_all
         cols.f.fxf[c] = ms[c].fxf; cols.f.fyf[c] = ms[c].fyf; cols.f.fzf[c] = ms[c].fzf;
     }
     const esc::DevModel m0 = ms[0];
-    return [h, cols, m0, dg](const void* in, void* out, const int* active, double* part, cudaStream_t s) {
-        esc::DevCols c = cols;
-        c.dotp = part;
-        return esc::launch_hv_cols<RR>(m0, c, h->passes, in, out, h->D, dg, s, active);
+    const int k = std::max(1, std::min(h->cols_per_launch, esc::MAX_COLS));
+    return [h, cols, m0, dg, k](const void* in, void* out, const int* active, double* part, cudaStream_t s) {
+        int G = 0;
+        for (int c0 = 0; c0 < cols.ncols; c0 += k) {
+            esc::DevCols c = cols;
+            c.ncols = std::min(k, cols.ncols - c0);
+            c.col0 = c0;
+            for (int i = 0; i < c.ncols; i++) {
+                c.f.fx[i] = cols.f.fx[c0 + i]; c.f.fy[i] = cols.f.fy[c0 + i]; c.f.fz[i] = cols.f.fz[c0 + i];
+                c.f.fxf[i] = cols.f.fxf[c0 + i]; c.f.fyf[i] = cols.f.fyf[c0 + i]; c.f.fzf[i] = cols.f.fzf[c0 + i];
+            }
+            c.dotp = part;
+            const size_t off = (size_t)c0 * cols.ld * 2 * sizeof(RR);
+            G = esc::launch_hv_cols<RR>(m0, c, h->passes, (const char*)in + off, (char*)out + off, h->D, dg, s,
+                                        active ? active + c0 : nullptr);
+        }
+        return G;
     };
 }
 
@@ -276,6 +290,89 @@ void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) 
     sync(h);
 }
 
+// FP64 residual refinement of the handle's ground state (a complex64 ground state in particular):
+// psi in complex128; per step r = H psi - E psi with E = <psi|H psi> (tiled complex128 passes),
+// then the lowest Ritz vector of H on span{psi, r}: the 2x2 matrix [[E, |r|], [|r|, <r^|H|r^>]]
+// (<r^|H psi> = |r| since r is orthogonal to psi), with <r^|H|r^> from the FP64 energy sweep, so
+// only two complex128 vectors are held.  rnorm[s] = |r| before step s, rnorm[steps] after the last.
+// The refined vector replaces the handle's ground state (complex128 from then on; a Ritz basis no
+// longer matches it), and its energy replaces the lowest Ritz value.
+void refine_gs(esc_handle* h, int steps, double* E_out, double* rnorm) {
+    const int64_t D = h->D;
+    void* psi = nullptr;
+    void* r = nullptr;
+    // the complex64 ground state and the float diagonal make room for two complex128 vectors
+    if (h->d_diag[1]) { cudaFree(h->d_diag[1]); h->d_diag[1] = nullptr; h->diag_bytes[1] = 0; }
+    release_staging(h, 0);
+    if (cudaMalloc(&psi, (size_t)D * 16) != cudaSuccess) {
+        (void)cudaGetLastError();
+        throw Fail(ESC_ERR_MEMORY, "refinement vectors do not fit on the device");
+    }
+    if (h->basis_dt == ESC_C64) esc::launch_convert_c64_to_c128(h->d_gs, psi, D, h->stream);
+    else ESC_CUDA(cudaMemcpyAsync(psi, h->d_gs, (size_t)D * 16, cudaMemcpyDeviceToDevice, h->stream));
+    sync(h);
+    cudaFree(h->d_gs);
+    h->d_gs = nullptr;
+    h->gs_bytes = 0;
+    if (cudaMalloc(&r, (size_t)D * 16) != cudaSuccess) {
+        (void)cudaGetLastError();
+        h->d_gs = psi;   // keep the (unrefined) ground state, now complex128
+        h->gs_bytes = (size_t)D * 16;
+        h->basis_dt = ESC_C128;
+        h->have_basis = false;
+        throw Fail(ESC_ERR_MEMORY, "refinement vectors do not fit on the device");
+    }
+    ensure_partials(h, 4);
+    ensure_t(h->d_sc, h->sc_bytes, std::max(h->sc_bytes, (size_t)16 * sizeof(double)));
+    Pipe<double> P(h);
+    auto host = [&](const double* d, int n, double* out) {
+        ESC_CUDA(cudaMemcpyAsync(out, d, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        sync(h);
+    };
+    double nn[2];
+    P.nrm2(psi, h->d_sc);
+    P.scale(psi, psi, h->d_sc);
+    double E = 0.0;
+    for (int s = 0;; s++) {
+        P.hv(psi, r);                                              // r = H psi
+        P.dot(psi, r, h->d_sc);
+        host(h->d_sc, 2, nn);
+        E = nn[0];
+        esc::launch_axpby<double>(r, psi, r, cplx(1, 0), cplx(-E, 0), D, h->stream);   // r -= E psi
+        P.nrm2(r, h->d_sc);
+        host(h->d_sc, 1, nn);
+        const double rho = std::sqrt(nn[0]);
+        if (rnorm) rnorm[s] = rho;
+        if (s == steps || !(rho > 0.0)) {
+            for (int q = s + 1; rnorm && q <= steps; q++) rnorm[q] = rho;
+            break;
+        }
+        esc::launch_axpby<double>(r, r, r, cplx(1.0 / rho, 0), cplx(0, 0), D, h->stream);   // r^ = r / |r|
+        std::vector<double> hrr;
+        esc::launch_energy<double>(h->dm, h->passes, r, D, h->d_part, esc::RED_MAX_BLOCKS, hrr, h->stream);
+        // lowest eigenpair of [[E, rho], [rho, hrr]]
+        const double a = E, b = rho, c = hrr[0];
+        const double mid = 0.5 * (a + c), rad = std::hypot(0.5 * (a - c), b);
+        const double lam = mid - rad;
+        double c0 = b, c1 = lam - a;                               // (A - lam) x = 0, first row
+        if (std::fabs(c0) + std::fabs(c1) == 0.0) { c0 = 1.0; c1 = 0.0; }
+        const double nrm = std::hypot(c0, c1);
+        c0 /= nrm; c1 /= nrm;
+        if (c0 < 0) { c0 = -c0; c1 = -c1; }
+        esc::launch_axpby<double>(psi, r, psi, cplx(c0, 0), cplx(c1, 0), D, h->stream);
+        P.nrm2(psi, h->d_sc);
+        P.scale(psi, psi, h->d_sc);
+    }
+    cudaFree(r);
+    h->d_gs = psi;
+    h->gs_bytes = (size_t)D * 16;
+    h->basis_dt = ESC_C128;
+    h->have_basis = false;
+    if (!h->ritz.empty()) h->ritz[0] = E;
+    if (E_out) *E_out = E;
+    sync(h);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Batched continued-fraction Lanczos (batched.cu)
 // ---------------------------------------------------------------------------------------------
@@ -382,6 +479,10 @@ void cf_batch_run(esc_handle* h, int ncols, int kmax, const std::vector<int>& st
     }
 }
 
+template std::function<int(const void*, void*, const int*, double*, cudaStream_t)> hv_all_columns<float>(
+        esc_handle*, const std::vector<esc::DevModel>&, const void*);
+template std::function<int(const void*, void*, const int*, double*, cudaStream_t)> hv_all_columns<double>(
+        esc_handle*, const std::vector<esc::DevModel>&, const void*);
 template void lanczos_gs<float>(esc_handle*, const esc_lanczos_cfg&, const void*);
 template void lanczos_gs<double>(esc_handle*, const esc_lanczos_cfg&, const void*);
 template void cf_batch_run<float>(esc_handle*, int, int, const std::vector<int>&, const std::vector<esc::DevModel>&, double,

@@ -31,7 +31,7 @@ void save_tuning(const esc_handle* h, int T, int balance, const std::vector<esc:
     if (!fp) return;
     std::fprintf(fp, "%s | %d %d %d |", tune_key(h).c_str(), T, balance, (int)ps.size());
     for (const auto& p : ps) std::fprintf(fp, " %d,%d,%d", p.jit >= 0 ? 1 : 0, p.stages, p.tb_bits);
-    std::fprintf(fp, "\n");
+    std::fprintf(fp, " | %d\n", h->cols_per_launch);
     std::fclose(fp);
 }
 
@@ -60,6 +60,8 @@ bool load_tuning(esc_handle* h) {
         in >> v[0] >> c1 >> v[1] >> c2 >> v[2];
     }
     if (!in || T < 4) return false;
+    int k = 0;
+    if (in >> bar >> k && bar == '|' && k >= 1 && k <= esc::MAX_COLS) h->cols_per_launch = k;
     const esc::Plan plan = esc::make_plan(h->N, bond_pairs(h), T, 3, 200);
     if ((int)plan.tiles.size() != n) return false;
     install_plan(h, plan, balance, 2);
@@ -82,11 +84,65 @@ bool load_tuning(esc_handle* h) {
     return true;
 }
 
+// Columns per launch of the multi-column H.V (batched recurrences): the installed passes applied
+// to nb complex64 columns (as many as fit, at most 16) in launches of k = 1, 2, 4, ... columns; the
+// k with the lowest time per column is kept (h->cols_per_launch).
+std::string tune_columns(esc_handle* h) {
+    const int64_t D = h->D;
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { (void)cudaGetLastError(); return ""; }
+    const size_t per = (size_t)D * 16;   // one complex64 column in and out
+    const int nb = (int)std::min<size_t>(esc::MAX_COLS, fr > ((size_t)2 << 30) ? (fr - ((size_t)2 << 30)) / per : 0);
+    if (nb < 2) return "columns: not timed (fewer than two columns fit)\n";
+    void* buf = nullptr;
+    ESC_CUDA(cudaMalloc(&buf, (size_t)nb * per));
+    char* in = (char*)buf;
+    char* out = in + (size_t)nb * D * 8;
+    esc::launch_start_normal<float>(777, in, (int64_t)nb * D, h->stream);
+    const void* dg = diag_for(h, ESC_C64);
+    std::vector<esc::DevModel> ms(nb, h->dm);
+    cudaEvent_t e0, e1;
+    ESC_CUDA(cudaEventCreate(&e0));
+    ESC_CUDA(cudaEventCreate(&e1));
+    std::ostringstream rep;
+    rep << "columns (" << nb << " complex64 columns):";
+    std::vector<std::pair<int, double>> tk;
+    for (int k = 1; k <= nb; k *= 2) {
+        h->cols_per_launch = k;
+        auto f = hv_all_columns<float>(h, ms, dg);
+        f(in, out, nullptr, nullptr, h->stream);
+        std::vector<float> ms3(3);
+        for (float& x : ms3) {
+            ESC_CUDA(cudaEventRecord(e0, h->stream));
+            f(in, out, nullptr, nullptr, h->stream);
+            ESC_CUDA(cudaEventRecord(e1, h->stream));
+            ESC_CUDA(cudaEventSynchronize(e1));
+            ESC_CUDA(cudaEventElapsedTime(&x, e0, e1));
+        }
+        std::sort(ms3.begin(), ms3.end());
+        const double pc = ms3[1] / nb;
+        rep << " k=" << k << " " << pc << " ms/column";
+        tk.push_back({k, pc});
+    }
+    rep << "\n";
+    // the most columns per launch whose time per column is within 0.5 % of the fastest (fewer launches)
+    double best = 1e300;
+    for (auto& x : tk) best = std::min(best, x.second);
+    int bk = 1;
+    for (auto& x : tk)
+        if (x.second <= best * 1.005) bk = x.first;
+    h->cols_per_launch = bk >= nb ? esc::MAX_COLS : bk;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    return rep.str();
+}
+
 // Self-tuning of the complex64 H.v.  Plans: tile bits T in {11, 12, 13} (above 26 sites 12 and 13:
 // 11 needs one pass more there) x first-fit / group-minimising
 // term-to-pass assignment (make_passes modes 0 and 2; the balanced mode 1 never won).  Kernel variants per plan: ahead-of-time vs run-time specialised;
-// 512, 256 or 128 threads per 4096-state tile (8, 16, 32 register states each), 512 or 256 (the
-// latter specialised only) per 8192-state tile (16, 32); 2 or 3 tile buffers, or 2 plus staged
+// 512, 256 or 128 threads per 4096-state tile (8, 16, 32 register states each), 1024, 512 or 256
+// (the latter specialised only) per 8192-state tile (8, 16, 32); 2 or 3 tile buffers, or 2 plus staged
 // epilogue loads.  Every variant is timed pass by pass (CUDA events on the
 // handle's stream, median of 3 after a warm-up); a plan's composite takes the fastest variant of
 // each pass (light and heavy passes prefer different variants) and is timed as a whole; the
@@ -132,10 +188,12 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
             for (int balance : {0, 2}) {
                 std::vector<std::vector<esc::DevPass>> vars;
                 std::vector<std::vector<double>> per;
-                for (int tb : {9, 8, 7})
+                for (int tb : {10, 9, 8, 7})
                 for (int stages : {2, 3, 4})
                     for (int jit : {0, 1}) {
-                        if (T == 13 && (tb == 7 || (tb == 8 && !jit))) continue;   // 8192-state tiles: 512 threads, or 256 specialised
+                        // 8192-state tiles: 1024 or 512 threads, or 256 specialised; 4096: 512 / 256 / 128
+                        if (T == 13 && (tb == 7 || (tb == 8 && !jit))) continue;
+                        if (T != 13 && tb == 10) continue;
                         install_plan(h, plan, balance, stages, tb);
                         if (jit) specialise(h, h->passes, 1);
                         bool spec = false;
@@ -181,10 +239,11 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
     cudaFree(buf);
     install_plan(h, bplan, bbal, 2);
     h->passes = bpasses;
+    rep << tune_columns(h);
     save_tuning(h, bT, bbal, bpasses);
     rep << "chosen: T=" << bT << " balance=" << bbal << " passes:";
     for (const auto& ps : bpasses) rep << " " << (ps.jit >= 0 ? "jit" : "aot") << "/" << ps.stages << "/" << (1 << ps.tb_bits);
-    rep << " (" << best << " ms)\n";
+    rep << " columns per launch " << h->cols_per_launch << " (" << best << " ms)\n";
     return rep.str();
 }
 

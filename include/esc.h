@@ -130,6 +130,8 @@ typedef struct {
     double tol;             /* a column stops when beta_k < tol * |phi|  (<= 0: 1e-10)           */
     esc_dtype dtype;        /* storage/arithmetic of the recurrence vectors                      */
     int use_graph;          /* 1: one iteration captured in a CUDA graph and replayed            */
+    int fp64_head;          /* ESC_C64 only: the first fp64_head steps run on complex128 copies   *
+                             * of the columns before the complex64 tail (0: none)                 */
 } esc_cf_batch_cfg;
 
 typedef struct esc_handle esc_handle;
@@ -223,6 +225,15 @@ esc_status esc_rayleigh(esc_handle* h, const void* v, esc_dtype dt, int flags, d
  *     written by the same call, so nothing has to be cleared between calls. */
 esc_status esc_rayleigh_noalloc(const esc_params* p, const void* v, esc_dtype dt, void* stream, double* E);
 
+/* FP64 residual refinement of the handle's ground state (extension; no reference counterpart),
+ * for ground states from a complex64 Lanczos run.  Each of `steps` steps evaluates r = H psi - E psi
+ * in FP64 (E = <psi|H|psi>, complex128 tiled passes) and replaces psi by the lowest Ritz vector of
+ * H on span{psi, r}.  rnorm (may be NULL, steps+1 entries) receives |r| before each step and after
+ * the last; E (may be NULL) the final <psi|H|psi>.  The refined vector becomes the handle's ground
+ * state (complex128; esc_spectrum in CF mode starts from it; Ritz mode needs a new Lanczos run).
+ * Needs two complex128 vectors of device memory. */
+esc_status esc_refine_gs(esc_handle* h, int steps, double* E, double* rnorm);
+
 /* ---- solvers ----------------------------------------------------------------------------------- */
 
 /* Ground-state Lanczos.  Replaces DynLanczosSolver::Lanczos_Nirav (src/DynLanczosSolver.h:38-239)
@@ -276,6 +287,13 @@ esc_status esc_autotune(esc_handle* h, char* report, size_t report_len);
  * spectrum of `kind`, by reverse mode through the continued fraction and the dynamical Lanczos
  * recurrence (vectors recomputed, not stored). */
 esc_status esc_grad(esc_handle* h, const esc_dyn_cfg* cfg, double* dE0, double* dS);
+
+/* ---- diagnostics ------------------------------------------------------------------------------- */
+
+/* Arithmetic ceilings of the current device (no reference counterpart): out[0..2] = FP32 FMA,
+ * packed f32x2 FMA and FP64 FMA throughput in TFLOP/s (an FMA counts 2 flops, a packed FMA 4),
+ * out[3..5] = the timed kernels' durations in ms.  About three seconds of device time. */
+esc_status esc_alu_peaks(double* out);
 
 #ifdef __cplusplus
 }
