@@ -171,7 +171,7 @@ void grad_impl(esc_handle* h, const esc_dyn_cfg* cfg, double* dE0, double* dS) {
         copyv(h, r, p);
         double rr = dotc(h, r, r).real();
         const double rr0 = rr;
-        for (int it = 0; it < 3000 && rr > 1e-26 * rr0; it++) {
+        for (int it = 0; it < 20000 && rr > 1e-26 * rr0; it++) {
             Hv(p, Ap);
             axpby(h, Ap, p, Ap, cplx(1, 0), cplx(-E0, 0));
             project(Ap);

@@ -291,17 +291,21 @@ void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) 
 }
 
 // FP64 residual refinement of the handle's ground state (a complex64 ground state in particular):
-// psi in complex128; per step r = H psi - E psi with E = <psi|H psi> (tiled complex128 passes),
-// then the lowest Ritz vector of H on span{psi, r}: the 2x2 matrix [[E, |r|], [|r|, <r^|H|r^>]]
-// (<r^|H psi> = |r| since r is orthogonal to psi), with <r^|H|r^> from the FP64 energy sweep, so
-// only two complex128 vectors are held.  rnorm[s] = |r| before step s, rnorm[steps] after the last.
-// The refined vector replaces the handle's ground state (complex128 from then on; a Ritz basis no
-// longer matches it), and its energy replaces the lowest Ritz value.
+// locally optimal conjugate-gradient steps (LOBPCG with one vector) in FP64.  Per step, with psi
+// normalised: r = H psi - E psi, E = <psi|H psi> (tiled complex128 passes); p = the previous update
+// direction, orthonormalised against psi and r^ = r/|r|; psi <- lowest Ritz vector of H on
+// span{psi, r^, p^}.  In that basis <r^|H psi> = |r| and <p^|H psi> = 0, and <r^|H r^>, <p^|H p^> and
+// the cross term <r^|H p^> (by polarisation, from r^ + p^ and r^ + i p^) come from the FP64 energy
+// sweep, which forms no H v: three complex128 vectors in all.  A phase on p^ makes the 3x3 matrix
+// real tridiagonal.  rnorm[s] = |r| before step s, rnorm[steps] after the last.  The refined vector
+// replaces the handle's ground state (complex128 from then on; a Ritz basis no longer matches it)
+// and its energy the lowest Ritz value.
 void refine_gs(esc_handle* h, int steps, double* E_out, double* rnorm) {
     const int64_t D = h->D;
     void* psi = nullptr;
     void* r = nullptr;
-    // the complex64 ground state and the float diagonal make room for two complex128 vectors
+    void* p = nullptr;
+    // the complex64 ground state and the float diagonal make room for three complex128 vectors
     if (h->d_diag[1]) { cudaFree(h->d_diag[1]); h->d_diag[1] = nullptr; h->diag_bytes[1] = 0; }
     release_staging(h, 0);
     if (cudaMalloc(&psi, (size_t)D * 16) != cudaSuccess) {
@@ -312,62 +316,91 @@ void refine_gs(esc_handle* h, int steps, double* E_out, double* rnorm) {
     else ESC_CUDA(cudaMemcpyAsync(psi, h->d_gs, (size_t)D * 16, cudaMemcpyDeviceToDevice, h->stream));
     sync(h);
     cudaFree(h->d_gs);
-    h->d_gs = nullptr;
-    h->gs_bytes = 0;
-    if (cudaMalloc(&r, (size_t)D * 16) != cudaSuccess) {
+    h->d_gs = psi;   // from here on the ground state is complex128 (refined in place)
+    h->gs_bytes = (size_t)D * 16;
+    h->basis_dt = ESC_C128;
+    h->have_basis = false;
+    if (cudaMalloc(&r, (size_t)D * 16) != cudaSuccess || cudaMalloc(&p, (size_t)D * 16) != cudaSuccess) {
         (void)cudaGetLastError();
-        h->d_gs = psi;   // keep the (unrefined) ground state, now complex128
-        h->gs_bytes = (size_t)D * 16;
-        h->basis_dt = ESC_C128;
-        h->have_basis = false;
+        if (r) cudaFree(r);
         throw Fail(ESC_ERR_MEMORY, "refinement vectors do not fit on the device");
     }
+    struct Free {
+        void* a;
+        void* b;
+        ~Free() { cudaFree(a); cudaFree(b); }
+    } guard{r, p};
     ensure_partials(h, 4);
     ensure_t(h->d_sc, h->sc_bytes, std::max(h->sc_bytes, (size_t)16 * sizeof(double)));
     Pipe<double> P(h);
-    auto host = [&](const double* d, int n, double* out) {
-        ESC_CUDA(cudaMemcpyAsync(out, d, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    auto dot = [&](const void* a, const void* b) {
+        double v[2];
+        P.dot(a, b, h->d_sc);
+        ESC_CUDA(cudaMemcpyAsync(v, h->d_sc, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
         sync(h);
+        return cplx(v[0], v[1]);
     };
-    double nn[2];
-    P.nrm2(psi, h->d_sc);
-    P.scale(psi, psi, h->d_sc);
+    auto axpby = [&](const void* x, const void* y, void* out, cplx a, cplx b) {
+        esc::launch_axpby<double>(x, y, out, a, b, D, h->stream);
+    };
+    auto sweep = [&](const void* v) {     // <v|H|v> in FP64, no H v formed
+        std::vector<double> e;
+        esc::launch_energy<double>(h->dm, h->passes, v, D, h->d_part, esc::RED_MAX_BLOCKS, e, h->stream);
+        return e[0];
+    };
+    axpby(psi, psi, psi, cplx(1.0 / std::sqrt(dot(psi, psi).real()), 0), cplx(0, 0));
     double E = 0.0;
+    bool have_p = false;
     for (int s = 0;; s++) {
         P.hv(psi, r);                                              // r = H psi
-        P.dot(psi, r, h->d_sc);
-        host(h->d_sc, 2, nn);
-        E = nn[0];
-        esc::launch_axpby<double>(r, psi, r, cplx(1, 0), cplx(-E, 0), D, h->stream);   // r -= E psi
-        P.nrm2(r, h->d_sc);
-        host(h->d_sc, 1, nn);
-        const double rho = std::sqrt(nn[0]);
+        E = dot(psi, r).real();
+        axpby(r, psi, r, cplx(1, 0), cplx(-E, 0));                 // r -= E psi
+        const double rho = std::sqrt(dot(r, r).real());
         if (rnorm) rnorm[s] = rho;
         if (s == steps || !(rho > 0.0)) {
             for (int q = s + 1; rnorm && q <= steps; q++) rnorm[q] = rho;
             break;
         }
-        esc::launch_axpby<double>(r, r, r, cplx(1.0 / rho, 0), cplx(0, 0), D, h->stream);   // r^ = r / |r|
-        std::vector<double> hrr;
-        esc::launch_energy<double>(h->dm, h->passes, r, D, h->d_part, esc::RED_MAX_BLOCKS, hrr, h->stream);
-        // lowest eigenpair of [[E, rho], [rho, hrr]]
-        const double a = E, b = rho, c = hrr[0];
-        const double mid = 0.5 * (a + c), rad = std::hypot(0.5 * (a - c), b);
-        const double lam = mid - rad;
-        double c0 = b, c1 = lam - a;                               // (A - lam) x = 0, first row
-        if (std::fabs(c0) + std::fabs(c1) == 0.0) { c0 = 1.0; c1 = 0.0; }
-        const double nrm = std::hypot(c0, c1);
-        c0 /= nrm; c1 /= nrm;
-        if (c0 < 0) { c0 = -c0; c1 = -c1; }
-        esc::launch_axpby<double>(psi, r, psi, cplx(c0, 0), cplx(c1, 0), D, h->stream);
-        P.nrm2(psi, h->d_sc);
-        P.scale(psi, psi, h->d_sc);
+        axpby(r, psi, r, cplx(1.0 / rho, 0), cplx(0, 0));          // r^
+        axpby(r, psi, r, cplx(1, 0), -dot(psi, r));                // re-orthogonalise against psi
+        axpby(r, psi, r, cplx(1.0 / std::sqrt(dot(r, r).real()), 0), cplx(0, 0));
+        const double h22 = sweep(r);
+        double h33 = 0.0, h23 = 0.0;
+        cplx ph(1, 0);
+        if (have_p) {
+            axpby(p, psi, p, cplx(1, 0), -dot(psi, p));            // p^ orthonormal to psi and r^
+            axpby(p, r, p, cplx(1, 0), -dot(r, p));
+            const double np = std::sqrt(dot(p, p).real());
+            have_p = np > 1e-14;
+            if (have_p) {
+                axpby(p, r, p, cplx(1.0 / np, 0), cplx(0, 0));
+                h33 = sweep(p);
+                axpby(p, r, p, cplx(1, 0), cplx(1, 0));            // r^ + p^
+                const double s1 = sweep(p);
+                axpby(p, r, p, cplx(0, 1), cplx(0, -1));           // i (r^ + p^) - i r^ = i p^ ... then + r^
+                axpby(p, r, p, cplx(1, 0), cplx(1, 0));            // r^ + i p^
+                const double s2 = sweep(p);
+                axpby(p, r, p, cplx(0, -1), cplx(0, 1));           // -i (r^ + i p^) + i r^ = p^
+                const cplx c23(0.5 * (s1 - h22 - h33), -0.5 * (s2 - h22 - h33));   // <r^|H p^>
+                h23 = std::abs(c23);
+                ph = h23 > 0.0 ? std::conj(c23) / h23 : cplx(1, 0);   // <r^|H (ph p^)> = |c23|
+            }
+        }
+        // lowest Ritz pair of the real tridiagonal [[E, rho, 0], [rho, h22, h23], [0, h23, h33]]
+        const int n = have_p ? 3 : 2;
+        std::vector<double> d{E, h22, h33}, e{rho, h23, 0.0}, Z;
+        d.resize(n);
+        e.resize(n);
+        if (!esc::tridiag_eig(n, d, e, &Z)) throw Fail(ESC_ERR_NUMERIC, "refinement: 3x3 eigensolver failed");
+        double z1 = Z[0], z2 = Z[1], z3 = n == 3 ? Z[2] : 0.0;
+        if (z1 < 0) { z1 = -z1; z2 = -z2; z3 = -z3; }
+        // new direction p = z2 r^ + z3 ph p^, then psi <- z1 psi + p
+        if (have_p) axpby(p, r, p, z3 * ph, cplx(z2, 0));
+        else axpby(r, r, p, cplx(z2, 0), cplx(0, 0));
+        axpby(psi, p, psi, cplx(z1, 0), cplx(1, 0));
+        axpby(psi, psi, psi, cplx(1.0 / std::sqrt(dot(psi, psi).real()), 0), cplx(0, 0));
+        have_p = true;
     }
-    cudaFree(r);
-    h->d_gs = psi;
-    h->gs_bytes = (size_t)D * 16;
-    h->basis_dt = ESC_C128;
-    h->have_basis = false;
     if (!h->ritz.empty()) h->ritz[0] = E;
     if (E_out) *E_out = E;
     sync(h);

@@ -93,7 +93,7 @@ CF_STEPS, NW, DW, ETA = 48, 500, 6.0 / 499, 0.05
 def tt_spectrum(theta, Lx, Ly, kind="Energy Current", want_grad=False):
     K, J, hf = (float(x) for x in theta)
     b = -hf / S3
-    hh = esc.Handle(dict(Lx=Lx, Ly=Ly, Kxx=K, Kyy=K, Kzz=K, Bxx=b, Byy=b, Bzz=b, jheis=J, lanczos_steps=200))
+    hh = esc.Handle(dict(Lx=Lx, Ly=Ly, Kxx=K, Kyy=K, Kzz=K, Bxx=b, Byy=b, Bzz=b, jheis=J, lanczos_steps=400))
     r = hh.lanczos_gs(start=_start(hh.D), lanctype="GS")   # the same start vector at every parameter point
     col = 5 if kind == "Energy Current" else 14
     S = hh.spectrum(kind, "CF", omega_steps=NW - 1, domega=DW, eta=ETA, cf_steps=CF_STEPS)[:, col]
@@ -167,6 +167,7 @@ def test_c5_gradients_18_sites_16_samples():
         g, fd = check_against_fd(theta, 3, 6, kind, weights)
         err = np.abs(g - fd).max() / max(1.0, np.abs(fd).max())
         worst = max(worst, err)
+        print(f"  sample {i} K={theta[0]:.4f} J={theta[1]:.4f} h={theta[2]:.4f} {kind}: relative error {err:.1e}")
         assert err <= 1e-5, (i, theta, g, fd)
     print(f"C5 (18 sites, 16 samples): max relative |adjoint - central difference| = {worst:.1e}")
 
@@ -190,10 +191,11 @@ def test_refine_gs_reduces_fp64_residual():
         h.refine_gs(2)
     ref = esc.Handle(p).lanczos_gs(steps=200, lanctype="GS", reortho=0)            # FP64 run
     r32 = h.lanczos_gs(steps=200, lanctype="GS", reortho=0, dtype=np.complex64)
-    E, rn = h.refine_gs(steps=6)
+    E, rn = h.refine_gs(steps=12)
     print(f"refinement (18 sites): |H psi - E psi| {' -> '.join(f'{x:.2e}' for x in rn)}; "
           f"E0 complex64 Lanczos {r32['E0']:.15f}, refined {E:.15f}, FP64 Lanczos {ref['E0']:.15f}")
-    assert rn[-1] < rn[0] and np.all(np.diff(rn) <= 1e-15)
+    # locally optimal steps minimise the Rayleigh quotient (the residual need not fall every step)
+    assert rn[-1] < 0.1 * rn[0]
     assert abs(E - ref["E0"]) <= 1e-10 * abs(ref["E0"])
     assert abs(h.rayleigh() - E) <= 1e-12 * abs(E)          # the refined vector is the handle's ground state
     # the spectra start from it (CF mode, complex64 vectors from the FP64 ground state)
