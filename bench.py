@@ -254,6 +254,83 @@ def lanczos_step_report(esc, sites, steps=24):
             "step_over_hv": round(step_ms / hv_ms, 3), "tuning": tune}
 
 
+def refine_report(esc, sites, gs_steps=300, refine_steps=20):
+    """FP64 residual refinement of a complex64 ground state: |H psi - E psi| (FP64) before and after
+    refinement steps, the energies, and the times."""
+    import numpy as np
+    h = esc.Handle(workload(sites))
+    h.autotune()
+    t0 = time.perf_counter()
+    r = h.lanczos_gs(steps=gs_steps, lanctype="GS", reortho=0, dtype=np.complex64, want_gs=False)
+    t1 = time.perf_counter()
+    e_ray = h.rayleigh()
+    t2 = time.perf_counter()
+    E, rn = h.refine_gs(refine_steps)
+    t3 = time.perf_counter()
+    h.close()
+    return {"sites": sites, "gs_steps": gs_steps, "E0_lanczos_c64": r["E0"], "E0_rayleigh_fp64": e_ray,
+            "E0_refined": E, "refine_steps": refine_steps, "residual": [float(x) for x in rn],
+            "lanczos_s": round(t1 - t0, 2), "rayleigh_s": round(t2 - t1, 2), "refine_s": round(t3 - t2, 2)}
+
+
+def c3_report(esc, gs_steps=300, cf_steps=1000, refine_steps=10):
+    """Mixed precision against FP64 for the 32-site workload (K=-1, J=0.05, h=0.02 [111], seed 1):
+    on the 28-site cluster (7x2 unit cells) both run -- FP64 ground state and FP64 continued
+    fractions against the complex64 ground state (FP64 Rayleigh value, FP64 refinement) and complex64
+    continued fractions -- and the E0 and S(omega) differences are reported; on the 32-site cluster
+    FP64 does not fit (a complex128 vector is 68.7 GB), and the mixed E0, the FP64 residual of the
+    refined ground state and the spectrum are reported.  JeJe spectra, 2000 omega in [0, 6],
+    eta = 0.05."""
+    import numpy as np
+    out = {"cf_steps": cf_steps, "gs_steps": gs_steps, "omega": "2000 points in [0,6]", "eta": 0.05}
+    kw = dict(omega_steps=1999, domega=6.0 / 1999, eta=0.05)
+    # 28 sites, FP64
+    h = esc.Handle(esc.ConstVariables(**workload(28), **kw))
+    h.autotune()
+    t0 = time.perf_counter()
+    r64 = h.lanczos_gs(steps=gs_steps, lanctype="GS", reortho=0, want_gs=False)
+    t1 = time.perf_counter()
+    S64 = h.spectrum("Energy Current", "CF", cf_steps=cf_steps)
+    t2 = time.perf_counter()
+    h.close()
+    # 28 sites, mixed
+    h = esc.Handle(esc.ConstVariables(**workload(28), **kw))
+    h.autotune()
+    t3 = time.perf_counter()
+    r32 = h.lanczos_gs(steps=gs_steps, lanctype="GS", reortho=0, dtype=np.complex64, want_gs=False)
+    e_ray = h.rayleigh()
+    E_ref, rn = h.refine_gs(refine_steps)
+    t4 = time.perf_counter()
+    S32 = h.spectrum("Energy Current", "CF", cf_steps=cf_steps, dtype=np.complex64)
+    t5 = time.perf_counter()
+    h.close()
+    e64 = r64["E0"]
+    out["n28"] = {"E0_fp64": e64, "E0_c64_lanczos": r32["E0"], "E0_c64_rayleigh_fp64": e_ray, "E0_refined": E_ref,
+                  "relerr_E0_c64_lanczos": abs(r32["E0"] - e64) / abs(e64),
+                  "relerr_E0_rayleigh": abs(e_ray - e64) / abs(e64), "relerr_E0_refined": abs(E_ref - e64) / abs(e64),
+                  "refine_residual": [float(rn[0]), float(rn[-1])],
+                  "max_abs_dS": float(np.abs(S32[:, 1:] - S64[:, 1:]).max()), "max_abs_S": float(np.abs(S64[:, 1:]).max()),
+                  "fp64_gs_s": round(t1 - t0, 1), "fp64_S_s": round(t2 - t1, 1), "mixed_gs_s": round(t4 - t3, 1),
+                  "mixed_S_s": round(t5 - t4, 1)}
+    # 32 sites, mixed only
+    h = esc.Handle(esc.ConstVariables(**workload(32), **kw))
+    h.autotune()
+    t6 = time.perf_counter()
+    r = h.lanczos_gs(steps=gs_steps, lanctype="GS", reortho=0, dtype=np.complex64, want_gs=False)
+    e_ray = h.rayleigh()
+    E_ref, rn = h.refine_gs(refine_steps)
+    t7 = time.perf_counter()
+    S = h.spectrum("Energy Current", "CF", cf_steps=cf_steps // 2, dtype=np.complex64)
+    t8 = time.perf_counter()
+    h.close()
+    out["n32"] = {"E0_c64_lanczos": r["E0"], "E0_c64_rayleigh_fp64": e_ray, "E0_refined": E_ref,
+                  "E0_per_site": E_ref / 32, "refine_residual": [float(rn[0]), float(rn[-1])],
+                  "cf_steps": cf_steps // 2, "max_abs_S": float(np.abs(S[:, 1:]).max()),
+                  "omega_at_max_tt": float(S[np.abs(S[:, 5]).argmax(), 0]),
+                  "gs_and_refine_s": round(t7 - t6, 1), "time_to_S_s": round(t8 - t7, 1)}
+    return out
+
+
 def reduce_max(x, dist, device):
     """Max over the ranks of a per-rank time (the slowest replica sets the job's time)."""
     import torch
@@ -314,6 +391,10 @@ def main():
                          "FP64 Rayleigh refinement) and print one JSON line, then exit")
     ap.add_argument("--alu-report", action="store_true",
                     help="measure the FP32 / packed FP32 / FP64 FMA ceilings of the GPU (clocks sampled) and print one JSON line")
+    ap.add_argument("--refine-report", action="store_true",
+                    help="FP64 residual refinement of a complex64 ground state of --sites; print one JSON line")
+    ap.add_argument("--c3-report", action="store_true",
+                    help="mixed precision against FP64 at 28 sites and the mixed 32-site run; print one JSON line")
     ap.add_argument("--step-report", action="store_true",
                     help="time one complex64 Lanczos step of the --sites cluster against one H.v and print one JSON line")
     ap.add_argument("--autotune-report", action="store_true",
@@ -351,6 +432,12 @@ def main():
         return
     if args.step_report:
         print(json.dumps(lanczos_step_report(esc, args.sites)), flush=True)
+        return
+    if args.refine_report:
+        print(json.dumps(refine_report(esc, args.sites)), flush=True)
+        return
+    if args.c3_report:
+        print(json.dumps(c3_report(esc)), flush=True)
         return
     if args.tts_report:
         print(json.dumps(mixed_spectrum_report(esc, args.sites)), flush=True)

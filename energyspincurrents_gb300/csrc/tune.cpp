@@ -84,6 +84,45 @@ bool load_tuning(esc_handle* h) {
     return true;
 }
 
+// The installed composite against the plan's ahead-of-time 512-thread kernel on one complex64
+// vector: a tuned configuration must compute the same H.v (to complex64 rounding).  On a mismatch
+// the handle returns to the plan and passes it had before tuning, and the report says so.
+std::string verify_composite(esc_handle* h, const esc::Plan& plan, int balance, const esc::Plan& keep,
+                             const std::vector<esc::DevPass>& keep_passes) {
+    const int64_t D = h->D;
+    void* buf = nullptr;
+    ESC_CUDA(cudaMalloc(&buf, (size_t)D * 24));
+    char* v = (char*)buf;
+    char* a = v + (size_t)D * 8;
+    char* b = a + (size_t)D * 8;
+    esc::launch_start_normal<float>(4242, v, D, h->stream);
+    const void* dg = diag_for(h, ESC_C64);
+    const std::vector<esc::DevPass> ref = esc::make_passes(plan, h->dm, balance, 2, 9);
+    esc::launch_hv_tiled<float>(h->dm, h->passes, v, a, D, dg, h->stream);
+    esc::launch_hv_tiled<float>(h->dm, ref, v, b, D, dg, h->stream);
+    std::vector<float> x((size_t)D * 2), y((size_t)D * 2);
+    ESC_CUDA(cudaMemcpyAsync(x.data(), a, (size_t)D * 8, cudaMemcpyDeviceToHost, h->stream));
+    ESC_CUDA(cudaMemcpyAsync(y.data(), b, (size_t)D * 8, cudaMemcpyDeviceToHost, h->stream));
+    sync(h);
+    cudaFree(buf);
+    double dmax = 0.0, ymax = 0.0;
+    for (size_t i = 0; i < x.size(); i++) {
+        dmax = std::max(dmax, (double)std::fabs(x[i] - y[i]));
+        ymax = std::max(ymax, (double)std::fabs(y[i]));
+    }
+    const double rel = dmax / std::max(ymax, 1e-300);
+    std::ostringstream o;
+    if (!(rel <= 1e-5)) {
+        install_plan(h, keep, -1, 0);
+        h->passes = keep_passes;
+        o << "verification FAILED (relative difference " << rel << " against the ahead-of-time kernel): the "
+          << "configuration before tuning is kept\n";
+    } else {
+        o << "verified against the ahead-of-time kernel: relative difference " << rel << "\n";
+    }
+    return o.str();
+}
+
 // Columns per launch of the multi-column H.V (batched recurrences): the installed passes applied
 // to nb complex64 columns (as many as fit, at most 16) in launches of k = 1, 2, 4, ... columns; the
 // k with the lowest time per column is kept (h->cols_per_launch).
@@ -239,6 +278,7 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
     cudaFree(buf);
     install_plan(h, bplan, bbal, 2);
     h->passes = bpasses;
+    rep << verify_composite(h, bplan, bbal, keep, keep_passes);
     rep << tune_columns(h);
     save_tuning(h, bT, bbal, bpasses);
     rep << "chosen: T=" << bT << " balance=" << bbal << " passes:";

@@ -191,7 +191,7 @@ def test_refine_gs_reduces_fp64_residual():
         h.refine_gs(2)
     ref = esc.Handle(p).lanczos_gs(steps=200, lanctype="GS", reortho=0)            # FP64 run
     r32 = h.lanczos_gs(steps=200, lanctype="GS", reortho=0, dtype=np.complex64)
-    E, rn = h.refine_gs(steps=12)
+    E, rn = h.refine_gs(steps=40)
     print(f"refinement (18 sites): |H psi - E psi| {' -> '.join(f'{x:.2e}' for x in rn)}; "
           f"E0 complex64 Lanczos {r32['E0']:.15f}, refined {E:.15f}, FP64 Lanczos {ref['E0']:.15f}")
     # locally optimal steps minimise the Rayleigh quotient (the residual need not fall every step)

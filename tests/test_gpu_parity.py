@@ -412,7 +412,7 @@ def test_autotune_keeps_hv_and_reports_candidates():
     before = h.hv(x).astype(np.complex128)
     rep = h.autotune()
     lines = [l for l in rep.splitlines() if l.startswith("T=")]
-    assert len(lines) >= 8 and "chosen:" in rep
+    assert len(lines) >= 8 and "chosen:" in rep and "verified against the ahead-of-time kernel" in rep
     assert relerr(h.hv(x).astype(np.complex128), before) < 2e-6
     r = h.lanczos_gs(start=O.random_start(0, h.D), lanctype="GS", reortho=1)
     ref = esc.Handle(p).lanczos_gs(start=O.random_start(0, h.D), lanctype="GS", reortho=1)
