@@ -331,6 +331,55 @@ def c3_report(esc, gs_steps=300, cf_steps=1000, refine_steps=10):
     return out
 
 
+def e2e_report(esc, sites=32, reps=3):
+    """The legs of the pipelined host-buffer H.v (esc_hv_batched, 2 complex64 columns in reference
+    order) timed alone: host->device copy of one vector, device->host copy, both at once on two
+    streams, the device work of one column (basis permutation in, H.v, permutation out), and the
+    whole pipelined call.  Pinned host buffers; wall-clock after a warm-up, best of `reps`."""
+    import numpy as np
+    import torch
+    h = esc.Handle(workload(sites))
+    tune = h.autotune().strip().splitlines()[-1]
+    D = h.D
+    hin = torch.empty((2, D), dtype=torch.complex64, pin_memory=True)
+    hout = torch.empty((2, D), dtype=torch.complex64, pin_memory=True)
+    hin.zero_()
+    out = {"sites": sites, "vector_GB": D * 8 / 1e9, "tuning": tune}
+
+    def best(f):
+        f()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            f()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return min(ts) * 1e3
+
+    d0 = torch.empty(D, dtype=torch.complex64, device="cuda")
+    d1 = torch.empty(D, dtype=torch.complex64, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    out["h2d_ms"] = best(lambda: d0.copy_(hin[0], non_blocking=True))
+    out["d2h_ms"] = best(lambda: hout[0].copy_(d0, non_blocking=True))
+
+    def both():
+        with torch.cuda.stream(s1):
+            d0.copy_(hin[0], non_blocking=True)
+        with torch.cuda.stream(s2):
+            hout[1].copy_(d1, non_blocking=True)
+    out["h2d_and_d2h_ms"] = best(both)
+    out["device_column_ms"] = best(lambda: h.hv_device(d0.data_ptr(), d1.data_ptr(), esc.C64, esc.DEVICE_PTR))
+    del d0, d1
+    torch.cuda.empty_cache()
+    out["pipelined_2col_ms"] = best(lambda: h.hv_batched(hin.numpy(), out=hout.numpy()))
+    vb = D * 8 / 1e9
+    out["link_bound_2col_ms"] = round(max(2 * out["h2d_ms"], 2 * out["d2h_ms"], out["h2d_and_d2h_ms"] + out["h2d_ms"]), 1)
+    out["e2e_GBs"] = round(2 * 2 * vb / (out["pipelined_2col_ms"] * 1e-3), 1)
+    h.close()
+    return {k: (round(v, 2) if isinstance(v, float) else v) for k, v in out.items()}
+
+
 def reduce_max(x, dist, device):
     """Max over the ranks of a per-rank time (the slowest replica sets the job's time)."""
     import torch
@@ -395,6 +444,8 @@ def main():
                     help="FP64 residual refinement of a complex64 ground state of --sites; print one JSON line")
     ap.add_argument("--c3-report", action="store_true",
                     help="mixed precision against FP64 at 28 sites and the mixed 32-site run; print one JSON line")
+    ap.add_argument("--e2e-report", action="store_true",
+                    help="time the legs of the pipelined host-buffer H.v of --sites alone; print one JSON line")
     ap.add_argument("--step-report", action="store_true",
                     help="time one complex64 Lanczos step of the --sites cluster against one H.v and print one JSON line")
     ap.add_argument("--autotune-report", action="store_true",
@@ -432,6 +483,9 @@ def main():
         return
     if args.step_report:
         print(json.dumps(lanczos_step_report(esc, args.sites)), flush=True)
+        return
+    if args.e2e_report:
+        print(json.dumps(e2e_report(esc, args.sites)), flush=True)
         return
     if args.refine_report:
         print(json.dumps(refine_report(esc, args.sites)), flush=True)
