@@ -701,13 +701,17 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_o
             // ESC_PASS_BALANCE=2: local search from first-fit that moves single terms between
             // eligible passes while the total number of register groups (shared-memory loads per
             // state) decreases; a pass's groups are counted with its best register sites, as below.
+            // The groups are counted for 512 threads per tile whatever tb_bits is, so that every
+            // kernel variant of a plan assigns the same terms to the same pass (the self-tuner
+            // combines passes of different variants into one H.v).
+            constexpr int ASSIGN_TB_BITS = 9;
             auto pass_cost = [&](int pi, int add, int drop) {
                 std::vector<unsigned long long> gm;
                 for (size_t i = 0; i < terms.size(); i++)
                     if (((int)i != drop && asg[i] == pi) || (int)i == add) gm.push_back(terms[i].mask);
                 const std::vector<int>& B = P.tiles[pi];
                 const int c = std::min(P.c, (int)B.size());
-                const int nf = (int)B.size() - c, r = std::max(0, (int)B.size() - tb_bits);
+                const int nf = (int)B.size() - c, r = std::max(0, (int)B.size() - ASSIGN_TB_BITS);
                 int best = 1 << 30;
                 for (unsigned sel = 0; sel < (1u << nf); sel++) {
                     if (__builtin_popcount(sel) != std::min(r, nf)) continue;

@@ -88,7 +88,7 @@ bool load_tuning(esc_handle* h) {
 // vector: a tuned configuration must compute the same H.v (to complex64 rounding).  On a mismatch
 // the handle returns to the plan and passes it had before tuning, and the report says so.
 std::string verify_composite(esc_handle* h, const esc::Plan& plan, int balance, const esc::Plan& keep,
-                             const std::vector<esc::DevPass>& keep_passes) {
+                             const std::vector<esc::DevPass>& keep_passes, bool& verified) {
     const int64_t D = h->D;
     void* buf = nullptr;
     ESC_CUDA(cudaMalloc(&buf, (size_t)D * 24));
@@ -112,7 +112,8 @@ std::string verify_composite(esc_handle* h, const esc::Plan& plan, int balance, 
     }
     const double rel = dmax / std::max(ymax, 1e-300);
     std::ostringstream o;
-    if (!(rel <= 1e-5)) {
+    verified = rel <= 1e-5;
+    if (!verified) {
         install_plan(h, keep, -1, 0);
         h->passes = keep_passes;
         o << "verification FAILED (relative difference " << rel << " against the ahead-of-time kernel): the "
@@ -278,9 +279,10 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
     cudaFree(buf);
     install_plan(h, bplan, bbal, 2);
     h->passes = bpasses;
-    rep << verify_composite(h, bplan, bbal, keep, keep_passes);
+    bool verified = false;
+    rep << verify_composite(h, bplan, bbal, keep, keep_passes, verified);
     rep << tune_columns(h);
-    save_tuning(h, bT, bbal, bpasses);
+    if (verified) save_tuning(h, bT, bbal, bpasses);
     rep << "chosen: T=" << bT << " balance=" << bbal << " passes:";
     for (const auto& ps : bpasses) rep << " " << (ps.jit >= 0 ? "jit" : "aot") << "/" << ps.stages << "/" << (1 << ps.tb_bits);
     rep << " columns per launch " << h->cols_per_launch << " (" << best << " ms)\n";
