@@ -273,7 +273,7 @@ def refine_report(esc, sites, gs_steps=300, refine_steps=20):
             "lanczos_s": round(t1 - t0, 2), "rayleigh_s": round(t2 - t1, 2), "refine_s": round(t3 - t2, 2)}
 
 
-def c3_report(esc, gs_steps=300, cf_steps=1000, refine_steps=10):
+def c3_report(esc, gs_steps=300, cf_steps=1000, refine28=40, refine32=10):
     """Mixed precision against FP64 for the 32-site workload (K=-1, J=0.05, h=0.02 [111], seed 1):
     on the 28-site cluster (7x2 unit cells) both run -- FP64 ground state and FP64 continued
     fractions against the complex64 ground state (FP64 Rayleigh value, FP64 refinement) and complex64
@@ -282,7 +282,8 @@ def c3_report(esc, gs_steps=300, cf_steps=1000, refine_steps=10):
     refined ground state and the spectrum are reported.  JeJe spectra, 2000 omega in [0, 6],
     eta = 0.05."""
     import numpy as np
-    out = {"cf_steps": cf_steps, "gs_steps": gs_steps, "omega": "2000 points in [0,6]", "eta": 0.05}
+    out = {"cf_steps": cf_steps, "gs_steps": gs_steps, "omega": "2000 points in [0,6]", "eta": 0.05,
+           "refine_steps": {"n28": refine28, "n32": refine32}}
     kw = dict(omega_steps=1999, domega=6.0 / 1999, eta=0.05)
     # 28 sites, FP64
     h = esc.Handle(esc.ConstVariables(**workload(28), **kw))
@@ -299,7 +300,7 @@ def c3_report(esc, gs_steps=300, cf_steps=1000, refine_steps=10):
     t3 = time.perf_counter()
     r32 = h.lanczos_gs(steps=gs_steps, lanctype="GS", reortho=0, dtype=np.complex64, want_gs=False)
     e_ray = h.rayleigh()
-    E_ref, rn = h.refine_gs(refine_steps)
+    E_ref, rn = h.refine_gs(refine28)
     t4 = time.perf_counter()
     S32 = h.spectrum("Energy Current", "CF", cf_steps=cf_steps, dtype=np.complex64)
     t5 = time.perf_counter()
@@ -318,7 +319,7 @@ def c3_report(esc, gs_steps=300, cf_steps=1000, refine_steps=10):
     t6 = time.perf_counter()
     r = h.lanczos_gs(steps=gs_steps, lanctype="GS", reortho=0, dtype=np.complex64, want_gs=False)
     e_ray = h.rayleigh()
-    E_ref, rn = h.refine_gs(refine_steps)
+    E_ref, rn = h.refine_gs(refine32)
     t7 = time.perf_counter()
     S = h.spectrum("Energy Current", "CF", cf_steps=cf_steps // 2, dtype=np.complex64)
     t8 = time.perf_counter()

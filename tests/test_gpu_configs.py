@@ -201,3 +201,84 @@ def test_refine_gs_reduces_fp64_residual():
     # the spectra start from it (CF mode, complex64 vectors from the FP64 ground state)
     s = h.spectrum("Energy Current", "CF", omega_steps=199, domega=0.03, eta=0.05, cf_steps=100, dtype=np.complex64)
     assert np.isfinite(s).all()
+
+
+# ---------------------------------------------------------------------------------------------------
+# C2: plain FP64 at 24 sites against the oracle (fixtures from tests/golden/make_config_fixtures.py:
+# the oracle's three-vector FP64 Lanczos, its CF recurrences and the reference's operators)
+# ---------------------------------------------------------------------------------------------------
+import os  # noqa: E402
+
+from conftest import GOLDEN  # noqa: E402
+
+C2 = os.path.join(GOLDEN, "c2_n24.npz")
+C2L = os.path.join(GOLDEN, "c2_n18_local.npz")
+
+
+def c2_handle(g, tile_bits=None, monkeypatch=None):
+    Lx, Ly, K, J, hf, seed, gs_steps, cf_steps, nw, wmax, eta = g["params"]
+    if tile_bits:
+        monkeypatch.setenv("ESC_TILE_BITS", str(tile_bits))
+    h = esc.Handle(kh(int(Lx), int(Ly), hf, K=K, J=J, seed=int(seed), omega_steps=int(nw) - 1, domega=wmax / (nw - 1),
+                      eta=eta))
+    if tile_bits:
+        monkeypatch.delenv("ESC_TILE_BITS")
+    return h, int(gs_steps), int(cf_steps)
+
+
+def spectra_and_envelope(g, keys, monkeypatch):
+    """The GPU's spectra for `keys` and, as the rounding envelope, their difference from the same
+    computation with another tiling (another summation order in every H.v)."""
+    out = {}
+    for tb in (None, 11):
+        h, gs_steps, cf_steps = c2_handle(g, tb, monkeypatch)
+        r = h.lanczos_gs(steps=gs_steps, lanctype="GS", reortho=0)    # reference start vector from RandomSeed
+        for key, kind in keys:
+            out[(key, tb)] = h.spectrum(kind, "CF", cf_steps=cf_steps)
+        out[("gs", tb)] = r
+        h.close()
+    return out
+
+
+@pytest.mark.skipif(not os.path.exists(C2), reason="C2 fixture not generated")
+def test_c2_fp64_24_sites_vs_oracle(monkeypatch):
+    g = np.load(C2)
+    keys = [(k, kind) for k, kind in (("JeJe", "Energy Current"), ("JsJs", "Spin Current")) if k in g.files]
+    out = spectra_and_envelope(g, keys, monkeypatch)
+    r = out[("gs", None)]
+    # ground state: 300 FP64 Lanczos steps without reorthogonalisation, E0 to 1e-10 relative
+    assert abs(r["E0"] - g["E0"]) <= 1e-10 * abs(g["E0"]), (r["E0"], float(g["E0"]))
+    np.testing.assert_allclose(r["alpha"][:40], g["alpha"][:40], atol=1e-10)
+    np.testing.assert_allclose(r["beta"][1:41], g["beta"][1:41], atol=1e-10)
+    # the CF recurrences of every resolvent: first coefficients against the oracle's
+    h, _, _ = c2_handle(g)
+    gs = h.lanczos_gs(steps=300, lanctype="GS", reortho=0)["gs"]
+    for key, ops in (("JeJe", ["JexTotal", "JeyTotal"]), ("JsJs", ["JsxTotal", "JsyTotal", "JszTotal"])):
+        if key + "_cf_a" not in g.files:
+            continue
+        ch = [h.apply(o, 0, gs) for o in ops]
+        ch.append(sum(ch))
+        cf = h.cf_batched(np.stack(ch), 60, use_graph=True)
+        for c, (a, b) in enumerate(cf):
+            np.testing.assert_allclose(a[:40], g[key + "_cf_a"][c, :40], atol=1e-9)
+            np.testing.assert_allclose(b[:41], g[key + "_cf_b"][c, :41], rtol=1e-9)
+    # spectra: 1e-8, or 3x the GPU's own rounding envelope where 500 unconverged CF steps make
+    # FP64 runs that differ only in summation order disagree by more
+    for key, _ in keys:
+        s, s2 = out[(key, None)], out[(key, 11)]
+        env = np.abs(s - s2).max()
+        err = np.abs(s - g[key]).max()
+        print(f"C2 {key}: max |S_GPU - S_oracle| = {err:.2e}, GPU rounding envelope {env:.2e}")
+        assert err <= max(1e-8, 3 * env), (key, err, env)
+
+
+@pytest.mark.skipif(not os.path.exists(C2L), reason="C2 local fixture not generated")
+def test_c2_local_szsz_18_sites_vs_oracle(monkeypatch):
+    g = np.load(C2L)
+    out = spectra_and_envelope(g, [("SSLocal", "LocalSzSz")], monkeypatch)
+    assert abs(out[("gs", None)]["E0"] - g["E0"]) <= 1e-10 * abs(g["E0"])
+    s, s2 = out[("SSLocal", None)], out[("SSLocal", 11)]
+    env = np.abs(s - s2).max()
+    err = np.abs(s - g["SSLocal"]).max()
+    print(f"C2 LocalSzSz (18 sites): max |S_GPU - S_oracle| = {err:.2e}, GPU rounding envelope {env:.2e}")
+    assert err <= max(1e-8, 3 * env), (err, env)
