@@ -16,7 +16,9 @@ GOLDEN = os.path.join(REPO, "tests", "golden")
 
 
 def golden_names():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+    """Fixtures written by the reference's own code (tests/golden/make_golden.py); the configuration
+    fixtures of the oracle (c2_*.npz, tests/golden/make_config_fixtures.py) are not among them."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("c2_"))
 
 
 def parse_param_text(text):
