@@ -36,9 +36,8 @@ typedef enum {
     ESC_ERR_MEMORY = 2,    /* device or host allocation failed / problem too large         */
     ESC_ERR_CUDA = 3,      /* CUDA runtime error                                           */
     ESC_ERR_NUMERIC = 4,   /* eigensolver failure, NaN in alpha/beta (reference: runtime_error) */
-    ESC_ERR_STATE = 5,     /* call order (e.g. spectrum before a ground state)             */
-    ESC_ERR_TIMEOUT = 6    /* a bounded device wait gave up                                */
-} esc_status;
+    ESC_ERR_STATE = 5      /* call order (e.g. spectrum before a ground state)             */
+} esc_status;             /* no kernel of this library waits on a flag or barrier, so no call times out */
 
 typedef enum { ESC_C128 = 0, ESC_C64 = 1 } esc_dtype;
 
