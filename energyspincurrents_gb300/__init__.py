@@ -75,7 +75,7 @@ _lib = None
 # every symbol declared in include/esc.h
 EXPORTS = ["esc_params_default", "esc_params_from_file", "esc_lattice", "esc_plan", "esc_create", "esc_destroy", "esc_last_error",
            "esc_num_sites", "esc_dim", "esc_neighbors", "esc_basis_permutation", "esc_stream", "esc_hv", "esc_hv_batched", "esc_apply_op",
-           "esc_start_vector", "esc_rayleigh", "esc_rayleigh_noalloc", "esc_refine_gs", "esc_lanczos_gs", "esc_cf_batched", "esc_spectrum", "esc_measure_local", "esc_grad", "esc_autotune", "esc_two_point", "esc_alu_peaks"]
+           "esc_start_vector", "esc_rayleigh", "esc_rayleigh_noalloc", "esc_refine_gs", "esc_lanczos_gs", "esc_cf_batched", "esc_spectrum", "esc_measure_local", "esc_grad", "esc_autotune", "esc_two_point", "esc_alu_peaks", "esc_exact_diag"]
 
 
 def lib_path():
@@ -121,6 +121,7 @@ def lib():
     L.esc_autotune.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
     L.esc_two_point.argtypes = [vp, ci, ci, vp]
     L.esc_alu_peaks.argtypes = [vp]
+    L.esc_exact_diag.argtypes = [vp, vp, vp, ci]
     _lib = L
     return L
 
@@ -309,6 +310,14 @@ class Handle:
         v = np.ascontiguousarray(v)
         _check(self.h, lib().esc_rayleigh(self.h, _ptr(v), _dt(v), flags, ctypes.byref(E)))
         return E.value
+
+    def exact_diag(self):
+        """Solver=ED: all eigenvalues (ascending) and the ground state; the eigenpairs replace the
+        Ritz pairs for the Ritz-mode spectra."""
+        ev = np.empty(self.D)
+        gs = np.empty(self.D, dtype=np.complex128)
+        _check(self.h, lib().esc_exact_diag(self.h, _ptr(ev), _ptr(gs), 0))
+        return ev, gs
 
     def refine_gs(self, steps=4):
         """FP64 residual refinement of the ground state; returns (E, |H psi - E psi| before each

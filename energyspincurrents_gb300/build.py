@@ -25,7 +25,7 @@ EXE = os.path.join(OUT, "LanczosCond")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kernels.cu", "hv_tiled.cu", "batched.cu", "hv_jit.cu", "permute.cu", "alu_bench.cu"]
 CPP_SOURCES = ["esc_abi.cpp", "lanczos.cpp", "spectra.cpp", "grad.cpp", "tune.cpp", "params.cpp", "model.cpp", "numerics.cpp",
-               "planner.cpp"]
+               "planner.cpp", "exactdiag.cpp"]
 
 
 def _nvcc():
@@ -102,7 +102,7 @@ def build(force=False, verbose=False):
         list(ex.map(run, jobs))
     if force or jobs or not os.path.exists(LIB):
         run([nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-Xcompiler", "-fopenmp", "-lgomp",
-             "-L", os.path.join(cuda, "lib64"), "-lnvrtc", "-Xlinker", "-rpath", "-Xlinker", os.path.join(cuda, "lib64")])
+             "-L", os.path.join(cuda, "lib64"), "-lnvrtc", "-ldl", "-Xlinker", "-rpath", "-Xlinker", os.path.join(cuda, "lib64")])
         os.replace(LIB + ".tmp", LIB)
     exe_src = os.path.join(CSRC, "LanczosCond.cpp")
     if os.path.exists(exe_src) and (force or _newer(EXE, [exe_src, LIB] + hdrs)):

@@ -59,6 +59,59 @@ static void write_spectrum(const char* fname, int kind, const std::vector<double
     }
 }
 
+// The reference's main after the ground state (main.cpp:92-202): local expectation values, then
+// the dynamics the input file asks for, each written to its spectrum file.
+static int run_observables_and_dynamics(esc_handle* h, const esc_params& p, bool measure, esc_dtype dtype) {
+    const int N = esc_num_sites(h);
+    esc_status st = ESC_OK;
+    if (measure) {
+        std::vector<dcomplex> s(3 * (size_t)N), je(2 * (size_t)N);
+        const bool complete = std::string(p.model) == "Kitaev";
+        st = esc_measure_local(h, (double*)s.data(), complete ? (double*)je.data() : nullptr);
+        if (st != ESC_OK) die(h, st, "esc_measure_local");
+        std::cout << "\n-------- measuring: site, <sx>, <sy>, <sz>, <spin_total>, <sp>, <sm> --------" << std::endl;
+        const dcomplex I(0.0, 1.0);
+        for (int si = 0; si < N; si++) {
+            const dcomplex sx = s[3 * si], sy = s[3 * si + 1], sz = s[3 * si + 2];
+            std::cout << si << " \t " << sx << " \t " << sy << " \t " << sz << " \t " << sx + sy + sz << " \t "
+                      << sx + I * sy << " \t " << sx - I * sy << std::endl;
+        }
+        if (complete) {
+            std::cout << "\n-------- measuring: site, <Je_xi>, <Je_yi>, <Je_zi>, <Je_total> --------" << std::endl;
+            for (int si = 0; si < N; si++)
+                std::cout << si << " \t " << je[2 * si] << " \t " << je[2 * si + 1] << " \t " << " \t "
+                          << je[2 * si] + je[2 * si + 1] << std::endl;
+        }
+    }
+
+    auto dyn = [&](int kind, const char* banner, const char* fname) {
+        std::cout << " ==================================================================== " << std::endl;
+        std::cout << banner << std::endl;
+        std::cout << " ==================================================================== " << std::endl;
+        esc_dyn_cfg dc{kind, p.dyn_mode, p.omega_steps, p.domega, p.eta,
+                       p.dyn_lanczos_steps > 0 ? p.dyn_lanczos_steps : p.lanczos_steps, dtype};
+        int nr = 0, nc = 0;
+        esc_status s2 = esc_spectrum(h, &dc, nullptr, &nr, &nc);
+        if (s2 != ESC_OK) die(h, s2, "esc_spectrum");
+        std::vector<double> out((size_t)nr * nc);
+        s2 = esc_spectrum(h, &dc, out.data(), &nr, &nc);
+        if (s2 != ESC_OK) die(h, s2, "esc_spectrum");
+        write_spectrum(fname, kind, out, nr, nc);
+        std::cout << std::setprecision(8);
+        const int every = kind == ESC_DYN_JEJE ? 1 : 200;
+        for (int k = 0; k < nr; k += every) {
+            for (int q = 0; q < nc; q++) std::cout << out[(size_t)k * nc + q] << " \t ";
+            std::cout << " \n ";
+        }
+        std::cout << " " << std::endl << std::endl;
+    };
+    if (p.local_skw) dyn(ESC_DYN_JSJS, "                   Spin Dynamical Correlations		                   ", "JsJs_outSpectrum.real");
+    if (p.energy_curr_dyn) dyn(ESC_DYN_JEJE, "              Energy Current Dynamical Correlations				   ", "JeJe_outSpectrum.real");
+    if (p.local_szsz_dyn) dyn(ESC_DYN_LOCALSZSZ, "                 Local Spin Dynamical Correlations                  ", "2SSLocal_outSpectrum.real");
+    esc_destroy(h);
+    return 0;
+}
+
 int main(int argc, char* argv[]) {
     std::cout << "Hello, World!" << std::endl;
     if (argc != 2) throw std::invalid_argument("USE:: executable inputfile");
@@ -79,6 +132,17 @@ int main(int argc, char* argv[]) {
     const int64_t D = esc_dim(h);
     std::cout << "number of ket basis: " << D << std::endl;
 
+    if (std::string(p.solver) == "ED") {
+        // main.cpp:79-83: ExactDiag (src/Exactdiag.h:36-81) + fillFromED
+        std::cout << "Begin Exact Diagonalization! --- " << std::endl;
+        std::vector<double> ev((size_t)D);
+        st = esc_exact_diag(h, ev.data(), nullptr, 0);
+        if (st != ESC_OK) die(h, st, "esc_exact_diag");
+        for (double x : ev) std::cout << x << ", ";
+        std::cout << " Ground-state energy:= " << std::setprecision(16) << ev[0] << std::endl;
+        std::cout << std::setprecision(8) << std::fixed;
+        return run_observables_and_dynamics(h, p, true, ESC_C128);
+    }
     const int M = p.lanczos_steps;
     const int lt = std::string(p.lanctype) == "OnlyEgs" ? 0 : std::string(p.lanctype) == "GS" ? 1 : 2;
     esc_lanczos_cfg cfg{M, p.lanczos_eps, lt, p.reortho, p.precision ? ESC_C64 : ESC_C128};
@@ -109,50 +173,6 @@ int main(int argc, char* argv[]) {
     std::cout << std::endl;
     std::cout << std::setprecision(8) << std::fixed;
 
-    if (lt != 0) {
-        std::vector<dcomplex> s(3 * (size_t)N), je(2 * (size_t)N);
-        const bool complete = std::string(p.model) == "Kitaev";
-        st = esc_measure_local(h, (double*)s.data(), complete ? (double*)je.data() : nullptr);
-        if (st != ESC_OK) die(h, st, "esc_measure_local");
-        std::cout << "\n-------- measuring: site, <sx>, <sy>, <sz>, <spin_total>, <sp>, <sm> --------" << std::endl;
-        const dcomplex I(0.0, 1.0);
-        for (int si = 0; si < N; si++) {
-            const dcomplex sx = s[3 * si], sy = s[3 * si + 1], sz = s[3 * si + 2];
-            std::cout << si << " \t " << sx << " \t " << sy << " \t " << sz << " \t " << sx + sy + sz << " \t "
-                      << sx + I * sy << " \t " << sx - I * sy << std::endl;
-        }
-        if (complete) {
-            std::cout << "\n-------- measuring: site, <Je_xi>, <Je_yi>, <Je_zi>, <Je_total> --------" << std::endl;
-            for (int si = 0; si < N; si++)
-                std::cout << si << " \t " << je[2 * si] << " \t " << je[2 * si + 1] << " \t " << " \t "
-                          << je[2 * si] + je[2 * si + 1] << std::endl;
-        }
-    }
-
-    auto dyn = [&](int kind, const char* banner, const char* fname) {
-        std::cout << " ==================================================================== " << std::endl;
-        std::cout << banner << std::endl;
-        std::cout << " ==================================================================== " << std::endl;
-        esc_dyn_cfg dc{kind, p.dyn_mode, p.omega_steps, p.domega, p.eta,
-                       p.dyn_lanczos_steps > 0 ? p.dyn_lanczos_steps : p.lanczos_steps, cfg.dtype};
-        int nr = 0, nc = 0;
-        esc_status s2 = esc_spectrum(h, &dc, nullptr, &nr, &nc);
-        if (s2 != ESC_OK) die(h, s2, "esc_spectrum");
-        std::vector<double> out((size_t)nr * nc);
-        s2 = esc_spectrum(h, &dc, out.data(), &nr, &nc);
-        if (s2 != ESC_OK) die(h, s2, "esc_spectrum");
-        write_spectrum(fname, kind, out, nr, nc);
-        std::cout << std::setprecision(8);
-        const int every = kind == ESC_DYN_JEJE ? 1 : 200;
-        for (int k = 0; k < nr; k += every) {
-            for (int q = 0; q < nc; q++) std::cout << out[(size_t)k * nc + q] << " \t ";
-            std::cout << " \n ";
-        }
-        std::cout << " " << std::endl << std::endl;
-    };
-    if (p.local_skw) dyn(ESC_DYN_JSJS, "                   Spin Dynamical Correlations		                   ", "JsJs_outSpectrum.real");
-    if (p.energy_curr_dyn) dyn(ESC_DYN_JEJE, "              Energy Current Dynamical Correlations				   ", "JeJe_outSpectrum.real");
-    if (p.local_szsz_dyn) dyn(ESC_DYN_LOCALSZSZ, "                 Local Spin Dynamical Correlations                  ", "2SSLocal_outSpectrum.real");
-    esc_destroy(h);
-    return 0;
+    return run_observables_and_dynamics(h, p, lt != 0, cfg.dtype);
 }
+

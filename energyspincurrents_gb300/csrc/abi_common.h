@@ -43,6 +43,7 @@ struct esc_handle {
     // ground-state Lanczos results
     int nsteps = 0;
     bool have_gs = false, have_basis = false;
+    bool exact = false;   // the basis holds exact eigenvectors (Solver=ED): Ritz overlaps need no Z
     esc_dtype basis_dt = ESC_C128;
     int64_t L_ld = 0;
     std::vector<double> alpha, beta, ritz, Z;
@@ -135,6 +136,8 @@ struct Pipe {
 // lanczos.cpp
 template <typename R> void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start);
 void refine_gs(esc_handle* h, int steps, double* E, double* rnorm);
+// exactdiag.cpp
+void exact_diag(esc_handle* h);
 template <typename RR>
 std::function<int(const void*, void*, const int*, double*, cudaStream_t)> hv_all_columns(
         esc_handle* h, const std::vector<esc::DevModel>& ms, const void* dg);
@@ -191,6 +194,7 @@ struct Spectra {
         *elastic = cplx(el[0], el[1]);
         std::vector<cplx> O(M);
         for (int n = 0; n < M; n++) {
+            if (h->exact) { O[n] = cplx(r[2 * n], r[2 * n + 1]); continue; }   // eigenvectors themselves
             cplx s(0, 0);
             for (int m = 0; m < M; m++) s += h->Z[(size_t)n * M + m] * cplx(r[2 * m], r[2 * m + 1]);
             O[n] = s;

@@ -211,8 +211,6 @@ esc_status esc_create(const esc_params* p, esc_handle** out) {
     std::unique_ptr<esc_handle> h(new esc_handle());
     esc_status st = guarded(h.get(), [&]() {
         h->p = *p;
-        const std::string solver(p->solver);
-        if (solver == "ED") throw Fail(ESC_ERR_PARAM, "Solver=ED (dense diagonalisation) is not provided on the GPU; use Solver=none");
         esc::build_lattice(*p, h->L);
         esc::build_bonds(*p, h->L, h->bonds);
         h->N = h->L.N;

@@ -238,6 +238,8 @@ template <typename R> void launch_gemv_sub(const void* L, int64_t ld, int m, con
 template <typename R> void launch_lincomb(const void* L, int64_t ld, int m, const double* z, void* out, int64_t n,
                                           cudaStream_t s);
 void launch_convert_c128_to_c64(const void* in, void* out, int64_t n, cudaStream_t s);
+// unit vectors e_{j0} .. e_{j0+ncols-1} as ncols columns of D states (stride D)
+template <typename R> void launch_unit_columns(void* out, int64_t D, int64_t j0, int ncols, cudaStream_t s);
 void launch_convert_c64_to_c128(const void* in, void* out, int64_t n, cudaStream_t s);
 template <typename R> void launch_start_normal(uint64_t seed, void* out, int64_t n, cudaStream_t s);
 

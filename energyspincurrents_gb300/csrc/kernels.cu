@@ -530,6 +530,28 @@ void launch_start_normal(uint64_t seed, void* out, int64_t n, cudaStream_t s) {
     ESC_CUDA(cudaGetLastError());
 }
 
+// out[c][i] = (i == j0 + c) for c < ncols: unit vectors e_{j0} .. e_{j0+ncols-1}, stride D
+template <typename R>
+__global__ void __launch_bounds__(256) k_unit_columns(typename V2<R>::T* __restrict__ out, long long D, long long j0,
+                                                      int ncols) {
+    const long long n = (long long)ncols * D;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        typename V2<R>::T v;
+        v.x = (i % D == j0 + i / D) ? (R)1 : (R)0;
+        v.y = (R)0;
+        out[i] = v;
+    }
+}
+template <typename R>
+void launch_unit_columns(void* out, int64_t D, int64_t j0, int ncols, cudaStream_t s) {
+    typedef typename V2<R>::T C;
+    k_unit_columns<R><<<grid_for((int64_t)ncols * D, 256, SMS * 16), 256, 0, s>>>((C*)out, D, j0, ncols);
+    ESC_CUDA(cudaGetLastError());
+}
+template void launch_unit_columns<double>(void*, int64_t, int64_t, int, cudaStream_t);
+template void launch_unit_columns<float>(void*, int64_t, int64_t, int, cudaStream_t);
+
 // explicit instantiations
 #define ESC_INST(R)                                                                                        \
     template void launch_apply<R>(const DevOp&, const void*, void*, int64_t, cudaStream_t);                \

@@ -79,6 +79,7 @@ void lanczos_gs(esc_handle* h, const esc_lanczos_cfg& cfg, const void* d_start) 
     const bool store = cfg.lanctype != 0 && !recompute;  // OnlyEgs keeps no basis (returns a zero vector)
     const bool reo = store && cfg.reortho;
     h->have_gs = h->have_basis = false;
+    h->exact = false;
     if (!reo) {
         // ---- unnormalised recurrence on the batched engine --------------------------------------
         const size_t nd = (size_t)esc::CFB_GRID * 2 + (size_t)M * 2 + (size_t)(M + 1) + (size_t)(M + 2);
@@ -320,6 +321,7 @@ void refine_gs(esc_handle* h, int steps, double* E_out, double* rnorm) {
     h->gs_bytes = (size_t)D * 16;
     h->basis_dt = ESC_C128;
     h->have_basis = false;
+    h->exact = false;
     if (cudaMalloc(&r, (size_t)D * 16) != cudaSuccess || cudaMalloc(&p, (size_t)D * 16) != cudaSuccess) {
         (void)cudaGetLastError();
         if (r) cudaFree(r);

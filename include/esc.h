@@ -245,6 +245,15 @@ esc_status esc_lanczos_gs(esc_handle* h, const esc_lanczos_cfg* cfg, const void*
                           double* E0, double* alpha, double* beta, double* ritz, int* steps,
                           void* gs_out);
 
+/* Dense exact diagonalisation, the reference's Solver=ED.  Replaces ExactDiag +
+ * DynLanczosSolver::fillFromED (src/Exactdiag.h:36-81, src/DynLanczosSolver.h:269-283, chosen in
+ * main.cpp:79-83): the 2^N x 2^N complex128 matrix of H is built on the device and diagonalised
+ * (cuSOLVER, loaded at run time); all 2^N eigenpairs then take the place of the Ritz pairs, so
+ * esc_spectrum (Ritz mode) sums over the exact spectrum, and the ground state is the lowest
+ * eigenvector.  evals (may be NULL): 2^N eigenvalues ascending; gs_out (may be NULL): the ground
+ * state (host unless ESC_DEVICE_PTR).  At most 14 sites (the matrix is 4^N x 16 bytes). */
+esc_status esc_exact_diag(esc_handle* h, double* evals, void* gs_out, int flags);
+
 /* Batched continued-fraction coefficients (extension; the reference has no continued fraction).
  * starts: ncols vectors of 2^N states with stride ld (elements).  On return, for column c:
  * a[c*max_steps + k] (k < lens[c]) and b[c*(max_steps+1) + k] (k <= lens[c]), b[.. + 0] = |phi_c|,

@@ -619,3 +619,34 @@ def test_lanczos_eps_exit_matches_reference_rule():
     assert np.array_equal(r["alpha"], full["alpha"][:n])
     w = [O.tridiag_eig(full["alpha"][:k + 1], full["beta"][1:k + 1], vectors=False)[0] for k in range(n)]
     assert abs(w[n - 1] - w[n - 2]) < 1e-9 and all(abs(w[k] - w[k - 1]) >= 1e-9 for k in range(1, n - 1))
+
+
+@pytest.mark.parametrize("shape", [(2, 4), (3, 4)])
+def test_exact_diag_vs_dense_and_oracle_spectra(shape):
+    """Solver=ED (ExactDiag + fillFromED, src/Exactdiag.h:36-81, src/DynLanczosSolver.h:269-283):
+    eigenvalues against numpy's dense eigensolver, the ground state, and the Ritz-mode spectra over
+    all exact eigenpairs against the oracle's Lehmann sums over the same eigenpairs (the reference's
+    own ExactDiag adds its COO lists to an uninitialised matrix, src/Exactdiag.h:42, so its output
+    cannot pin this)."""
+    Lx, Ly = shape
+    p = kitaev(Lx=Lx, Ly=Ly, J=0.1, solver="ED")
+    h = esc.Handle(p)
+    ev, gs = h.exact_diag()
+    m = O.Model("Kitaev", Lx, Ly, 1, 1, -1.0, -1.0, -1.0, p["Bxx"], p["Byy"], p["Bzz"], 0.1, 4, True)
+    w, V = np.linalg.eigh(m.dense())
+    assert np.abs(ev - w).max() < 1e-12 * max(1.0, np.abs(w).max())
+    assert abs(abs(np.vdot(V[:, 0], gs)) - 1.0) < 1e-10
+    m.set_eigenpairs(w, V)
+    for kind in ("Energy Current", "Spin Current", "LocalSzSz"):
+        s = h.spectrum(kind, "Ritz")
+        ref = m.dynamics(kind)
+        assert s.shape == ref.shape
+        assert np.abs(s - ref).max() < 1e-8 * max(1.0, np.abs(ref).max()), kind
+    loc, _ = h.measure_local()
+    assert np.abs(loc[:, 2] - np.array([np.vdot(gs, h.apply("Sz", i, gs)) for i in range(h.N)])).max() < 1e-12
+
+
+def test_exact_diag_size_limit():
+    h = esc.Handle(kitaev(Lx=3, Ly=6, solver="ED"))
+    with pytest.raises(esc.EscError, match="at most 14 sites"):
+        h.exact_diag()
