@@ -71,7 +71,6 @@ struct DevCols {
     double* dotp = nullptr;
 };
 DevCols single_column(const DevModel& m);
-DevCols with_field(DevCols c, int col, double bx, double by, double bz);   // Bx/2 ... from full fields
 
 // Operator = sum of terms; term t = coef * f_{n-1} ... f_0 (f_0 applied first), each factor a
 // single-site S^x/S^y/S^z.  Gather form: out[k] += coef * phi_t(k0) * in[k0], k0 = k ^ flip.

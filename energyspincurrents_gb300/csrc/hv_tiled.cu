@@ -548,12 +548,6 @@ DevCols single_column(const DevModel& m) {
     return c;
 }
 
-DevCols with_field(DevCols c, int col, double bx, double by, double bz) {
-    c.f.fx[col] = 0.5 * bx; c.f.fy[col] = 0.5 * by; c.f.fz[col] = 0.5 * bz;
-    c.f.fxf[col] = (float)c.f.fx[col]; c.f.fyf[col] = (float)c.f.fy[col]; c.f.fzf[col] = (float)c.f.fz[col];
-    return c;
-}
-
 // FP64 energy sweep: sum over one pass of conj(v[k]) (H_pass v)[k], computed in FP64 from a
 // complex64 or complex128 vector, without writing H v.  The passes of a plan add up to
 // <v|H|v>.  One (re, im) partial per CTA (fixed grid: deterministic).
