@@ -15,6 +15,7 @@ host->device copy, H.v, device->host copy inside the timed region), clocks.
 import argparse
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -521,8 +522,12 @@ def main():
     st = esc.lib().esc_start_vector(h.h, 1, 1, esc.ctypes.c_void_p(v.data_ptr()), edt, flags)
     assert st == 0, esc.lib().esc_last_error(h.h)
     npasses = esc.plan(esc.ConstVariables(**params))[1]
+    npairs = 0
     if tuning:
-        npasses = len(tuning.split("passes:")[1].split("(")[0].split())
+        chosen = tuning.split("passes:")[1]
+        npasses = len(re.findall(r"\b(?:jit|aot)/\d+/\d+", chosen))
+        m = re.search(r"slab pairs (\d+)", chosen)
+        npairs = int(m.group(1)) if m else 0
     torch.cuda.synchronize()
 
     def step():
@@ -620,7 +625,7 @@ def main():
                 "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
                 "config": dict(workload_config(args.sites, world, args.dtype), tuning=tuning),
                 "roofline": roof, "cpu_baseline": cb, "e2e": e2e, "time_to_S": tts, "clocks": clk.summary(),
-                "gpu_launches": args.steps * npasses}
+                "gpu_launches": args.steps * (npasses - npairs)}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -20,7 +20,7 @@ import numpy as np
 _PKG = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_PKG, "_build", "libesc.so")
 
-ESC_OK, ESC_ERR_PARAM, ESC_ERR_MEMORY, ESC_ERR_CUDA, ESC_ERR_NUMERIC, ESC_ERR_STATE = range(6)
+ESC_OK, ESC_ERR_PARAM, ESC_ERR_MEMORY, ESC_ERR_CUDA, ESC_ERR_NUMERIC, ESC_ERR_STATE, ESC_ERR_TIMEOUT = range(7)
 C128, C64 = 0, 1
 DEVICE_PTR, ASYNC, INTERNAL_ORDER = 1, 2, 4
 

@@ -38,6 +38,8 @@ struct esc_handle {
     void* d_cfb = nullptr; size_t cfb_bytes = 0;       // batched CF vectors (3 x ncols x D)
     double* d_cfs = nullptr; size_t cfs_bytes = 0;     // batched CF scalars
     int* d_cfi = nullptr; size_t cfi_bytes = 0;        // batched CF flags / counters
+    unsigned* slab_sync = nullptr;                     // slab-pair error flag + counters (DevModel::slab_sync)
+    unsigned long long slab_seen = 0;                  // slab-pair launches seen at the last check
     void* d_diag[2] = {nullptr, nullptr};              // diagonal of the bond terms per dtype
     size_t diag_bytes[2] = {0, 0};
     // ground-state Lanczos results

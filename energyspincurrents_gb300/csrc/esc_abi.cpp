@@ -52,7 +52,24 @@ void ensure(void*& p, size_t& cap, size_t need) {
     }
     cap = need;
 }
-void sync(esc_handle* h) { ESC_CUDA(cudaStreamSynchronize(h->stream)); }
+// Synchronises the handle's stream; reports a slab-pair wait that gave up since the last check
+// (the flag is read only when slab-pair launches were made since then).
+void sync(esc_handle* h) {
+    ESC_CUDA(cudaStreamSynchronize(h->stream));
+    if (!h->slab_sync) return;
+    const unsigned long long n = esc::slab_pair_launches();
+    if (n == h->slab_seen) return;
+    h->slab_seen = n;
+    unsigned e = 0;
+    ESC_CUDA(cudaMemcpyAsync(&e, h->slab_sync, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+    ESC_CUDA(cudaStreamSynchronize(h->stream));
+    if (e) {
+        ESC_CUDA(cudaMemsetAsync(h->slab_sync, 0, sizeof(unsigned), h->stream));
+        ESC_CUDA(cudaStreamSynchronize(h->stream));
+        throw Fail(ESC_ERR_TIMEOUT, "a slab-pair H.v launch gave up waiting for its tiles: the results since the last "
+                                    "synchronisation are invalid");
+    }
+}
 
 // Precomputed bond diagonal (the analogue of the reference's HDiag without the field term),
 // 4 B/state for complex64, 8 B/state for complex128; computed on first use.  If it cannot be
@@ -174,6 +191,7 @@ void install_plan(esc_handle* h, const esc::Plan& plan, int balance, int stages,
     std::vector<esc::Bond> rb(h->bonds);
     for (auto& b : rb) { b.i = h->plan.perm[b.i]; b.j = h->plan.perm[b.j]; }
     h->dm = esc::make_dev_model(h->p, h->L, rb, h->p.Bxx, h->p.Byy, h->p.Bzz);
+    h->dm.slab_sync = h->slab_sync;
     h->passes = esc::make_passes(h->plan, h->dm, balance, stages, tb_bits);
     std::vector<int> inv(h->N), fwd(h->N);
     for (int s = 0; s < h->N; s++) { inv[h->plan.perm[s]] = s; fwd[s] = h->plan.perm[s]; }
@@ -235,6 +253,15 @@ esc_status esc_create(const esc_params* p, esc_handle** out) {
         ESC_CUDA(cudaGetDevice(&h->device));
         ESC_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
         ensure_partials(h.get(), 4);
+        // slab-pair words (passes paired from SLAB_MIN_SITES sites, or at any size by ESC_SLAB_PAIRS=1)
+        const int pe = esc::slab_pairs_env();
+        if (pe == 1 || (pe < 0 && h->N >= esc::SLAB_MIN_SITES)) {
+            const size_t bytes = esc::slab_sync_words(h->N) * sizeof(unsigned);
+            ESC_CUDA(cudaMalloc((void**)&h->slab_sync, bytes));
+            ESC_CUDA(cudaMemsetAsync(h->slab_sync, 0, bytes, h->stream));
+            h->dm.slab_sync = h->slab_sync;
+            h->slab_seen = esc::slab_pair_launches();
+        }
         if (!load_tuning(h.get())) {
             specialise(h.get(), h->passes);
             if (const char* e = std::getenv("ESC_AUTOTUNE"))
@@ -265,7 +292,7 @@ esc_status esc_autotune(esc_handle* h, char* report, size_t report_len) {
 esc_status esc_destroy(esc_handle* h) {
     if (!h) return ESC_OK;
     for (void* p : {(void*)h->d_part, (void*)h->d_sc, h->d_L, h->d_work, h->d_gs, h->d_io, h->d_diag[0], h->d_diag[1],
-                    h->d_cfb, (void*)h->d_cfs, (void*)h->d_cfi})
+                    h->d_cfb, (void*)h->d_cfs, (void*)h->d_cfi, (void*)h->slab_sync})
         if (p) cudaFree(p);
     if (h->stream) cudaStreamDestroy(h->stream);
     for (cudaStream_t x : {h->s_in, h->s_out})

@@ -53,6 +53,9 @@ struct DevModel {
     float fxf, fyf, fzf, padf;
     float ceqf[MAX_BONDS], cdifff[MAX_BONDS];
     float dqf[MAX_BONDS];   // dz/4
+    // device words of the slab-pair passes (hv_tiled.cu): [0] error flag, [SLAB_CNT0 ..] per-slab
+    // counters; NULL: passes are never paired (a model that no handle owns)
+    unsigned* slab_sync;
 };
 void fill_float_copies(DevModel& m);
 // Per-column field (batched H.V with one field per column).
@@ -142,26 +145,57 @@ struct DevPass {
     int jit;      // kernel specialised for this pass at run time (hv_jit.cu), -1: none
     int stages;   // complex64 pass: 2 or 3 tile buffers per CTA, 4 = 2 + staged epilogue loads
     int tb_bits;  // complex64 grouped pass: log2 of the threads per tile (9: 512, 8: 256, 7: 128)
+    // Slab pair (complex64, one column): pair = 1 marks the first pass of a pair with the next pass
+    // (both run in one launch, slab by slab); slab_bits = bits spanned by the two tiles together.
+    int pair, slab_bits;
+    int jit_pair;  // specialised pair kernel of this pass and the next (hv_jit.cu), -1: none
 };
+// Slab pairs: consecutive passes whose tiles together span at most SLAB_MAX_BITS bits can run as
+// one launch over slabs of 2^slab_bits states (2^21 complex64 states = 16 MB: the slab's input,
+// partial result and diagonal can stay in the L2 cache between the two passes).  From
+// SLAB_MIN_SITES sites on the planner orders the passes in such pairs and the self-tuner times the
+// paired launches against the single ones; ESC_SLAB_PAIRS=1 pairs at any size without tuning, =0
+// never.
+constexpr int SLAB_MIN_SITES = 27;
+constexpr int SLAB_MAX_BITS = 21;
+constexpr int SLAB_CNT0 = 32;   // first counter word of DevModel::slab_sync
+// -1: no environment override, 0: pairs off, 1: pairs at every size
+int slab_pairs_env();
+// Slab-pair launches made by this process so far (a handle checks its error flag when it changed).
+unsigned long long slab_pair_launches();
+// Marks the slab pairs of a pass list (DevPass::pair, ::slab_bits): consecutive passes whose
+// tiles span at most SLAB_MAX_BITS of the N bits together, greedily from the first pass.
+void mark_pairs(std::vector<DevPass>& ps, int N);
+// Words of DevModel::slab_sync for a basis of N sites.
+inline size_t slab_sync_words(int N) { return (size_t)SLAB_CNT0 + (N > 12 ? (size_t)1 << (N - 12) : 1); }
+// Orders the passes of a plan so that consecutive pairs span few bits (planner.cpp); applied
+// from SLAB_MIN_SITES sites on, or at any size when ESC_SLAB_PAIRS is set.
+void order_for_pairs(Plan& P);
 // Builds one DevPass per plan pass from the relabelled model; throws if a term fits no tile.
 // balance: term -> pass assignment (0 first eligible pass, 1 balanced, -1 from ESC_PASS_BALANCE);
 // stages: tile buffers of the complex64 passes (0: from ESC_STAGES, default 2).
 // tb_bits: threads per tile of the grouped complex64 pass, 2^tb_bits (7..9; 0: ESC_TB_BITS, else 9).
 std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance = -1, int stages = 0, int tb_bits = 0);
 }  // namespace esc
-namespace escdev { struct PassTab; }
+namespace escdev { struct PassTab; struct PairTab; }
 namespace esc {
 // Run-time specialisation of the complex64 passes (hv_jit.cu): compiles one kernel per eligible
-// pass with its term groups written out, for the current device, and sets DevPass::jit.  Returns
-// false (passes unchanged) with a message if NVRTC or the module load fails.
+// pass with its term groups written out, and one per slab pair of two such passes, for the
+// current device, and sets DevPass::jit and ::jit_pair.  Returns false (passes unchanged) with a
+// message if NVRTC or the module load fails.
 bool jit_compile(std::vector<DevPass>& passes, std::string& err);
 // The CUDA source jit_compile hands to NVRTC; which (optional) receives the pass index of each
-// kernel esc_jit_pass<k>.
-std::string jit_source(const std::vector<DevPass>& passes, std::vector<int>* which);
+// kernel esc_jit_pass<k>, pairs the first pass of each kernel esc_jit_pair<q>.
+std::string jit_source(const std::vector<DevPass>& passes, std::vector<int>* which, std::vector<int>* pairs = nullptr);
 // Launches the specialised kernel of pass p; returns its grid size.
 int jit_launch(const DevPass& p, const escdev::PassTab& pt, const void* diag, const void* in, void* out, int64_t D,
                int sms, cudaStream_t s, const int* active);
 escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m, const DevCols* cols = nullptr, double* dotp = nullptr);
+// Slab-pair table of passes a and b (a.pair set) over N sites; sync = DevModel::slab_sync.
+escdev::PairTab make_pair_tab(const DevPass& a, const DevPass& b, int N, unsigned* sync);
+// Launches the specialised pair kernel of a (a.jit_pair) cooperatively; returns its grid.
+int jit_pair_launch(const DevPass& a, const escdev::PassTab& pa, const escdev::PassTab& pb, const escdev::PairTab& st,
+                    const void* diag, const void* in, void* out, int64_t D, int sms, cudaStream_t s, const int* active);
 // Default tile buffers per CTA of the complex64 passes (2; ESC_STAGES=3 for three).
 int pass_stages();
 // diag: precomputed diagonal of the bond terms (no field), R per state (launch_diag); may be NULL,

@@ -92,8 +92,23 @@ std::string terms_source(const DevPass& p, int k) {
       << "extern \"C\" __global__ void __launch_bounds__(" << TB << ", " << min_ctas(p) << ") esc_jit_pass" << k
       << "(const __grid_constant__ escdev::PassTab p, const float* __restrict__ diag, const float2* __restrict__ in,"
          " float2* __restrict__ out, long long ntiles, const int* __restrict__ active) {\n"
-      << "  escdev::pass_body<" << E << ", " << (p.stages >= 2 && p.stages <= 4 ? p.stages : 2) << ", Terms" << k << ", "
+      << "  escdev::pass_body<" << E << ", " << (p.stages >= 2 && p.stages <= 5 ? p.stages : 2) << ", Terms" << k << ", "
       << TB << ">(p, Terms" << k << "{}, diag, in, out, ntiles, active);\n}\n";
+    return o.str();
+}
+
+// Slab-pair kernel q of passes a, b (terms functors Terms<ka>, Terms<kb>): pair_body of
+// hv_pass_device.cuh, launched cooperatively.
+std::string pair_source(const DevPass& a, int ka, int kb, int q) {
+    const int TB = 1 << a.tb_bits;
+    const int E = 1 << (a.Tp - a.tb_bits);
+    std::ostringstream o;
+    o << "extern \"C\" __global__ void __launch_bounds__(" << TB << ", " << min_ctas(a) << ") esc_jit_pair" << q
+      << "(const __grid_constant__ escdev::PassTab pa, const __grid_constant__ escdev::PassTab pb,"
+         " const __grid_constant__ escdev::PairTab st, const float* __restrict__ diag, const float2* __restrict__ in,"
+         " float2* __restrict__ out, const int* __restrict__ active) {\n"
+      << "  escdev::pair_body<" << E << ", " << TB << ">(pa, pb, st, Terms" << ka << "{}, Terms" << kb
+      << "{}, diag, in, out, active);\n}\n";
     return o.str();
 }
 
@@ -105,6 +120,7 @@ struct Driver {
     decltype(&::cuFuncSetAttribute) funcSetAttribute = nullptr;
     decltype(&::cuOccupancyMaxActiveBlocksPerMultiprocessor) occupancy = nullptr;
     decltype(&::cuLaunchKernel) launchKernel = nullptr;
+    decltype(&::cuLaunchCooperativeKernel) launchCooperative = nullptr;
     decltype(&::cuGetErrorString) getErrorString = nullptr;
     bool ok = false;
 };
@@ -128,7 +144,8 @@ const Driver& driver() {
         x.ok = resolve("cuModuleLoadData", x.moduleLoadData) && resolve("cuModuleGetFunction", x.moduleGetFunction) &&
                resolve("cuFuncSetAttribute", x.funcSetAttribute) &&
                resolve("cuOccupancyMaxActiveBlocksPerMultiprocessor", x.occupancy) &&
-               resolve("cuLaunchKernel", x.launchKernel) && resolve("cuGetErrorString", x.getErrorString);
+               resolve("cuLaunchKernel", x.launchKernel) && resolve("cuGetErrorString", x.getErrorString) &&
+               resolve("cuLaunchCooperativeKernel", x.launchCooperative);
         return x;
     }();
     return d;
@@ -144,14 +161,26 @@ bool drv(CUresult r, const char* what, std::string& err) {
 
 }  // namespace
 
-std::string jit_source(const std::vector<DevPass>& passes, std::vector<int>* which) {
+std::string jit_source(const std::vector<DevPass>& passes, std::vector<int>* which, std::vector<int>* pairs) {
     std::string src(kPassDeviceSource);
+    std::vector<int> kof(passes.size(), -1);
     int k = 0;
     for (size_t i = 0; i < passes.size(); i++)
         if (eligible(passes[i])) {
-            src += terms_source(passes[i], k++);
+            src += terms_source(passes[i], k);
+            kof[i] = k++;
             if (which) which->push_back((int)i);
         }
+    // slab pairs of two specialised passes of one shape
+    int q = 0;
+    for (size_t i = 0; i + 1 < passes.size(); i++) {
+        const DevPass& a = passes[i];
+        const DevPass& b = passes[i + 1];
+        if (a.pair && kof[i] >= 0 && kof[i + 1] >= 0 && a.tb_bits == b.tb_bits && a.Tp == b.Tp) {
+            src += pair_source(a, kof[i], kof[i + 1], q++);
+            if (pairs) pairs->push_back((int)i);
+        }
+    }
     return src;
 }
 
@@ -165,8 +194,8 @@ bool jit_compile(std::vector<DevPass>& passes, std::string& err) {
     int major = 0, minor = 0;
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
     cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
-    std::vector<int> which;
-    const std::string src = jit_source(passes, &which);
+    std::vector<int> which, pairs;
+    const std::string src = jit_source(passes, &which, &pairs);
     if (which.empty()) return true;
     const Driver& D = driver();
     if (!D.ok) {
@@ -220,9 +249,27 @@ bool jit_compile(std::vector<DevPass>& passes, std::string& err) {
             g_entries.push_back(e);
             ids.push_back((int)g_entries.size() - 1);
         }
+        for (size_t q = 0; q < pairs.size(); q++) {
+            const DevPass& p = passes[pairs[q]];
+            JitEntry e;
+            e.device = dev;
+            e.TB = 1 << p.tb_bits;
+            e.E = 1 << (p.Tp - p.tb_bits);
+            e.smem = (size_t)2 * e.TB * e.E * sizeof(float2);
+            const std::string name = "esc_jit_pair" + std::to_string(q);
+            if (!drv(D.moduleGetFunction(&e.fn, mod, name.c_str()), "cuModuleGetFunction", err)) return false;
+            if (!drv(D.funcSetAttribute(e.fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)e.smem),
+                     "cuFuncSetAttribute", err))
+                return false;
+            if (!drv(D.occupancy(&e.per_sm, e.fn, e.TB, e.smem), "cuOccupancyMaxActiveBlocksPerMultiprocessor", err))
+                return false;
+            g_entries.push_back(e);
+            ids.push_back((int)g_entries.size() - 1);
+        }
         it = g_cache.emplace(key, ids).first;
     }
     for (size_t k = 0; k < which.size(); k++) passes[which[k]].jit = it->second[k];
+    for (size_t q = 0; q < pairs.size(); q++) passes[pairs[q]].jit_pair = it->second[which.size() + q];
     return true;
 }
 
@@ -247,6 +294,32 @@ int jit_launch(const DevPass& p, const escdev::PassTab& pt, const void* diag, co
     std::string err;
     if (!drv(driver().launchKernel(e.fn, (unsigned)g, 1, 1, (unsigned)e.TB, 1, 1, (unsigned)e.smem, (CUstream)s, args, nullptr),
              "cuLaunchKernel", err))
+        throw CudaError(err);
+    return (int)g;
+}
+
+int jit_pair_launch(const DevPass& a, const escdev::PassTab& pa, const escdev::PassTab& pb, const escdev::PairTab& st,
+                    const void* diag, const void* in, void* out, int64_t D, int sms, cudaStream_t s, const int* active) {
+    (void)D;
+    JitEntry e;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (a.jit_pair < 0 || a.jit_pair >= (int)g_entries.size()) throw std::invalid_argument("no specialised pair kernel");
+        e = g_entries[a.jit_pair];
+    }
+    const long long items = (2 * st.nslab) << st.inner;
+    const long long g = std::min<long long>(items, (long long)sms * std::max(e.per_sm, 1));
+    if (g <= 0) return 0;
+    escdev::PassTab ta = pa, tb = pb;
+    escdev::PairTab tp = st;
+    const float* dg = (const float*)diag;
+    const float2* vin = (const float2*)in;
+    float2* vout = (float2*)out;
+    const int* act = active;
+    void* args[] = {&ta, &tb, &tp, &dg, &vin, &vout, &act};
+    std::string err;
+    if (!drv(driver().launchCooperative(e.fn, (unsigned)g, 1, 1, (unsigned)e.TB, 1, 1, (unsigned)e.smem, (CUstream)s, args),
+             "cuLaunchCooperativeKernel", err))
         throw CudaError(err);
     return (int)g;
 }

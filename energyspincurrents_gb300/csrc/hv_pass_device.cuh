@@ -198,6 +198,17 @@ __device__ __forceinline__ void issue_tile(const PassTab& p, const float2* __res
     }
 }
 
+// copies the float tile b (4 states per 16-byte copy: half a run of 8) of x into dst (tile layout)
+template <int E, int TB>
+__device__ __forceinline__ void issue_tile_f32(const PassTab& p, const float* __restrict__ x, float* dst,
+                                               unsigned long long b, int tid) {
+#pragma unroll
+    for (int i = 0; i < E / 4; i++) {
+        const int q = tid + TB * i;
+        cp_async16(dst + 4 * q, x + (b | p.tabLo[(q >> 1) & 63] | p.tabHi[q >> 7] | (unsigned long long)((q & 1) << 2)));
+    }
+}
+
 // Sums conj(v) o over a thread's E states of one item in float-float and adds them to the
 // column's accumulators (alpha epilogue).
 template <int E, int TB>
@@ -304,6 +315,101 @@ __device__ __forceinline__ void pass_body_staged(const PassTab& p, const Terms& 
     if (p.dotp) da.store(p, cmask, tid, TB / 32);
 }
 
+// 2-stage tile ring + staging area, one item ahead (see pass_body, NS = 5).
+template <int E, int TB, class Terms>
+__device__ __forceinline__ void pass_body_ahead(const PassTab& p, const Terms& terms, const float* __restrict__ diag,
+                                                const float2* __restrict__ in, float2* __restrict__ out,
+                                                long long ntiles, const int* __restrict__ active) {
+    const unsigned cmask = column_mask(p, active);
+    if (!cmask) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* bufs = reinterpret_cast<float2*>(smem_raw);   // 2 x (TB E) states
+    float2* stage = bufs + 2 * TB * E;                     // TB E partials (or diagonal entries)
+    __shared__ unsigned long long hi_off[E];
+    __shared__ float dsm[MAXC][32][4];
+    DotAcc da{dsm};
+    const int tid = threadIdx.x;
+    unsigned long long lo, lo2[2];
+    tile_offsets<E, TB>(p, tid, hi_off, lo, lo2);
+    if (p.dotp) da.clear(tid, TB);
+    __syncthreads();
+    const long long g = gridDim.x;
+    const long long ld = p.ld;
+    const int c0 = __ffs((int)cmask) - 1;
+    const unsigned long long dg = tile_bits(p, g);
+    auto advance = [&](long long& tt, int& cc, unsigned long long& bb) {
+        const int nx = next_column(cmask, cc);
+        if (nx >= 0) {
+            cc = nx;
+        } else {
+            cc = c0;
+            tt += g;
+            bb = deposit_add(bb, dg, p.rmask);
+        }
+    };
+    // copies of item (tt, cc): its tile into buffer `slot`, the same tile of the partial result (or
+    // of the diagonal) into the staging area, in tile layout
+    auto issue = [&](long long tt, int cc, unsigned long long bb, int slot) {
+        if (tt < ntiles) {
+            issue_tile<E, TB>(p, in + cc * ld, bufs + slot * (TB * E), bb, tid, lo2);
+            if (p.diag) issue_tile_f32<E, TB>(p, diag, reinterpret_cast<float*>(stage), bb, tid);
+            else if (p.accumulate) issue_tile<E, TB>(p, out + cc * ld, stage, bb, tid, lo2);
+        }
+        cp_async_commit();
+    };
+    long long t = blockIdx.x;
+    int c = c0;
+    unsigned long long bt = tile_bits(p, t);
+    issue(t, c, bt, 0);
+    long long tn = t;
+    int cn = c;
+    unsigned long long bn = bt;
+    advance(tn, cn, bn);
+    for (int cur = 0; t < ntiles; cur ^= 1) {
+        cp_async_wait<0>();
+        __syncthreads();   // item t's tile (every thread's copies) has landed; buffer cur^1 is free
+        float2 pre[E];
+        float dpre[E];
+#pragma unroll
+        for (int j = 0; j < E; j++) {
+            if (p.diag) dpre[j] = reinterpret_cast<const float*>(stage)[tid + TB * j];
+            else if (p.accumulate) pre[j] = stage[tid + TB * j];
+        }
+        __syncthreads();   // every thread's staging reads are performed before the area is refilled
+        issue(tn, cn, bn, cur ^ 1);   // [item t+1]
+        float2* tile = bufs + cur * (TB * E);
+        float2* outc = out + c * ld;
+        const unsigned long long base = bt | lo;
+        const float2 vfx = make_float2(p.fx[c], p.fx[c]);
+        const float fy = p.fy[c], fz = p.fz[c];
+        float2 acc[E];
+#pragma unroll
+        for (int j = 0; j < E; j++) acc[j] = make_float2(0.f, 0.f);
+        terms(tile, tid, vfx, fy, acc);
+#pragma unroll
+        for (int j = 0; j < E; j++) {
+            const unsigned long long k = base | hi_off[j];
+            float2 o = acc[j];
+            if (p.diag) {
+                const float dgv = fmaf(fz, (float)(p.N - 2 * __popcll(k)), dpre[j]);
+                const float2 v = tile[tid + TB * j];
+                o.x = fmaf(dgv, v.x, o.x);
+                o.y = fmaf(dgv, v.y, o.y);
+            } else if (p.accumulate) {
+                o.x += pre[j].x;
+                o.y += pre[j].y;
+            }
+            outc[k] = o;
+            acc[j] = o;
+        }
+        if (p.dotp) dot_item<E, TB>(da, c, tid, tile, acc);
+        t = tn; c = cn; bt = bn;
+        advance(tn, cn, bn);
+    }
+    cp_async_wait<0>();
+    if (p.dotp) da.store(p, cmask, tid, TB / 32);
+}
+
 // One pass over all tiles.  Terms: functor terms(tile, tid, vfx, fy, acc) adding the off-diagonal
 // terms of the pass for the thread's E states.  diag (pass 1): bond part of the diagonal per state.
 // NS-stage ring of tile buffers: the next NS-1 items are in flight while one is computed; every
@@ -314,12 +420,22 @@ __device__ __forceinline__ void pass_body_staged(const PassTab& p, const Terms& 
 // partial result of the earlier passes, or the bond diagonal in pass 1): they are copied with
 // cp.async as well, so no register holds them while the terms are applied and the compiler cannot
 // sink them next to their use.  Commit order per iteration: [partials of item i] [tile of item i+1].
+//
+// NS = 5 runs the same two tile buffers and staging area one item ahead, with the partials (or the
+// diagonal) copied as a tile, in 16-byte runs like the input: at the top of item i each thread
+// moves its states' staged partials into registers, and then the copies of item i+1's tile and
+// partials are issued, so they are in flight while item i is computed and stored, and neither the
+// terms nor the epilogue of an item waits for DRAM.
 template <int E, int NS, class Terms, int TB = TPB>
 __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, const float* __restrict__ diag,
                                           const float2* __restrict__ in, float2* __restrict__ out, long long ntiles,
                                           const int* __restrict__ active) {
     if constexpr (NS == 4) {
         pass_body_staged<E, TB>(p, terms, diag, in, out, ntiles, active);
+        return;
+    }
+    if constexpr (NS == 5) {
+        pass_body_ahead<E, TB>(p, terms, diag, in, out, ntiles, active);
         return;
     }
     const unsigned cmask = column_mask(p, active);
@@ -401,6 +517,191 @@ __device__ __forceinline__ void pass_body(const PassTab& p, const Terms& terms, 
     }
     cp_async_wait<0>();
     if (p.dotp) da.store(p, cmask, tid, TB / 32);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Slab pairs.  Two passes A and B whose tiles together span U bits run in one launch over slabs of
+// 2^U states (the states that agree on the other N - U bits): a slab's tiles of A, then its tiles
+// of B, which read the partial result that A wrote into the slab.  At U = 21 a slab is 16 MB of
+// complex64 states, so B finds the slab's input and A's partial result in the L2 cache: for the two
+// passes, DRAM sees one read of the input, one read of the earlier partial (or the diagonal) and
+// one write of the result, as for a single pass.
+//
+// Items (one tile of one pass each) are dealt round-robin to the CTAs in the order
+//     A(0) | A(1) B(0) | A(2) B(1) | ... | A(S-1) B(S-2) | B(S-1)
+// (A(s): the 2^(U-T) tiles of A in slab s), so B(s) begins one slab after A(s).  Before computing
+// a tile of B(s), a CTA waits until every tile of A(s) has been written (a per-slab counter,
+// raised after a tile's stores with a fence).  The launch is cooperative, so all CTAs are
+// resident, and every tile that a wait depends on comes earlier in the order and waits for
+// nothing itself: the waits end.  Each wait still gives up after about a second, sets *err and
+// lets the launch finish (with a wrong result, which the host reports).
+struct PairTab {
+    unsigned char rest[2][40];   // per pass: global bits of the tile number, slab-internal bits first
+    int nrest;                   // N - T
+    int inner;                   // U - T: log2 of the tiles of one pass in one slab
+    long long nslab;             // 2^(N - U)
+    unsigned* cnt;               // [nslab] tiles of A written, per slab (zero at launch)
+    unsigned* err;               // set to 1 by a wait that gave up
+    unsigned need;               // tiles of A per slab: 2^inner
+};
+
+// item k -> pass (sec = 0: A, 1: B), slab s and tile number t = s 2^inner + (tile in slab)
+__device__ __forceinline__ void pair_item(const PairTab& st, long long k, int& sec, long long& s, long long& t) {
+    const long long q = k >> st.inner;
+    if (q == 0) {
+        sec = 0; s = 0;
+    } else if (q == 2 * st.nslab - 1) {
+        sec = 1; s = st.nslab - 1;
+    } else if (q & 1) {
+        sec = 0; s = (q + 1) >> 1;
+    } else {
+        sec = 1; s = (q >> 1) - 1;
+    }
+    t = (s << st.inner) | (k & ((1ll << st.inner) - 1));
+}
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+// Waits until *cnt >= need.  Gives up after about one second (and after 2^24 polls whatever the
+// timer says), setting *err; returns at once once an earlier wait of the launch has given up.
+static __device__ __noinline__ void wait_slab(const unsigned* cnt, unsigned need, unsigned* err) {
+    if (ld_acquire_u32(cnt) >= need) return;
+    const unsigned long long t0 = globaltimer_ns();
+    for (unsigned it = 0; it < (1u << 24); it++) {
+        __nanosleep(200);
+        if (ld_acquire_u32(cnt) >= need) return;
+        if ((it & 63) == 0) {
+            if (ld_acquire_u32(err)) return;
+            if (globaltimer_ns() - t0 > 1000000000ull) break;
+        }
+    }
+    atomicExch(err, 1u);
+}
+
+// One launch of a slab pair (single column, 2 tile buffers).  Per state the same operations in the
+// same order as pass_body, so the result is bit-identical to the two passes run one after the other.
+// The per-pass tables the items need (tile-number bits, run offsets) are copied to shared memory
+// once, so an item's addresses cost a few shared-memory loads.
+template <int E, int TB, class TermsA, class TermsB>
+__device__ __forceinline__ void pair_body(const PassTab& pa, const PassTab& pb, const PairTab& st, const TermsA& ta,
+                                          const TermsB& tb, const float* __restrict__ diag,
+                                          const float2* __restrict__ in, float2* __restrict__ out,
+                                          const int* __restrict__ active) {
+    if (active && !active[0]) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* bufs = reinterpret_cast<float2*>(smem_raw);   // 2 x (TB E) states
+    __shared__ unsigned long long hi_off[2][E];
+    __shared__ unsigned long long s_lo[2][64], s_hi[2][16];   // PassTab::tabLo / tabHi of A and B
+    __shared__ unsigned long long lut[2][5][64];              // tile number, 6 bits at a time -> global bits
+    __shared__ float dsm[MAXC][32][4];
+    DotAcc da{dsm};
+    const int tid = threadIdx.x;
+    if (tid < E) {
+        hi_off[0][tid] = pa.tabLo[((TB * tid) >> 3) & 63] | pa.tabHi[(TB * tid) >> 9];
+        hi_off[1][tid] = pb.tabLo[((TB * tid) >> 3) & 63] | pb.tabHi[(TB * tid) >> 9];
+    }
+    for (int i = tid; i < 64; i += TB) {
+        s_lo[0][i] = pa.tabLo[i];
+        s_lo[1][i] = pb.tabLo[i];
+    }
+    for (int i = tid; i < 16; i += TB) {
+        s_hi[0][i] = pa.tabHi[i];
+        s_hi[1][i] = pb.tabHi[i];
+    }
+    for (int i = tid; i < 2 * 5 * 64; i += TB) {
+        const int x = i / 320, c = (i / 64) % 5, v = i & 63;
+        unsigned long long b = 0;
+        for (int q = 0; q < 6; q++)
+            if (6 * c + q < st.nrest && ((v >> q) & 1)) b |= 1ull << st.rest[x][6 * c + q];
+        lut[x][c][v] = b;
+    }
+    if (pb.dotp) da.clear(tid, TB);
+    __syncthreads();
+    auto tile_of = [&](int x, long long t) {
+        return lut[x][0][t & 63] | lut[x][1][(t >> 6) & 63] | lut[x][2][(t >> 12) & 63] | lut[x][3][(t >> 18) & 63] |
+               lut[x][4][(t >> 24) & 63];
+    };
+    const long long g = gridDim.x;
+    const long long total = (2 * st.nslab) << st.inner;
+    long long ki = blockIdx.x;   // issue cursor
+    auto issue = [&](int slot) {
+        if (ki < total) {
+            int sec;
+            long long s, t;
+            pair_item(st, ki, sec, s, t);
+            const unsigned long long b = tile_of(sec, t);
+            const unsigned long long l0 = s_lo[sec][(tid >> 2) & 63] | (unsigned long long)((2 * tid) & 7);
+            const unsigned long long l1 = s_lo[sec][((tid >> 2) + 32) & 63] | (unsigned long long)((2 * tid) & 7);
+            float2* dst = bufs + slot * (TB * E);
+#pragma unroll
+            for (int i = 0; i < E / 2; i++) {   // as issue_tile
+                const unsigned long long l = (TB == 128 && (i & 1)) ? l1 : l0;
+                cp_async16(dst + 2 * (tid + TB * i), in + (b | l | s_hi[sec][(tid + TB * i) >> 8]));
+            }
+        }
+        cp_async_commit();
+        ki += g;
+    };
+    const int N = pa.N;
+    const float2 vfx = make_float2(pa.fx[0], pa.fx[0]);
+    const float fy = pa.fy[0], fz = pa.fz[0];
+    issue(0);
+    int cur = 0;
+    for (long long k = blockIdx.x; k < total; k += g, cur ^= 1) {
+        issue(cur ^ 1);
+        int sec;
+        long long s, t;
+        pair_item(st, k, sec, s, t);
+        if (sec && tid == 0) wait_slab(st.cnt + s, st.need, st.err);
+        cp_async_wait<1>();
+        __syncthreads();
+        const unsigned long long base =
+            tile_of(sec, t) | s_lo[sec][(tid >> 3) & 63] | s_hi[sec][tid >> 9] | (unsigned long long)(tid & 7);
+        const unsigned long long* ho = hi_off[sec];
+        float2* tile = bufs + cur * (TB * E);
+        const int pdiag = sec ? pb.diag : pa.diag, pacc = sec ? pb.accumulate : pa.accumulate;
+        float2 acc[E], pre[E];
+        float dpre[E];
+#pragma unroll
+        for (int j = 0; j < E; j++) {
+            acc[j] = make_float2(0.f, 0.f);
+            if (pdiag) dpre[j] = diag[base | ho[j]];
+            else if (pacc) pre[j] = __ldcg(out + (base | ho[j]));
+        }
+        if (sec) tb(tile, tid, vfx, fy, acc);
+        else ta(tile, tid, vfx, fy, acc);
+#pragma unroll
+        for (int j = 0; j < E; j++) {
+            const unsigned long long kk = base | ho[j];
+            float2 o = acc[j];
+            if (pdiag) {
+                const float dgv = fmaf(fz, (float)(N - 2 * __popcll(kk)), dpre[j]);
+                const float2 v = tile[tid + TB * j];
+                o.x = fmaf(dgv, v.x, o.x);
+                o.y = fmaf(dgv, v.y, o.y);
+            } else if (pacc) {
+                o.x += pre[j].x;
+                o.y += pre[j].y;
+            }
+            out[kk] = o;
+            acc[j] = o;
+        }
+        if (sec && pb.dotp) dot_item<E, TB>(da, 0, tid, tile, acc);
+        __syncthreads();   // buffer `cur` is refilled by the next iteration's prefetch
+        if (!sec && tid == 0) {
+            __threadfence();   // the tile's stores (ordered before by the barrier) before the count
+            atomicAdd(st.cnt + s, 1u);
+        }
+    }
+    cp_async_wait<0>();
+    if (pb.dotp) da.store(pb, 1u, tid, TB / 32);
 }
 
 }  // namespace escdev

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -509,6 +510,52 @@ __global__ void __launch_bounds__(TB, TB * E >= 8192 ? 1 : 2) k_hv_pass_f32g(con
     escdev::pass_body<E, NS, RuntimeTerms<E, TB>, TB>(pt, RuntimeTerms<E, TB>{p}, diag, in, out, ntiles, active);
 }
 
+// Slab pair of two grouped passes (hv_pass_device.cuh: pair_body), ahead of time: 2 tile buffers,
+// one CTA per SM for 8192-state tiles, two for 4096.  Launched cooperatively.
+template <int E, int TB>
+__global__ void __launch_bounds__(TB, TB * E >= 8192 ? 1 : 2) k_hv_pair_f32g(const __grid_constant__ escdev::PassTab pa,
+                                                      const __grid_constant__ escdev::PassTab pb,
+                                                      const __grid_constant__ escdev::PairTab st,
+                                                      const __grid_constant__ DevPass a,
+                                                      const __grid_constant__ DevPass b,
+                                                      const float* __restrict__ diag,
+                                                      const float2* __restrict__ in,
+                                                      float2* __restrict__ out, const int* __restrict__ active) {
+    escdev::pair_body<E, TB>(pa, pb, st, RuntimeTerms<E, TB>{a}, RuntimeTerms<E, TB>{b}, diag, in, out, active);
+}
+
+escdev::PairTab make_pair_tab(const DevPass& a, const DevPass& b, int N, unsigned* sync) {
+    escdev::PairTab t;
+    std::memset(&t, 0, sizeof(t));
+    const unsigned long long all = N >= 64 ? ~0ull : (1ull << N) - 1ull;
+    unsigned long long ra = 0, rb = 0;
+    for (int q = 0; q < a.nrest; q++) ra |= 1ull << a.rest[q];
+    for (int q = 0; q < b.nrest; q++) rb |= 1ull << b.rest[q];
+    const unsigned long long ta = all & ~ra, tb = all & ~rb, u = ta | tb;
+    const int U = __builtin_popcountll(u);
+    if (a.Tp != b.Tp || a.nrest != b.nrest || a.nrest > 30 || U >= N || U - a.Tp > 30)
+        throw std::invalid_argument("passes cannot form a slab pair");
+    t.nrest = a.nrest;
+    t.inner = U - a.Tp;
+    t.nslab = 1ll << (N - U);
+    // tile number: slab-internal bits (the other pass's tile bits) first, then the slab bits
+    const unsigned long long inner[2] = {tb & ~ta, ta & ~tb};
+    for (int x = 0; x < 2; x++) {
+        int n = 0;
+        for (int q = 0; q < N; q++)
+            if ((inner[x] >> q) & 1ull) t.rest[x][n++] = (unsigned char)q;
+        for (int q = 0; q < N; q++)
+            if (!((u >> q) & 1ull)) t.rest[x][n++] = (unsigned char)q;
+    }
+    t.err = sync;
+    t.cnt = sync + SLAB_CNT0;
+    t.need = 1u << t.inner;
+    // test hook: a count that is never reached, so that every wait of the launch gives up
+    if (const char* e = std::getenv("ESC_TEST_SLAB_STALL"))
+        if (std::atoi(e) > 0) t.need += 1;
+    return t;
+}
+
 escdev::PassTab make_pass_tab(const DevPass& p, const DevModel& m, const DevCols* cols, double* dotp) {
     escdev::PassTab t;
     std::memset(&t, 0, sizeof(t));
@@ -751,7 +798,7 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_o
         DevPass& d = out[pi];
         std::memset(&d, 0, sizeof(d));
         d.jit = -1;
-        d.stages = stages >= 2 && stages <= 4 ? stages : pass_stages();
+        d.stages = stages >= 2 && stages <= 5 ? stages : pass_stages();
         d.tb_bits = tb_bits;
         std::vector<int> B = P.tiles[pi];
         d.Tp = (int)B.size();
@@ -862,8 +909,30 @@ std::vector<DevPass> make_passes(const Plan& P, const DevModel& m, int balance_o
             d.gnt[d.ngroup] = (unsigned char)n;
             d.ngroup++;
         }
+        d.jit_pair = -1;
     }
+    if (slab_pairs_env() == 1) mark_pairs(out, P.N);
     return out;
+}
+
+void mark_pairs(std::vector<DevPass>& ps, int N) {
+    const unsigned long long all = N >= 64 ? ~0ull : (1ull << N) - 1ull;
+    std::vector<unsigned long long> tm(ps.size(), all);
+    for (size_t i = 0; i < ps.size(); i++) {
+        ps[i].pair = 0;
+        ps[i].slab_bits = 0;
+        for (int q = 0; q < ps[i].nrest; q++) tm[i] &= ~(1ull << ps[i].rest[q]);
+    }
+    for (size_t pi = 0; pi + 1 < ps.size();) {
+        const int ub = __builtin_popcountll(tm[pi] | tm[pi + 1]);
+        if (ub <= SLAB_MAX_BITS && ub < N && ps[pi].Tp == ps[pi + 1].Tp && ps[pi].c == 3 && ps[pi + 1].c == 3) {
+            ps[pi].pair = 1;
+            ps[pi].slab_bits = ub;
+            pi += 2;
+        } else {
+            pi++;
+        }
+    }
 }
 
 template <typename R>
@@ -909,8 +978,8 @@ static void run_f32(const DevModel& m, const DevPass& p, const void* diag, const
 template <int E, int NS, int TB = TILE_THREADS>
 static int run_f32g(const escdev::PassTab& pt, const DevPass& p, const void* diag, const void* in, void* out, int64_t D,
                     int sms, cudaStream_t s, const int* active) {
-    // NS-stage ring of tiles (NS = 4: 2 tiles + staging of the epilogue loads)
-    const size_t smem = (size_t)(NS == 4 ? 3 : NS) * TB * E * sizeof(float2);
+    // NS-stage ring of tiles (NS = 4, 5: 2 tiles + staging of the epilogue loads)
+    const size_t smem = (size_t)(NS >= 4 ? 3 : NS) * TB * E * sizeof(float2);
     // always raised: dynamic + static shared memory may pass 48 KB even when the ring alone does not
     ESC_CUDA(cudaFuncSetAttribute(k_hv_pass_f32g<E, NS, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
@@ -926,7 +995,7 @@ static int run_f32g(const escdev::PassTab& pt, const DevPass& p, const void* dia
 int pass_stages() {
     const char* e = std::getenv("ESC_STAGES");
     const int x = e ? std::atoi(e) : 2;
-    return x >= 2 && x <= 4 ? x : 2;
+    return x >= 2 && x <= 5 ? x : 2;
 }
 
 // Grouped complex64 pass (ahead of time): E = 2^(Tp - tb_bits) states per thread; returns the grid,
@@ -938,6 +1007,14 @@ static int run_grouped(const escdev::PassTab& pt, const DevPass& p, const void* 
         return 0;
     switch ((p.tb_bits == 8 ? 100 : p.tb_bits == 7 ? 200 : p.tb_bits == 10 ? 300 : 0) + (p.Tp == 11 ? 10 : p.Tp == 12 ? 20 : 30) +
             p.stages) {
+        case 335: return run_f32g<8, 5, 1024>(pt, p, diag, in, out, D, sms, s, active);
+        case 35: return run_f32g<16, 5, 512>(pt, p, diag, in, out, D, sms, s, active);
+        case 215: return run_f32g<16, 5, 128>(pt, p, diag, in, out, D, sms, s, active);
+        case 225: return run_f32g<32, 5, 128>(pt, p, diag, in, out, D, sms, s, active);
+        case 15: return run_f32g<4, 5>(pt, p, diag, in, out, D, sms, s, active);
+        case 25: return run_f32g<8, 5>(pt, p, diag, in, out, D, sms, s, active);
+        case 115: return run_f32g<8, 5, 256>(pt, p, diag, in, out, D, sms, s, active);
+        case 125: return run_f32g<16, 5, 256>(pt, p, diag, in, out, D, sms, s, active);
         case 332: return run_f32g<8, 2, 1024>(pt, p, diag, in, out, D, sms, s, active);
         case 333: return run_f32g<8, 3, 1024>(pt, p, diag, in, out, D, sms, s, active);
         case 334: return run_f32g<8, 4, 1024>(pt, p, diag, in, out, D, sms, s, active);
@@ -965,6 +1042,43 @@ static int run_grouped(const escdev::PassTab& pt, const DevPass& p, const void* 
     }
 }
 
+template <int E, int TB>
+static int run_pair_aot(const escdev::PassTab& pa, const escdev::PassTab& pb, const escdev::PairTab& st, const DevPass& a,
+                        const DevPass& b, const void* diag, const void* in, void* out, int sms, cudaStream_t s,
+                        const int* active) {
+    const size_t smem = (size_t)2 * TB * E * sizeof(float2);
+    ESC_CUDA(cudaFuncSetAttribute(k_hv_pair_f32g<E, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    ESC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_hv_pair_f32g<E, TB>, TB, smem));
+    const long long items = (2 * st.nslab) << st.inner;
+    const long long g = std::min<long long>(items, (long long)sms * std::max(per_sm, 1));
+    const float* dg = (const float*)diag;
+    const float2* vin = (const float2*)in;
+    float2* vout = (float2*)out;
+    void* args[] = {(void*)&pa, (void*)&pb, (void*)&st, (void*)&a, (void*)&b, (void*)&dg, (void*)&vin, (void*)&vout,
+                    (void*)&active};
+    ESC_CUDA(cudaLaunchCooperativeKernel((const void*)k_hv_pair_f32g<E, TB>, dim3((unsigned)g), dim3(TB), args, smem, s));
+    return (int)g;
+}
+
+static std::atomic<unsigned long long> g_pair_launches{0};
+unsigned long long slab_pair_launches() { return g_pair_launches.load(); }
+
+// Slab pair of passes a (a.pair set) and b on one complex64 column; returns the grid, or 0 when
+// no pair kernel exists for their shape (the caller then runs the passes one by one).
+static int run_pair(const DevModel& m, const DevPass& a, const DevPass& b, const DevCols& cols, double* dotp,
+                    const void* diag, const void* in, void* out, int64_t D, int sms, cudaStream_t s, const int* active) {
+    const bool aot = a.tb_bits == 9 && b.tb_bits == 9 && (a.Tp == 13 || a.Tp == 12);
+    if (!m.slab_sync || (a.jit_pair < 0 && !aot)) return 0;
+    const escdev::PairTab st = make_pair_tab(a, b, m.N, m.slab_sync);
+    const escdev::PassTab pa = make_pass_tab(a, m, &cols, nullptr), pb = make_pass_tab(b, m, &cols, dotp);
+    ESC_CUDA(cudaMemsetAsync(st.cnt, 0, (size_t)st.nslab * sizeof(unsigned), s));
+    g_pair_launches++;
+    if (a.jit_pair >= 0) return jit_pair_launch(a, pa, pb, st, diag, in, out, D, sms, s, active);
+    if (a.Tp == 13) return run_pair_aot<16, 512>(pa, pb, st, a, b, diag, in, out, sms, s, active);
+    return run_pair_aot<8, 512>(pa, pb, st, a, b, diag, in, out, sms, s, active);
+}
+
 template <typename R>
 int launch_hv_cols(const DevModel& m, const DevCols& cols, const std::vector<DevPass>& passes, const void* in, void* out,
                    int64_t D, const void* diag, cudaStream_t s, const int* active) {
@@ -976,6 +1090,17 @@ int launch_hv_cols(const DevModel& m, const DevCols& cols, const std::vector<Dev
     int G = 0;
     for (size_t pi = 0; pi < passes.size(); pi++) {
         const DevPass& p = passes[pi];
+        if constexpr (sizeof(R) == 4) {
+            if (p.pair && pi + 1 < passes.size() && cols.ncols == 1 && diag) {
+                double* dotp2 = pi + 2 == passes.size() ? cols.dotp : nullptr;
+                const int g2 = run_pair(m, p, passes[pi + 1], cols, dotp2, diag, in, out, D, sms, s, active);
+                if (g2) {
+                    if (dotp2) G = g2;
+                    pi++;
+                    continue;
+                }
+            }
+        }
         double* dotp = pi + 1 == passes.size() ? cols.dotp : nullptr;
         int g = 0;   // grid of a launch that handled every column (and the alpha epilogue)
         if constexpr (sizeof(R) == 4) {

@@ -10,11 +10,14 @@
 //      covering with one cluster less at a time by simulated annealing,
 //   3. numbers the sites so that pass 1 is the contiguous block of the T lowest bits and each later
 //      pass's new sites are contiguous too,
-//   4. assigns every term to the first pass whose tile contains it (the diagonal to pass 1).
+//   4. assigns every term to the first pass whose tile contains it (the diagonal to pass 1),
+//   5. from 27 sites on, orders the passes in pairs whose tiles span few bits together, for the
+//      slab-pair launches of hv_tiled.cu.
 // The relabelled model is the same Hamiltonian; only vectors crossing the C ABI are permuted.
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <numeric>
@@ -310,12 +313,76 @@ Plan make_plan(int N, const std::vector<std::pair<int, int>>& bonds, int T, int 
     {
         std::lock_guard<std::mutex> lk(mu);
         const auto it = cache.find(key);
-        if (it != cache.end()) return it->second;
+        if (it != cache.end()) {
+            Plan P = it->second;
+            order_for_pairs(P);
+            return P;
+        }
     }
     Plan P = search_plan(N, bonds, T, c, restarts, anneal_more);
-    std::lock_guard<std::mutex> lk(mu);
-    cache.emplace(key, P);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        cache.emplace(key, P);
+    }
+    order_for_pairs(P);
     return P;
+}
+
+int slab_pairs_env() {
+    const char* e = std::getenv("ESC_SLAB_PAIRS");
+    if (!e || !*e) return -1;
+    return std::atoi(e) != 0 ? 1 : 0;
+}
+
+// Pairs of passes for the slab-pair launches: the matching with the most pairs spanning at most
+// SLAB_MAX_BITS bits, then the fewest bits in total (every matching of the at most a few passes is
+// tried).  New order: the pair holding the first pass (first pass first), the other pairs, then the
+// passes left alone.  The first pass keeps the diagonal, and every pass keeps its tile, so only
+// the pass each term is assigned to (the first that holds it) and the order of the additions change.
+void order_for_pairs(Plan& P) {
+    const int np = (int)P.tiles.size();
+    if (np < 2 || np > 12 || (P.N < SLAB_MIN_SITES && slab_pairs_env() < 0)) return;
+    std::vector<unsigned long long> tm(np, 0);
+    for (int i = 0; i < np; i++)
+        for (int b : P.tiles[i]) tm[i] |= 1ull << b;
+    auto ubits = [&](int a, int b) { return __builtin_popcountll(tm[a] | tm[b]); };
+    std::vector<int> mate(np, -1), best_mate(np, -1);
+    int best_pairs = -1, best_bits = 1 << 30;
+    std::function<void(int, int, int)> rec = [&](int i, int pairs, int bits) {
+        while (i < np && mate[i] != -1) i++;
+        if (i == np) {
+            if (pairs > best_pairs || (pairs == best_pairs && bits < best_bits)) {
+                best_pairs = pairs;
+                best_bits = bits;
+                best_mate = mate;
+            }
+            return;
+        }
+        mate[i] = i;   // alone
+        rec(i + 1, pairs, bits);
+        for (int j = i + 1; j < np; j++)
+            if (mate[j] == -1 && ubits(i, j) <= SLAB_MAX_BITS) {
+                mate[i] = j;
+                mate[j] = i;
+                rec(i + 1, pairs + 1, bits + ubits(i, j));
+                mate[j] = -1;
+            }
+        mate[i] = -1;
+    };
+    rec(0, 0, 0);
+    if (best_pairs <= 0) return;
+    std::vector<int> order;
+    std::vector<char> used(np, 0);
+    auto take = [&](int i) { order.push_back(i); used[i] = 1; };
+    take(0);
+    if (best_mate[0] != 0) take(best_mate[0]);
+    for (int i = 1; i < np; i++)
+        if (!used[i] && best_mate[i] != i) { take(i); take(best_mate[i]); }
+    for (int i = 1; i < np; i++)
+        if (!used[i]) take(i);
+    std::vector<std::vector<int>> tiles;
+    for (int i : order) tiles.push_back(P.tiles[i]);
+    P.tiles = tiles;
 }
 
 namespace {

@@ -24,6 +24,37 @@ std::string tune_key(const esc_handle* h) {
     return k.str();
 }
 
+// Slab pairs of a composite (passes picked from several variant sets): one specialised module for
+// the composite, so that a pair kernel joins the two passes as they are; passes the tuner picked
+// ahead of time stay ahead of time.
+std::vector<esc::DevPass> with_pairs(const std::vector<esc::DevPass>& comp, int N) {
+    std::vector<esc::DevPass> cp = comp;
+    esc::mark_pairs(cp, N);
+    bool jit = false;
+    for (auto& p : cp) {
+        jit = jit || p.jit >= 0;
+        p.jit_pair = -1;
+    }
+    std::string err;
+    if (jit && esc::jit_compile(cp, err))
+        for (size_t i = 0; i < cp.size(); i++)
+            if (comp[i].jit < 0) cp[i].jit = -1;
+    return cp;
+}
+std::vector<esc::DevPass> without_pairs(const std::vector<esc::DevPass>& comp) {
+    std::vector<esc::DevPass> cu = comp;
+    for (auto& p : cu) {
+        p.pair = 0;
+        p.jit_pair = -1;
+    }
+    return cu;
+}
+bool has_pairs(const std::vector<esc::DevPass>& ps) {
+    for (const auto& p : ps)
+        if (p.pair) return true;
+    return false;
+}
+
 void save_tuning(const esc_handle* h, int T, int balance, const std::vector<esc::DevPass>& ps) {
     const char* f = std::getenv("ESC_TUNE_FILE");
     if (!f || !*f) return;
@@ -31,7 +62,7 @@ void save_tuning(const esc_handle* h, int T, int balance, const std::vector<esc:
     if (!fp) return;
     std::fprintf(fp, "%s | %d %d %d |", tune_key(h).c_str(), T, balance, (int)ps.size());
     for (const auto& p : ps) std::fprintf(fp, " %d,%d,%d", p.jit >= 0 ? 1 : 0, p.stages, p.tb_bits);
-    std::fprintf(fp, " | %d\n", h->cols_per_launch);
+    std::fprintf(fp, " | %d | %d\n", h->cols_per_launch, has_pairs(ps) ? 1 : 0);
     std::fclose(fp);
 }
 
@@ -60,8 +91,9 @@ bool load_tuning(esc_handle* h) {
         in >> v[0] >> c1 >> v[1] >> c2 >> v[2];
     }
     if (!in || T < 4) return false;
-    int k = 0;
+    int k = 0, pairs = 0;
     if (in >> bar >> k && bar == '|' && k >= 1 && k <= esc::MAX_COLS) h->cols_per_launch = k;
+    if (!(in >> bar >> pairs) || bar != '|') pairs = 0;
     const esc::Plan plan = esc::make_plan(h->N, bond_pairs(h), T, 3, 200);
     if ((int)plan.tiles.size() != n) return false;
     install_plan(h, plan, balance, 2);
@@ -80,7 +112,7 @@ bool load_tuning(esc_handle* h) {
         const auto it = built.find(var[p][0] ? std::array<int, 2>{-k[0], k[1]} : k);
         comp[p] = (it != built.end() ? it->second : built[k])[p];
     }
-    h->passes = comp;
+    h->passes = pairs && h->dm.slab_sync ? with_pairs(comp, h->N) : without_pairs(comp);
     return true;
 }
 
@@ -97,7 +129,7 @@ std::string verify_composite(esc_handle* h, const esc::Plan& plan, int balance, 
     char* b = a + (size_t)D * 8;
     esc::launch_start_normal<float>(4242, v, D, h->stream);
     const void* dg = diag_for(h, ESC_C64);
-    const std::vector<esc::DevPass> ref = esc::make_passes(plan, h->dm, balance, 2, 9);
+    const std::vector<esc::DevPass> ref = without_pairs(esc::make_passes(plan, h->dm, balance, 2, 9));
     esc::launch_hv_tiled<float>(h->dm, h->passes, v, a, D, dg, h->stream);
     esc::launch_hv_tiled<float>(h->dm, ref, v, b, D, dg, h->stream);
     std::vector<float> x((size_t)D * 2), y((size_t)D * 2);
@@ -183,7 +215,7 @@ std::string tune_columns(esc_handle* h) {
 // term-to-pass assignment (make_passes modes 0 and 2; the balanced mode 1 never won).  Kernel variants per plan: ahead-of-time vs run-time specialised;
 // 512, 256 or 128 threads per 4096-state tile (8, 16, 32 register states each), 1024, 512 or 256
 // (the latter specialised only) per 8192-state tile (8, 16, 32); 2 or 3 tile buffers, or 2 plus staged
-// epilogue loads.  Every variant is timed pass by pass (CUDA events on the
+// epilogue loads (issued with the item, or one item ahead).  Every variant is timed pass by pass (CUDA events on the
 // handle's stream, median of 3 after a warm-up); a plan's composite takes the fastest variant of
 // each pass (light and heavy passes prefer different variants) and is timed as a whole; the
 // fastest composite is installed.  All variants compute the same H.v up to complex64 rounding (the
@@ -229,7 +261,7 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
                 std::vector<std::vector<esc::DevPass>> vars;
                 std::vector<std::vector<double>> per;
                 for (int tb : {10, 9, 8, 7})
-                for (int stages : {2, 3, 4})
+                for (int stages : {2, 3, 4, 5})
                     for (int jit : {0, 1}) {
                         // 8192-state tiles: 1024 or 512 threads, or 256 specialised; 4096: 512 / 256 / 128
                         if (T == 13 && (tb == 7 || (tb == 8 && !jit))) continue;
@@ -261,9 +293,18 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
                     rep << " " << (comp[p].jit >= 0 ? "jit" : "aot") << "/" << comp[p].stages << "/" << (1 << comp[p].tb_bits);
                 }
                 install_plan(h, plan, balance, 2);   // model, permutations, diagonal of this plan
-                const double tc = median_ms(comp);
-                rep << ": " << tc << " ms\n";
-                if (tc < best) { best = tc; bplan = plan; bbal = balance; bT = T; bpasses = comp; }
+                const std::vector<esc::DevPass> cu = without_pairs(comp);
+                const double tc = median_ms(cu);
+                rep << ": " << tc << " ms";
+                if (tc < best) { best = tc; bplan = plan; bbal = balance; bT = T; bpasses = cu; }
+                const std::vector<esc::DevPass> cp = h->dm.slab_sync ? with_pairs(comp, h->N) : cu;
+                if (has_pairs(cp)) {
+                    // the same composite with its slab pairs in one launch each
+                    const double tp = median_ms(cp);
+                    rep << ", slab pairs " << tp << " ms";
+                    if (tp < best) { best = tp; bplan = plan; bbal = balance; bT = T; bpasses = cp; }
+                }
+                rep << "\n";
             }
         }
     } catch (...) {
@@ -285,6 +326,11 @@ std::string autotune(esc_handle* h, std::vector<double>* times) {
     if (verified) save_tuning(h, bT, bbal, bpasses);
     rep << "chosen: T=" << bT << " balance=" << bbal << " passes:";
     for (const auto& ps : bpasses) rep << " " << (ps.jit >= 0 ? "jit" : "aot") << "/" << ps.stages << "/" << (1 << ps.tb_bits);
+    if (has_pairs(bpasses)) {
+        int np = 0;
+        for (const auto& ps : bpasses) np += ps.pair ? 1 : 0;
+        rep << " slab pairs " << np;
+    }
     rep << " columns per launch " << h->cols_per_launch << " (" << best << " ms)\n";
     return rep.str();
 }

@@ -36,8 +36,13 @@ typedef enum {
     ESC_ERR_MEMORY = 2,    /* device or host allocation failed / problem too large         */
     ESC_ERR_CUDA = 3,      /* CUDA runtime error                                           */
     ESC_ERR_NUMERIC = 4,   /* eigensolver failure, NaN in alpha/beta (reference: runtime_error) */
-    ESC_ERR_STATE = 5      /* call order (e.g. spectrum before a ground state)             */
-} esc_status;             /* no kernel of this library waits on a flag or barrier, so no call times out */
+    ESC_ERR_STATE = 5,     /* call order (e.g. spectrum before a ground state)             */
+    ESC_ERR_TIMEOUT = 6    /* a wait inside a kernel gave up (slab-pair H.v: the CTAs of one
+                            * launch wait for each other's tiles, each wait at most ~1 s); the
+                            * results of the calls since the last successful synchronisation are
+                            * invalid, the handle stays usable.  Reported by the next call that
+                            * synchronises the handle's stream. */
+} esc_status;
 
 typedef enum { ESC_C128 = 0, ESC_C64 = 1 } esc_dtype;
 

@@ -226,11 +226,15 @@ def c2_handle(g, tile_bits=None, monkeypatch=None):
     return h, int(gs_steps), int(cf_steps)
 
 
+ALT_TILINGS = (11, 13)
+
+
 def spectra_and_envelope(g, keys, monkeypatch):
-    """The GPU's spectra for `keys` and, as the rounding envelope, their difference from the same
-    computation with another tiling (another summation order in every H.v)."""
+    """The GPU's spectra for `keys` with the default plan and with the alternative tilings (another
+    summation order in every H.v, and so another rounding of the ground state and of every CF
+    vector); the largest difference from the default is the rounding envelope."""
     out = {}
-    for tb in (None, 11):
+    for tb in (None,) + ALT_TILINGS:
         h, gs_steps, cf_steps = c2_handle(g, tb, monkeypatch)
         r = h.lanczos_gs(steps=gs_steps, lanctype="GS", reortho=0)    # reference start vector from RandomSeed
         for key, kind in keys:
@@ -268,11 +272,14 @@ def test_c2_fp64_24_sites_vs_oracle(monkeypatch):
             np.testing.assert_allclose(b[:41], g[key + "_cf_b"][c, :41], rtol=1e-5)
     # spectra: 1e-8, or 3x the GPU's own rounding envelope where 500 unconverged CF steps make
     # FP64 runs that differ only in summation order disagree by more
+    res = []
     for key, _ in keys:
-        s, s2 = out[(key, None)], out[(key, 11)]
-        env = np.abs(s - s2).max()
+        s = out[(key, None)]
+        env = max(np.abs(s - out[(key, tb)]).max() for tb in ALT_TILINGS)
         err = np.abs(s - g[key]).max()
         print(f"C2 {key}: max |S_GPU - S_oracle| = {err:.2e}, GPU rounding envelope {env:.2e}")
+        res.append((key, err, env))
+    for key, err, env in res:
         assert err <= max(1e-8, 3 * env), (key, err, env)
 
 
@@ -281,8 +288,8 @@ def test_c2_local_szsz_18_sites_vs_oracle(monkeypatch):
     g = np.load(C2L)
     out = spectra_and_envelope(g, [("SSLocal", "LocalSzSz")], monkeypatch)
     assert abs(out[("gs", None)]["E0"] - g["E0"]) <= 1e-10 * abs(g["E0"])
-    s, s2 = out[("SSLocal", None)], out[("SSLocal", 11)]
-    env = np.abs(s - s2).max()
+    s = out[("SSLocal", None)]
+    env = max(np.abs(s - out[("SSLocal", tb)]).max() for tb in ALT_TILINGS)
     err = np.abs(s - g["SSLocal"]).max()
     print(f"C2 LocalSzSz (18 sites): max |S_GPU - S_oracle| = {err:.2e}, GPU rounding envelope {env:.2e}")
     assert err <= max(1e-8, 3 * env), (err, env)

@@ -438,11 +438,12 @@ def test_two_point_corr_vs_oracle(pair, tmp_path):
         np.testing.assert_allclose(c, g[f"corr_{a}_{b}"], rtol=0, atol=1e-9)
 
 
-@pytest.mark.parametrize("stages", ["3", "4"])
+@pytest.mark.parametrize("stages", ["3", "4", "5"])
 @pytest.mark.parametrize("jit", ["0", "require"])
 def test_pass_variants_bitwise_equal(stages, jit, monkeypatch):
     """The complex64 pass variants (3-stage tile ring; 2 stages + epilogue loads staged through
-    shared memory), ahead-of-time and specialised, give bit-identical H.v to the 2-stage kernel."""
+    shared memory, issued with the item or one item ahead), ahead-of-time and specialised, give
+    bit-identical H.v to the 2-stage kernel."""
     p = kitaev(Lx=3, Ly=6, J=0.1)
     monkeypatch.setenv("ESC_JIT", "0")
     monkeypatch.setenv("ESC_STAGES", "2")
@@ -455,7 +456,7 @@ def test_pass_variants_bitwise_equal(stages, jit, monkeypatch):
 
 
 @pytest.mark.parametrize("tb", ["8", "7"])
-@pytest.mark.parametrize("stages", ["2", "4"])
+@pytest.mark.parametrize("stages", ["2", "4", "5"])
 @pytest.mark.parametrize("jit", ["0", "require"])
 def test_smaller_thread_tiles_match(tb, stages, jit, monkeypatch):
     """Grouped complex64 passes with 256 or 128 threads per 4096-state tile (16 or 32 register
@@ -475,7 +476,7 @@ def test_smaller_thread_tiles_match(tb, stages, jit, monkeypatch):
 
 
 @pytest.mark.parametrize("tb,jit", [("9", "0"), ("9", "require"), ("8", "require"), ("10", "0"), ("10", "require")])
-@pytest.mark.parametrize("stages", ["2", "4"])
+@pytest.mark.parametrize("stages", ["2", "4", "5"])
 def test_8192_state_tiles_match(tb, jit, stages, monkeypatch):
     """Grouped complex64 passes over 8192-state tiles (one CTA per SM; 1024 threads x 8 register
     states, 512 x 16, or 256 x 32 specialised) agree with the oracle to complex64 rounding; the
