@@ -215,14 +215,15 @@ def ground_state_report(esc, sites, steps=200):
             "tuning": tune, "vectors": "complex64, 3 resident + ground state"}
 
 
-def lanczos_step_report(esc, sites, steps=24):
+def lanczos_step_report(esc, sites, steps=24, autotune=True):
     """Cost of one ground-state Lanczos step (complex64, no reorthogonalisation: the H.v passes with
     alpha from the last pass's epilogue, then one update sweep fused with |u|^2) against one H.v,
-    both on the self-tuned passes.  The run is LancType=OnlyEgs, so nothing else is timed."""
+    both on the self-tuned passes (autotune=False: the configuration esc_create applied, e.g. from
+    ESC_TUNE_FILE).  The run is LancType=OnlyEgs, so nothing else is timed."""
     import numpy as np
     import torch
     h = esc.Handle(workload(sites))
-    tune = h.autotune().strip().splitlines()[-1]
+    tune = h.autotune().strip().splitlines()[-1] if autotune else os.environ.get("ESC_TUNE_FILE")
     D = h.D
     v = torch.empty(D, dtype=torch.complex64, device="cuda")
     out = torch.empty_like(v)
@@ -484,7 +485,7 @@ def main():
         print(json.dumps(r), flush=True)
         return
     if args.step_report:
-        print(json.dumps(lanczos_step_report(esc, args.sites)), flush=True)
+        print(json.dumps(lanczos_step_report(esc, args.sites, autotune=not args.no_autotune)), flush=True)
         return
     if args.e2e_report:
         print(json.dumps(e2e_report(esc, args.sites)), flush=True)
