@@ -215,7 +215,7 @@ def ground_state_report(esc, sites, steps=200):
             "tuning": tune, "vectors": "complex64, 3 resident + ground state"}
 
 
-def lanczos_step_report(esc, sites, steps=24, autotune=True):
+def lanczos_step_report(esc, sites, steps=48, autotune=True):
     """Cost of one ground-state Lanczos step (complex64, no reorthogonalisation: the H.v passes with
     alpha from the last pass's epilogue, then one update sweep fused with |u|^2) against one H.v,
     both on the self-tuned passes (autotune=False: the configuration esc_create applied, e.g. from
@@ -243,14 +243,15 @@ def lanczos_step_report(esc, sites, steps=24, autotune=True):
     del v, out
     torch.cuda.empty_cache()
     # warm-up run: allocates the recurrence vectors and the scalars once
-    h.lanczos_gs(steps=steps // 2, lanctype="OnlyEgs", reortho=0, dtype=np.complex64, want_gs=False)
+    short = steps // 3
+    h.lanczos_gs(steps=short, lanctype="OnlyEgs", reortho=0, dtype=np.complex64, want_gs=False)
     t = []
-    for n in (steps // 2, steps):
+    for n in (short, steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         h.lanczos_gs(steps=n, lanctype="OnlyEgs", reortho=0, dtype=np.complex64, want_gs=False)
         t.append(time.perf_counter() - t0)
-    step_ms = (t[1] - t[0]) / (steps - steps // 2) * 1e3     # set-up and start vector cancel
+    step_ms = (t[1] - t[0]) / (steps - short) * 1e3     # set-up and start vector cancel
     h.close()
     return {"sites": sites, "hv_ms": round(hv_ms, 3), "lanczos_step_ms": round(step_ms, 3),
             "step_over_hv": round(step_ms / hv_ms, 3), "tuning": tune}

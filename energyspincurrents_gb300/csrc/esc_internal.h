@@ -166,6 +166,11 @@ unsigned long long slab_pair_launches();
 // Marks the slab pairs of a pass list (DevPass::pair, ::slab_bits): consecutive passes whose
 // tiles span at most SLAB_MAX_BITS of the N bits together, greedily from the first pass.
 void mark_pairs(std::vector<DevPass>& ps, int N);
+// A pair kernel exists for passes a, b: the specialised one (a.jit_pair), or the ahead-of-time one
+// (512 threads per tile in both, 4096- or 8192-state tiles).
+inline bool pair_launchable(const DevPass& a, const DevPass& b) {
+    return a.jit_pair >= 0 || (a.tb_bits == 9 && b.tb_bits == 9 && (a.Tp == 12 || a.Tp == 13));
+}
 // Words of DevModel::slab_sync for a basis of N sites.
 inline size_t slab_sync_words(int N) { return (size_t)SLAB_CNT0 + (N > 12 ? (size_t)1 << (N - 12) : 1); }
 // Orders the passes of a plan so that consecutive pairs span few bits (planner.cpp); applied

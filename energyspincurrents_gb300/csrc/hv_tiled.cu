@@ -1068,8 +1068,7 @@ unsigned long long slab_pair_launches() { return g_pair_launches.load(); }
 // no pair kernel exists for their shape (the caller then runs the passes one by one).
 static int run_pair(const DevModel& m, const DevPass& a, const DevPass& b, const DevCols& cols, double* dotp,
                     const void* diag, const void* in, void* out, int64_t D, int sms, cudaStream_t s, const int* active) {
-    const bool aot = a.tb_bits == 9 && b.tb_bits == 9 && (a.Tp == 13 || a.Tp == 12);
-    if (!m.slab_sync || (a.jit_pair < 0 && !aot)) return 0;
+    if (!m.slab_sync || !pair_launchable(a, b)) return 0;
     const escdev::PairTab st = make_pair_tab(a, b, m.N, m.slab_sync);
     const escdev::PassTab pa = make_pass_tab(a, m, &cols, nullptr), pb = make_pass_tab(b, m, &cols, dotp);
     ESC_CUDA(cudaMemsetAsync(st.cnt, 0, (size_t)st.nslab * sizeof(unsigned), s));

@@ -39,6 +39,9 @@ std::vector<esc::DevPass> with_pairs(const std::vector<esc::DevPass>& comp, int 
     if (jit && esc::jit_compile(cp, err))
         for (size_t i = 0; i < cp.size(); i++)
             if (comp[i].jit < 0) cp[i].jit = -1;
+    // pairs without a kernel (e.g. the two passes chose different thread counts) run singly
+    for (size_t i = 0; i + 1 < cp.size(); i++)
+        if (cp[i].pair && !esc::pair_launchable(cp[i], cp[i + 1])) cp[i].pair = 0;
     return cp;
 }
 std::vector<esc::DevPass> without_pairs(const std::vector<esc::DevPass>& comp) {
