@@ -546,7 +546,7 @@ struct PairTab {
 };
 
 // item k -> pass (sec = 0: A, 1: B), slab s and tile number t = s 2^inner + (tile in slab)
-__device__ __forceinline__ void pair_item(const PairTab& st, long long k, int& sec, long long& s, long long& t) {
+__host__ __device__ __forceinline__ void pair_item(const PairTab& st, long long k, int& sec, long long& s, long long& t) {
     const long long q = k >> st.inner;
     if (q == 0) {
         sec = 0; s = 0;
